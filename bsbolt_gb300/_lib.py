@@ -1,0 +1,88 @@
+"""ctypes binding of libbsbgpu.so (the C ABI declared in include/bsbgpu.h).
+
+The library is the product path: there is no CPU fallback.  If it is missing
+or cannot be loaded, every call raises ``BsbError`` -- nothing silently
+computes on the host.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libbsbgpu.so")
+
+BSB_OK = 0
+BSB_EINVAL = -1
+BSB_ECUDA = -2
+BSB_ENOMEM = -3
+BSB_EIO = -4
+BSB_ETIMEOUT = -5
+BSB_ETOOLONG = -6
+BSB_ENOINDEX = -7
+
+# every extern "C" symbol include/bsbgpu.h declares
+EXPORTS = (
+    "bsb_ctx_create", "bsb_ctx_destroy", "bsb_last_error", "bsb_strerror", "bsb_ctx_stream",
+    "bsb_extend_batch", "bsb_extend_batch_device", "bsb_sync", "bsb_last_kernel_ms",
+    "bsb_probe_int_peak",
+)
+
+
+class BsbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"bsbgpu error {code}: {msg}")
+        self.code = code
+
+
+class ExtParam(ctypes.Structure):
+    """bsb_ext_param_t"""
+    _fields_ = [("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3),
+                ("o_del", ctypes.c_int32), ("e_del", ctypes.c_int32),
+                ("o_ins", ctypes.c_int32), ("e_ins", ctypes.c_int32),
+                ("zdrop", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libbsbgpu.so and declare its signatures (raises if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise BsbError(BSB_ECUDA, f"{path} is missing: run __graft_entry__.build() first "
+                                  "(the CUDA library is required; there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    P, I64, I32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    L.bsb_ctx_create.argtypes = [I32, ctypes.POINTER(P)]
+    L.bsb_ctx_create.restype = I32
+    L.bsb_ctx_destroy.argtypes = [P]
+    L.bsb_ctx_destroy.restype = None
+    L.bsb_last_error.argtypes = [P]
+    L.bsb_last_error.restype = ctypes.c_char_p
+    L.bsb_strerror.argtypes = [I32]
+    L.bsb_strerror.restype = ctypes.c_char_p
+    L.bsb_ctx_stream.argtypes = [P]
+    L.bsb_ctx_stream.restype = P
+    L.bsb_extend_batch.argtypes = [P, P, P, I64, P, I64, P, P]
+    L.bsb_extend_batch.restype = I32
+    L.bsb_extend_batch_device.argtypes = [P, P, P, I64, P, I64, P, P, P]
+    L.bsb_extend_batch_device.restype = I32
+    L.bsb_sync.argtypes = [P]
+    L.bsb_sync.restype = I32
+    L.bsb_probe_int_peak.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    L.bsb_probe_int_peak.restype = I32
+    L.bsb_last_kernel_ms.argtypes = [P]
+    L.bsb_last_kernel_ms.restype = ctypes.c_float
+    _lib = L
+    return L
+
+
+def check(ctx, rc: int):
+    if rc != 0:
+        L = load()
+        msg = L.bsb_last_error(ctx).decode() if ctx else L.bsb_strerror(rc).decode()
+        raise BsbError(rc, msg or L.bsb_strerror(rc).decode())
+    return rc

@@ -1,0 +1,240 @@
+// bsb_api.cu -- extern "C" boundary of the sm_103a bisulfite seed/extend library.
+//
+// Owns the context (device, stream, events, growable device scratch) and the
+// argument checks that turn the reference's assert()/err_fatal() exits into
+// error codes.
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "bsb_internal.cuh"
+
+int bsb_fail(bsb_ctx *ctx, int code, const char *fmt, ...)
+{
+    if (ctx) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+int bsb_cuda(bsb_ctx *ctx, cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return 0;
+    if (e == cudaErrorMemoryAllocation)
+        return bsb_fail(ctx, BSB_ENOMEM, "%s: %s", what, cudaGetErrorString(e));
+    return bsb_fail(ctx, BSB_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int bsb_ensure(bsb_ctx *ctx, void **buf, size_t *cur, size_t bytes, const char *what)
+{
+    if (*cur >= bytes && *buf) return 0;
+    if (*buf) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return bsb_cuda(ctx, e, what);
+        cudaFree(*buf);
+        *buf = nullptr;
+        *cur = 0;
+    }
+    size_t want = bytes + bytes / 4 + 4096;   // grow with headroom
+    cudaError_t e = cudaMalloc(buf, want);
+    if (e != cudaSuccess) {
+        *buf = nullptr;
+        return bsb_cuda(ctx, e, what);
+    }
+    *cur = want;
+    return 0;
+}
+
+extern "C" {
+
+const char *bsb_strerror(int code)
+{
+    switch (code) {
+    case BSB_OK: return "ok";
+    case BSB_EINVAL: return "invalid argument";
+    case BSB_ECUDA: return "CUDA error";
+    case BSB_ENOMEM: return "out of memory";
+    case BSB_EIO: return "index I/O error";
+    case BSB_ETIMEOUT: return "bounded device wait timed out";
+    case BSB_ETOOLONG: return "sequence too long";
+    case BSB_ENOINDEX: return "no index loaded";
+    default: return "unknown error";
+    }
+}
+
+int bsb_ctx_create(int device, bsb_ctx **out)
+{
+    if (!out) return BSB_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BSB_ECUDA;
+    if (device < 0 || device >= ndev) return BSB_EINVAL;
+    bsb_ctx *ctx = new (std::nothrow) bsb_ctx();
+    if (!ctx) return BSB_ENOMEM;
+    ctx->device = device;
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(device), "cudaSetDevice")) ||
+        (rc = bsb_cuda(ctx, cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device), "sm count")) ||
+        (rc = bsb_cuda(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream")) ||
+        (rc = bsb_cuda(ctx, cudaEventCreate(&ctx->ev0), "event")) ||
+        (rc = bsb_cuda(ctx, cudaEventCreate(&ctx->ev1), "event"))) {
+        bsb_ctx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return BSB_OK;
+}
+
+void bsb_ctx_destroy(bsb_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->d_in) cudaFree(ctx->d_in);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *bsb_last_error(const bsb_ctx *ctx)
+{
+    return ctx ? ctx->err.c_str() : "no context";
+}
+
+void *bsb_ctx_stream(bsb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+float bsb_last_kernel_ms(const bsb_ctx *ctx) { return ctx ? ctx->last_kernel_ms : 0.f; }
+
+}  // extern "C"
+
+static int check_param(bsb_ctx *ctx, const bsb_ext_param_t *param, KswParams *P)
+{
+    if (!param) return bsb_fail(ctx, BSB_EINVAL, "param is NULL");
+    if (param->e_del < 1 || param->e_ins < 1)
+        return bsb_fail(ctx, BSB_EINVAL, "gap extension penalties must be >= 1 (got %d, %d)",
+                        param->e_del, param->e_ins);
+    if (param->o_del < 0 || param->o_ins < 0)
+        return bsb_fail(ctx, BSB_EINVAL, "gap open penalties must be >= 0");
+    if (param->o_del > 65535 || param->o_ins > 65535 || param->e_del > 65535 || param->e_ins > 65535)
+        return bsb_fail(ctx, BSB_EINVAL, "gap penalties must be <= 65535");
+    memcpy(P->mat, param->mat, 25);
+    P->o_del = param->o_del; P->e_del = param->e_del;
+    P->o_ins = param->o_ins; P->e_ins = param->e_ins;
+    P->zdrop = param->zdrop;
+    int mx = 0;
+    for (int i = 0; i < 25; ++i) mx = mx > param->mat[i] ? mx : param->mat[i];
+    P->mat_max = mx;
+    for (int i = 0; i < 25; ++i)
+        if (param->mat[i] > 63 || param->mat[i] < -63)
+            return bsb_fail(ctx, BSB_EINVAL, "scoring matrix entries must lie in [-63, 63]");
+    return 0;
+}
+
+// Host-side validation of a job table (the kernel trusts what passes here).
+static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_t seq_bytes)
+{
+    const int qmax = ksw_max_qlen();
+    for (int64_t i = 0; i < n; ++i) {
+        const bsb_ext_job_t &j = jobs[i];
+        if (j.qlen < 0 || j.tlen < 0 || j.w < 0 || j.flags != 0)
+            return bsb_fail(ctx, BSB_EINVAL, "job %lld: negative length/band or nonzero flags", (long long)i);
+        if (j.h0 <= 0 || j.h0 > (1 << 24))
+            return bsb_fail(ctx, BSB_EINVAL, "job %lld: h0 must be in [1, 2^24] (ksw.c:385 asserts h0 > 0)",
+                            (long long)i);
+        if (j.qlen > qmax)
+            return bsb_fail(ctx, BSB_ETOOLONG, "job %lld: qlen %d exceeds %d", (long long)i, j.qlen, qmax);
+        if (j.qoff < 0 || j.toff < 0 || j.qoff + j.qlen > seq_bytes || j.toff + j.tlen > seq_bytes)
+            return bsb_fail(ctx, BSB_EINVAL, "job %lld: sequence range outside the buffer", (long long)i);
+        if ((int64_t)j.qlen + j.tlen > (1 << 30))
+            return bsb_fail(ctx, BSB_ETOOLONG, "job %lld: sequence too long", (long long)i);
+    }
+    return 0;
+}
+
+extern "C" int bsb_extend_batch_device(bsb_ctx *ctx, const bsb_ext_param_t *param,
+                                       const bsb_ext_job_t *d_jobs, int64_t n_jobs,
+                                       const uint8_t *d_seq, int64_t seq_bytes,
+                                       const int32_t *d_cost, bsb_ext_out_t *d_out, int64_t *d_cells)
+{
+    if (!ctx) return BSB_EINVAL;
+    KswParams P;
+    int rc = check_param(ctx, param, &P);
+    if (rc) return rc;
+    if (n_jobs < 0 || n_jobs > (int64_t)0x7fffffff) return bsb_fail(ctx, BSB_EINVAL, "n_jobs out of range");
+    if (n_jobs == 0) return 0;
+    if (!d_jobs || !d_seq || !d_out) return bsb_fail(ctx, BSB_EINVAL, "NULL buffer");
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->scratch, &ctx->scratch_bytes, ksw_scratch_bytes(n_jobs), "extension scratch")))
+        return rc;
+    cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, d_cost, d_out, d_cells, ctx->scratch,
+                               ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1);
+    ctx->pending_ksw = 1;
+    return bsb_cuda(ctx, e, "extension launch");
+}
+
+extern "C" int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_ext_job_t *jobs,
+                                int64_t n_jobs, const uint8_t *seq, int64_t seq_bytes, bsb_ext_out_t *out,
+                                int64_t *cells_out)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (n_jobs < 0) return bsb_fail(ctx, BSB_EINVAL, "n_jobs < 0");
+    if (n_jobs == 0) return 0;
+    if (!jobs || !seq || !out) return bsb_fail(ctx, BSB_EINVAL, "NULL buffer");
+    KswParams P;
+    int rc = check_param(ctx, param, &P);
+    if (rc) return rc;
+    if ((rc = check_jobs(ctx, jobs, n_jobs, seq_bytes))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+
+    const size_t jb = sizeof(bsb_ext_job_t) * (size_t)n_jobs;
+    const size_t sb = ((size_t)seq_bytes + 255) & ~(size_t)255;
+    const size_t ob = sizeof(bsb_ext_out_t) * (size_t)n_jobs;
+    const size_t cb = cells_out ? sizeof(int64_t) * (size_t)n_jobs : 0;
+    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, jb + sb + 256, "input staging"))) return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, ob + cb + 256, "output staging"))) return rc;
+    char *din = (char *)ctx->d_in;
+    uint8_t *d_seq = (uint8_t *)din;
+    bsb_ext_job_t *d_jobs = (bsb_ext_job_t *)(din + sb);
+    bsb_ext_out_t *d_out = (bsb_ext_out_t *)ctx->d_out;
+    int64_t *d_cells = cells_out ? (int64_t *)((char *)ctx->d_out + ((ob + 255) & ~(size_t)255)) : nullptr;
+
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seq, seq, seq_bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D seq")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_jobs, jobs, jb, cudaMemcpyHostToDevice, ctx->stream), "H2D jobs")))
+        return rc;
+    if ((rc = bsb_extend_batch_device(ctx, param, d_jobs, n_jobs, d_seq, seq_bytes, nullptr, d_out, d_cells)))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream), "D2H out")))
+        return rc;
+    if (cells_out &&
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(cells_out, d_cells, cb, cudaMemcpyDeviceToHost, ctx->stream), "D2H cells")))
+        return rc;
+    return bsb_sync(ctx);
+}
+
+extern "C" int bsb_sync(bsb_ctx *ctx)
+{
+    if (!ctx) return BSB_EINVAL;
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize"))) return rc;
+    if (ctx->pending_ksw) {
+        ctx->pending_ksw = 0;
+        cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1);
+        int rej = 0;
+        if ((rc = bsb_cuda(ctx, cudaMemcpy(&rej, ksw_rejected_counter(ctx->scratch), sizeof(int),
+                                           cudaMemcpyDeviceToHost), "rejected-job counter")))
+            return rc;
+        if (rej) return bsb_fail(ctx, BSB_EINVAL, "%d extension jobs failed the preconditions and were skipped", rej);
+    }
+    return 0;
+}

@@ -1,0 +1,59 @@
+// bsb_internal.cuh -- shared declarations of the sm_103a bisulfite seed/extend library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/bsbgpu.h"
+
+#define BSB_FULL_MASK 0xffffffffu
+
+// Largest query handled by the register-tiled extension kernels: 32 lanes x 32 slots - 1.
+#define BSB_KSW_MAX_QLEN 1023
+
+struct bsb_ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_kernel_ms = 0.f;
+    int pending_ksw = 0;      // an extension batch was launched since the last bsb_sync
+    std::string err;
+
+    // growable device scratch owned by the context
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // staging for the host-buffer entry points
+    void *d_in = nullptr;
+    size_t d_in_bytes = 0;
+    void *d_out = nullptr;
+    size_t d_out_bytes = 0;
+};
+
+// Sets ctx->err and returns code.
+int bsb_fail(bsb_ctx *ctx, int code, const char *fmt, ...);
+// Maps a CUDA error to BSB_ECUDA with a message; returns 0 for cudaSuccess.
+int bsb_cuda(bsb_ctx *ctx, cudaError_t e, const char *what);
+// Ensures *buf holds at least bytes of device memory (grow-only).
+int bsb_ensure(bsb_ctx *ctx, void **buf, size_t *cur, size_t bytes, const char *what);
+
+// Device-side scoring for one extension batch.
+struct KswParams {
+    int8_t mat[25];
+    int o_del, e_del, o_ins, e_ins, zdrop;
+    int mat_max;
+};
+
+// Launches the extension of n jobs (device buffers) on stream, scheduled by
+// tile bin and cost key (d_cost, or the plain bound when NULL).
+// scratch must hold ksw_scratch_bytes(n) bytes.  Returns a cudaError_t.
+size_t ksw_scratch_bytes(int64_t n);
+int ksw_max_qlen();
+// Device word counting the jobs the last launch rejected (precondition failures).
+int *ksw_rejected_counter(void *scratch);
+cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
+                       const uint8_t *d_seq, const int32_t *d_cost, bsb_ext_out_t *d_out,
+                       int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
+                       cudaEvent_t ev0, cudaEvent_t ev1);

@@ -1,0 +1,155 @@
+"""Seeded synthetic inputs for the bisulfite seed/extend path.
+
+No public dataset is used: every workload is generated here from
+``numpy.random.Generator(PCG64(seed))``.  Shapes follow the workloads the
+path is measured on:
+
+* ``ksw_jobs`` -- batched ``ksw_extend2`` jobs: query length U[10,140] in the
+  three-letter converted alphabet (A/G/T ~ 30/20/50 %, 1 % N), target = the
+  query mutated with 1 % substitutions and 0.1 % indels of length 1-5, plus
+  100 nt of flank; 20 % of jobs get an unrelated random target so z-drop and
+  the zero-row exit fire; h0 ~ U[19,100]; w = 100; end bonus 5.
+* ``bs_genome`` / ``bs_reads`` -- a GC-41 % reference with thinned CpG and
+  directional paired-end bisulfite reads (see their docstrings).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# bsb_ext_job_t in include/bsbgpu.h
+JOB_DTYPE = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"),
+                      ("h0", "<i4"), ("w", "<i4"), ("end_bonus", "<i4"), ("flags", "<i4")])
+
+NT4 = np.full(256, 4, np.uint8)
+for _i, _c in enumerate("ACGT"):
+    NT4[ord(_c)] = _i
+    NT4[ord(_c.lower())] = _i
+
+
+def fill_scmat(a: int = 1, b: int = 4) -> np.ndarray:
+    """Scoring matrix of bwa_fill_scmat (bsbolt/External/BWA/bwa.c:169-178): a on the
+    diagonal, -b off it, -1 against N."""
+    mat = np.full((5, 5), -1, np.int8)
+    for i in range(4):
+        for j in range(4):
+            mat[i, j] = a if i == j else -b
+    return mat.reshape(25)
+
+
+def _draw(rng, n, p):
+    """n base codes with probabilities p (resolution 1/1024) via a lookup table."""
+    p = np.asarray(p, float)
+    counts = np.floor(p / p.sum() * 1024 + 0.5).astype(np.int64)
+    counts[np.argmax(counts)] += 1024 - counts.sum()
+    lut = np.repeat(np.arange(len(p), dtype=np.uint8), counts)
+    return lut[rng.integers(0, 1024, n, dtype=np.uint16)]
+
+
+def _mutate(rng, seq, job_of, n_jobs, sub, indel, alphabet_p):
+    """Apply substitutions and indels to a concatenation of per-job sequences.
+
+    Returns (mutated concatenation, per-job lengths).  Deletions never cross a
+    job boundary."""
+    n = len(seq)
+    r = rng.random(n, dtype=np.float32)
+    ins = r < indel / 2
+    dele = (r >= indel / 2) & (r < indel)
+    subm = (r >= indel) & (r < indel + sub)
+    out = seq.copy()
+    if subm.any():
+        k = int(subm.sum())
+        # substitute with a different base drawn from the same alphabet
+        new = _draw(rng, k, alphabet_p[:4])
+        same = new == out[subm]
+        new[same] = (new[same] + 1 + rng.integers(0, 3, int(same.sum()))) % 4
+        out[subm] = new
+    keep = np.ones(n, np.int64)
+    if dele.any():
+        starts = np.nonzero(dele)[0]
+        lens = rng.integers(1, 6, len(starts))
+        # clip at the end of the job the deletion starts in
+        job_end = np.searchsorted(job_of, job_of[starts], side="right")
+        stops = np.minimum(starts + lens, job_end)
+        diff = np.zeros(n + 1, np.int64)
+        np.add.at(diff, starts, 1)
+        np.add.at(diff, stops, -1)
+        keep[np.cumsum(diff)[:n] > 0] = 0
+    ins_len = np.zeros(n, np.int64)
+    if ins.any():
+        ins_len[ins] = rng.integers(1, 6, int(ins.sum()))
+    per = ins_len + keep
+    total = int(per.sum())
+    res = np.empty(total, np.uint8)
+    pos = np.cumsum(per) - per             # start of each source position's output
+    # inserted bases first, then the kept base
+    if ins.any():
+        ipos = np.nonzero(ins_len)[0]
+        idx = np.repeat(pos[ipos], ins_len[ipos]) + (np.arange(int(ins_len[ipos].sum()))
+              - np.repeat(np.cumsum(ins_len[ipos]) - ins_len[ipos], ins_len[ipos]))
+        res[idx] = _draw(rng, len(idx), alphabet_p)
+    kp = keep.astype(bool)
+    res[pos[kp] + ins_len[kp]] = out[kp]
+    lens = np.bincount(job_of, weights=per, minlength=n_jobs).astype(np.int64)
+    return res, lens
+
+
+def ksw_jobs(n_jobs: int, seed: int = 20261203 + 1, qmin: int = 10, qmax: int = 140,
+             flank: int = 100, sub: float = 0.01, indel: float = 0.001,
+             unrelated: float = 0.2, h0_range=(19, 100), w: int = 100, end_bonus: int = 5,
+             chunk: int = 1 << 18):
+    """Batched ksw_extend2 jobs.  Returns (jobs[JOB_DTYPE], seq uint8 buffer).
+
+    Queries and targets are packed back to back in one byte buffer; job i's
+    query is seq[qoff:qoff+qlen] and its target seq[toff:toff+tlen]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.array([0.30, 0.0, 0.20, 0.50, 0.01])
+    p = p / p.sum()
+    jobs_all, parts, base = [], [], 0
+    for c0 in range(0, n_jobs, chunk):
+        m = min(chunk, n_jobs - c0)
+        qlen = rng.integers(qmin, qmax + 1, m).astype(np.int64)
+        qtot = int(qlen.sum())
+        q = _draw(rng, qtot, p)
+        job_of = np.repeat(np.arange(m), qlen)
+        mut, mlen = _mutate(rng, q, job_of, m, sub, indel, p)
+        unrel = rng.random(m) < unrelated
+        # target = mutated query + flank; unrelated jobs get random bases instead
+        tlen = mlen + flank
+        tlen[unrel] = qlen[unrel] + flank
+        t = np.empty(int(tlen.sum()), np.uint8)
+        toff_local = np.cumsum(tlen) - tlen
+        moff = np.cumsum(mlen) - mlen
+        rel = np.nonzero(~unrel)[0]
+        body = np.zeros(len(t), bool)
+        if len(rel):
+            # gather the mutated bodies of related jobs to the front of their targets
+            lens_r = mlen[rel]
+            within = np.arange(int(lens_r.sum())) - np.repeat(np.cumsum(lens_r) - lens_r, lens_r)
+            dst = np.repeat(toff_local[rel], lens_r) + within
+            t[dst] = mut[np.repeat(moff[rel], lens_r) + within]
+            body[dst] = True
+        # everything not yet written (flanks and unrelated bodies) is random
+        nfill = int((~body).sum())
+        t[~body] = _draw(rng, nfill, p)
+        qoff_local = np.cumsum(qlen) - qlen
+        js = np.zeros(m, JOB_DTYPE)
+        js["qoff"] = base + qoff_local
+        js["toff"] = base + qtot + toff_local
+        js["qlen"] = qlen
+        js["tlen"] = tlen
+        js["h0"] = rng.integers(h0_range[0], h0_range[1] + 1, m)
+        js["w"] = w
+        js["end_bonus"] = end_bonus
+        jobs_all.append(js)
+        parts.append(q)
+        parts.append(t)
+        base += qtot + len(t)
+    return np.concatenate(jobs_all), np.concatenate(parts)
+
+
+def cells_upper_bound(jobs: np.ndarray) -> np.ndarray:
+    """The plain schedule's cost bound: rows x band columns, qlen x min(tlen, qlen+w)."""
+    q = jobs["qlen"].astype(np.int64)
+    t = jobs["tlen"].astype(np.int64)
+    w = jobs["w"].astype(np.int64)
+    return q * np.minimum(t, q + w)
