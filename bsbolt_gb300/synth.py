@@ -153,3 +153,86 @@ def cells_upper_bound(jobs: np.ndarray) -> np.ndarray:
     t = jobs["tlen"].astype(np.int64)
     w = jobs["w"].astype(np.int64)
     return q * np.minimum(t, q + w)
+
+
+# ---------------------------------------------------------------- genomes / reads
+
+COMP = np.array([3, 2, 1, 0, 4], np.uint8)
+
+
+def bs_genome(n_contigs: int = 4, contig_len: int = 500_000, gc: float = 0.41,
+              cpg_frac: float = 0.01, seed: int = 20261203):
+    """i.i.d. contigs at the given GC with CpG thinned to ``cpg_frac`` of dinucleotides.
+
+    Returns a list of (name, codes uint8 0..3)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    at = (1 - gc) / 2
+    p = np.array([at, gc / 2, gc / 2, at])
+    contigs = []
+    expect = (gc / 2) ** 2
+    keep = min(1.0, cpg_frac / expect)
+    for k in range(n_contigs):
+        s = _draw(rng, contig_len, p)
+        cg = np.nonzero((s[:-1] == 1) & (s[1:] == 2))[0]
+        drop = cg[rng.random(len(cg)) >= keep]
+        s[drop] = 3                              # thinned CpG: C -> T
+        contigs.append((f"chr{k + 1}", s))
+    return contigs
+
+
+def write_fasta(path: str, contigs, width: int = 60) -> None:
+    letters = np.frombuffer(b"ACGTN", np.uint8)
+    with open(path, "w") as f:
+        for name, codes in contigs:
+            f.write(f">{name}\n")
+            txt = letters[codes].tobytes().decode()
+            for i in range(0, len(txt), width):
+                f.write(txt[i:i + width] + "\n")
+
+
+def bs_reads_pe(contigs, n_pairs: int, read_len: int = 100, insert_mean: float = 300,
+                insert_sd: float = 30, meth_cpg: float = 0.8, meth_ch: float = 0.01,
+                conversion: float = 0.995, err: float = 0.005, seed: int = 20261203):
+    """Directional paired-end bisulfite reads, drawn uniformly from both strands.
+
+    Returns (r1, r2): lists of uint8 code arrays (A0 C1 G2 T3), original bases
+    as sequenced, before the aligner's in-silico conversion."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lens = np.array([len(c[1]) for c in contigs], np.float64)
+    which = rng.choice(len(contigs), size=n_pairs, p=lens / lens.sum())
+    ins = np.maximum(np.round(rng.normal(insert_mean, insert_sd, n_pairs)).astype(np.int64), read_len)
+    strand = rng.random(n_pairs) < 0.5           # True: original bottom strand
+    r1s, r2s = [], []
+    for i in range(n_pairs):
+        g = contigs[which[i]][1]
+        L = int(min(ins[i], len(g)))
+        st = int(rng.integers(0, len(g) - L + 1))
+        frag = g[st:st + L].copy()
+        if strand[i]:
+            frag = COMP[frag[::-1]]
+        # methylation and bisulfite conversion on the sequenced strand
+        isc = frag == 1
+        nxt = np.concatenate([frag[1:], [4]])
+        cpg = isc & (nxt == 2)
+        meth = np.where(cpg, rng.random(L) < meth_cpg, rng.random(L) < meth_ch)
+        conv = isc & ~meth & (rng.random(L) < conversion)
+        frag[conv] = 3
+        r1 = frag[:read_len].copy()
+        r2 = COMP[frag[::-1][:read_len]].copy()
+        for r in (r1, r2):
+            e = rng.random(len(r)) < err
+            r[e] = (r[e] + rng.integers(1, 4, int(e.sum()))) % 4
+        r1s.append(r1)
+        r2s.append(r2)
+    return r1s, r2s
+
+
+def bs_convert(read: np.ndarray, g2a: bool) -> np.ndarray:
+    """In-silico conversion of bsConversion (bs_helpers.cpp:18-31): C->T for read 1,
+    G->A for read 2."""
+    r = read.copy()
+    if g2a:
+        r[r == 2] = 0
+    else:
+        r[r == 1] = 3
+    return r

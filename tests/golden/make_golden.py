@@ -27,6 +27,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 from bsbolt_gb300 import synth  # noqa: E402
 
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_data import GENOME, OPTS, golden_genome, golden_reads  # noqa: E402
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
 
@@ -137,7 +140,110 @@ def sha256(fn):
     return h.hexdigest()
 
 
+# ------------------------------------------------------------------ index
+
+def make_index(td):
+    fa = os.path.join(td, "ref.fa")
+    synth.write_fasta(fa, golden_genome())
+    prefix = os.path.join(td, "ref")
+    subprocess.check_call([os.path.join(REF, "bwa"), "index", "-a", "bwtsw", "-p", prefix, fa],
+                          stderr=subprocess.DEVNULL)
+    sums = {ext: sha256(prefix + "." + ext) for ext in ("pac", "opac", "ann", "amb", "bwt", "sa")}
+    import json
+    fn = os.path.join(HERE, "index_sha256.json")
+    with open(fn, "w") as f:
+        json.dump({"genome": GENOME, "files": sums}, f, indent=1)
+    print(fn)
+    return prefix
+
+
+# ------------------------------------------------------------------ reads
+
+def parse_dump(prefix, n_reads):
+    """Parse the binary streams golden_dump writes (see oracle/golden_dump.c)."""
+    out = {}
+    b = open(prefix + ".smem.bin", "rb").read()
+    off, smem, smem_off = 0, [], [0]
+    for _ in range(n_reads):
+        r, n = np.frombuffer(b, np.int32, 2, off); off += 8
+        smem.append(np.frombuffer(b, np.uint64, 4 * n, off).reshape(n, 4)); off += 32 * n
+        smem_off.append(smem_off[-1] + n)
+    out["smem"] = np.concatenate(smem) if smem else np.zeros((0, 4), np.uint64)
+    out["smem_off"] = np.array(smem_off, np.int64)
+    b = open(prefix + ".chain.bin", "rb").read()
+    off = 0
+    seed_dt = np.dtype([("rbeg", "<i8"), ("qbeg", "<i4"), ("len", "<i4"), ("score", "<i4"), ("pad", "<i4")])
+    for stage in ("chain0", "chain1"):
+        out[stage + "_rows"], out[stage + "_seeds"], out[stage + "_off"] = [], [], [0]
+    for _ in range(n_reads):
+        for stage in ("chain0", "chain1"):
+            r, n = np.frombuffer(b, np.int32, 2, off); off += 8
+            for _c in range(n):
+                h = np.frombuffer(b, np.int32, 5, off); off += 20
+                pos = np.frombuffer(b, np.int64, 1, off)[0]; off += 8
+                ns = int(h[0])
+                seeds = np.frombuffer(b, seed_dt, ns, off); off += 24 * ns
+                out[stage + "_rows"].append([h[0], h[1], h[2], h[3], h[4], pos, len(out[stage + "_seeds"])])
+                out[stage + "_seeds"].extend(seeds.tolist())
+            out[stage + "_off"].append(len(out[stage + "_rows"]))
+    for stage in ("chain0", "chain1"):
+        out[stage + "_rows"] = np.array(out[stage + "_rows"], np.int64).reshape(-1, 7)
+        out[stage + "_seeds"] = np.array(out[stage + "_seeds"], np.int64).reshape(-1, 5)[:, :4]
+        out[stage + "_off"] = np.array(out[stage + "_off"], np.int64)
+    b = open(prefix + ".reg.bin", "rb").read()
+    off, regs, reg_off = 0, [], [0]
+    for _ in range(n_reads):
+        r, n = np.frombuffer(b, np.int32, 2, off); off += 8
+        for _k in range(n):
+            rr = np.frombuffer(b, np.int64, 2, off); off += 16
+            v = np.frombuffer(b, np.int32, 9, off); off += 36
+            fr = np.frombuffer(b, np.float32, 1, off)[0]; off += 4
+            regs.append(list(rr) + list(v[:8]) + [int(np.float32(fr).view(np.int32))])
+        reg_off.append(len(regs))
+    out["regs"] = np.array(regs, np.int64).reshape(-1, 11)
+    out["reg_off"] = np.array(reg_off, np.int64)
+    b = open(prefix + ".ksw.bin", "rb").read()
+    off, kh, kr, kseq, koff = 0, [], [], [], [0]
+    while off < len(b):
+        h = np.frombuffer(b, np.int32, 10, off); off += 40
+        res = np.frombuffer(b, np.int32, 6, off); off += 24
+        q = np.frombuffer(b, np.uint8, h[1], off); off += h[1]
+        t = np.frombuffer(b, np.uint8, h[2], off); off += h[2]
+        kh.append(h[:7]); kr.append(res); kseq.append(q); kseq.append(t)
+        koff.append(koff[-1] + h[1] + h[2])
+    out["ksw_hdr"] = np.array(kh, np.int32).reshape(-1, 7)
+    out["ksw_out"] = np.array(kr, np.int32).reshape(-1, 6)
+    out["ksw_seq"] = np.concatenate(kseq) if kseq else np.zeros(0, np.uint8)
+    out["ksw_seq_off"] = np.array(koff, np.int64)
+    return out
+
+
+def make_reads(td, prefix):
+    reads = golden_reads()
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    fin = os.path.join(td, "reads.bin")
+    with open(fin, "wb") as f:
+        f.write(np.array([len(reads), offs[-1]], np.int64).tobytes())
+        f.write(offs.tobytes())
+        f.write(np.concatenate(reads).astype(np.uint8).tobytes())
+    for name, o in OPTS.items():
+        fo = os.path.join(td, f"opt_{name}.bin")
+        np.array(o, np.int32).tofile(fo)
+        outp = os.path.join(td, f"dump_{name}")
+        subprocess.check_call([os.path.join(REF, "golden_dump"), "reads", prefix, fin, outp, fo])
+        d = parse_dump(outp, len(reads))
+        fn = os.path.join(HERE, f"reads_{name}.npz")
+        np.savez_compressed(fn, reads=np.concatenate(reads), read_off=offs, opts=np.array(o, np.int32), **d)
+        print(fn, os.path.getsize(fn), "smem", len(d["smem"]), "regs", len(d["regs"]), "ksw", len(d["ksw_out"]))
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["ksw"]
     if "ksw" in what:
         make_ksw()
+    if "index" in what or "reads" in what:
+        with tempfile.TemporaryDirectory() as td:
+            prefix = make_index(td)
+            if "reads" in what:
+                make_reads(td, prefix)
