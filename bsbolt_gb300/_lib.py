@@ -26,6 +26,8 @@ EXPORTS = (
     "bsb_ctx_create", "bsb_ctx_destroy", "bsb_last_error", "bsb_strerror", "bsb_ctx_stream",
     "bsb_extend_batch", "bsb_extend_batch_device", "bsb_sync", "bsb_last_kernel_ms",
     "bsb_probe_int_peak",
+    "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
+    "bsb_sa_batch", "bsb_sa_batch_device",
 )
 
 
@@ -41,6 +43,21 @@ class ExtParam(ctypes.Structure):
                 ("o_del", ctypes.c_int32), ("e_del", ctypes.c_int32),
                 ("o_ins", ctypes.c_int32), ("e_ins", ctypes.c_int32),
                 ("zdrop", ctypes.c_int32)]
+
+
+class SeedOpt(ctypes.Structure):
+    """bsb_seed_opt_t"""
+    _fields_ = [("min_seed_len", ctypes.c_int32), ("split_factor", ctypes.c_float),
+                ("split_width", ctypes.c_int32), ("max_mem_intv", ctypes.c_int32)]
+
+
+class IndexView(ctypes.Structure):
+    """bsb_index_view_t"""
+    _fields_ = [("primary", ctypes.c_uint64), ("L2", ctypes.c_uint64 * 5),
+                ("bwt", ctypes.c_void_p), ("bwt_size", ctypes.c_uint64),
+                ("sa", ctypes.c_void_p), ("n_sa", ctypes.c_uint64),
+                ("sa_intv", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("pac", ctypes.c_void_p), ("l_pac", ctypes.c_int64)]
 
 
 _lib = None
@@ -74,6 +91,18 @@ def load(path: str = LIB_PATH):
     L.bsb_sync.restype = I32
     L.bsb_probe_int_peak.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     L.bsb_probe_int_peak.restype = I32
+    L.bsb_index_upload.argtypes = [P, P]
+    L.bsb_index_upload.restype = I32
+    L.bsb_index_load.argtypes = [P, ctypes.c_char_p]
+    L.bsb_index_load.restype = I32
+    L.bsb_seed_batch.argtypes = [P, P, ctypes.c_int32, P, P, P, I64, P]
+    L.bsb_seed_batch.restype = I32
+    L.bsb_seed_batch_device.argtypes = [P, P, ctypes.c_int32, P, P, I64, ctypes.c_int32, P, P]
+    L.bsb_seed_batch_device.restype = I32
+    L.bsb_sa_batch.argtypes = [P, P, I64, P]
+    L.bsb_sa_batch.restype = I32
+    L.bsb_sa_batch_device.argtypes = [P, P, I64, P]
+    L.bsb_sa_batch_device.restype = I32
     L.bsb_last_kernel_ms.argtypes = [P]
     L.bsb_last_kernel_ms.restype = ctypes.c_float
     _lib = L

@@ -100,6 +100,8 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_in) cudaFree(ctx->d_in);
     if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->seed_scratch) cudaFree(ctx->seed_scratch);
+    bsb_index_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -148,8 +150,8 @@ static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_
         const bsb_ext_job_t &j = jobs[i];
         if (j.qlen < 0 || j.tlen < 0 || j.w < 0 || j.flags != 0)
             return bsb_fail(ctx, BSB_EINVAL, "job %lld: negative length/band or nonzero flags", (long long)i);
-        if (j.h0 <= 0 || j.h0 > (1 << 24))
-            return bsb_fail(ctx, BSB_EINVAL, "job %lld: h0 must be in [1, 2^24] (ksw.c:385 asserts h0 > 0)",
+        if (j.h0 <= 0 || j.h0 > (1 << 20))
+            return bsb_fail(ctx, BSB_EINVAL, "job %lld: h0 must be in [1, 2^20] (ksw.c:385 asserts h0 > 0)",
                             (long long)i);
         if (j.qlen > qmax)
             return bsb_fail(ctx, BSB_ETOOLONG, "job %lld: qlen %d exceeds %d", (long long)i, j.qlen, qmax);

@@ -1,0 +1,262 @@
+// bsb_index.cu -- device-resident FM-index and the seeding / SA-lookup entry points.
+//
+// The index arrays are uploaded once per context in the reference's own
+// layout (64-byte occurrence blocks, uint64 sampled SA, 2-bit pac), so the
+// BWA driver can hand over what bwa_idx_load already read (bwa.c:363-524)
+// or the library can read the files itself (bwt_restore_bwt / bwt_restore_sa,
+// bwt.c:420-457).
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "bsb_internal.cuh"
+#include "fm_index.cuh"
+
+size_t seed_scratch_bytes(int n_threads, int max_len);
+size_t seed_padded_entries(int64_t total_bases, int n_reads);
+int seed_threads(int n_sm, int max_len);
+cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
+                        int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
+                        void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
+                        void *d_lists, int *d_ctrl, int n_sm, cudaStream_t st);
+cudaError_t sa_launch(const DevFM &F, const uint64_t *d_rows, int64_t n, uint64_t *d_pos, int n_sm, cudaStream_t st);
+
+void bsb_index_release(bsb_ctx *ctx)
+{
+    if (ctx->idx_bwt) cudaFree(ctx->idx_bwt);
+    if (ctx->idx_sa) cudaFree(ctx->idx_sa);
+    if (ctx->idx_pac) cudaFree(ctx->idx_pac);
+    ctx->idx_bwt = ctx->idx_sa = ctx->idx_pac = nullptr;
+    ctx->has_index = 0;
+}
+
+static DevFM dev_fm(const bsb_ctx *ctx)
+{
+    DevFM F;
+    F.blk = (const uint4 *)ctx->idx_bwt;
+    F.sa = (const uint64_t *)ctx->idx_sa;
+    F.primary = ctx->primary;
+    F.seq_len = ctx->seq_len;
+    for (int i = 0; i < 5; ++i) F.L2[i] = ctx->L2[i];
+    int sh = 0;
+    while ((1 << sh) < ctx->sa_intv) ++sh;
+    F.sa_shift = sh;
+    return F;
+}
+
+extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!v || !v->bwt || !v->sa) return bsb_fail(ctx, BSB_EINVAL, "index view is incomplete");
+    if (v->sa_intv < 1 || (v->sa_intv & (v->sa_intv - 1)))
+        return bsb_fail(ctx, BSB_EINVAL, "SA sample interval %d is not a power of 2", v->sa_intv);
+    const uint64_t seq_len = v->L2[4];
+    const uint64_t n_blocks = (seq_len + 127) / 128 + 1;
+    if (v->L2[0] != 0 || v->primary > seq_len || v->bwt_size < n_blocks * 16 - 8 - 8)
+        return bsb_fail(ctx, BSB_EIO, "inconsistent BWT header (seq_len %llu, %llu words)",
+                        (unsigned long long)seq_len, (unsigned long long)v->bwt_size);
+    if (v->n_sa != (seq_len + v->sa_intv) / v->sa_intv)
+        return bsb_fail(ctx, BSB_EIO, "SA length %llu does not match seq_len", (unsigned long long)v->n_sa);
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    bsb_index_release(ctx);
+    // the occurrence array is padded to whole 64-byte blocks so every block load stays inside it
+    const size_t bwt_bytes = n_blocks * 64;
+    if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_bwt, bwt_bytes), "index: occurrence array"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ctx->idx_bwt, 0, bwt_bytes, ctx->stream), "index memset"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_bwt, v->bwt, v->bwt_size * 4, cudaMemcpyHostToDevice, ctx->stream),
+                       "index: occurrence upload")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_sa, v->n_sa * 8), "index: suffix array"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_sa, v->sa, v->n_sa * 8, cudaMemcpyHostToDevice, ctx->stream),
+                       "index: SA upload")))
+        return rc;
+    if (v->pac && v->l_pac > 0) {
+        const size_t pb = (size_t)(v->l_pac + 3) / 4;
+        if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_pac, pb + 64), "index: pac"))) return rc;
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_pac, v->pac, pb, cudaMemcpyHostToDevice, ctx->stream),
+                           "index: pac upload")))
+            return rc;
+    }
+    ctx->primary = v->primary;
+    for (int i = 0; i < 5; ++i) ctx->L2[i] = v->L2[i];
+    ctx->seq_len = seq_len;
+    ctx->sa_intv = v->sa_intv;
+    ctx->n_sa = v->n_sa;
+    ctx->l_pac = v->l_pac;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "index upload"))) return rc;
+    ctx->has_index = 1;
+    return 0;
+}
+
+static bool read_all(const char *fn, std::vector<char> &buf)
+{
+    FILE *fp = fopen(fn, "rb");
+    if (!fp) return false;
+    fseek(fp, 0, SEEK_END);
+    long n = ftell(fp);
+    fseek(fp, 0, SEEK_SET);
+    if (n < 0) { fclose(fp); return false; }
+    buf.resize((size_t)n);
+    bool ok = n == 0 || fread(buf.data(), 1, (size_t)n, fp) == (size_t)n;
+    fclose(fp);
+    return ok;
+}
+
+extern "C" int bsb_index_load(bsb_ctx *ctx, const char *prefix)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!prefix) return bsb_fail(ctx, BSB_EINVAL, "prefix is NULL");
+    std::string p(prefix);
+    std::vector<char> bw, sa, pac, ann;
+    if (!read_all((p + ".bwt").c_str(), bw) || bw.size() < 40 + 4)
+        return bsb_fail(ctx, BSB_EIO, "cannot read %s.bwt", prefix);
+    if (!read_all((p + ".sa").c_str(), sa) || sa.size() < 56)
+        return bsb_fail(ctx, BSB_EIO, "cannot read %s.sa", prefix);
+    bsb_index_view_t v;
+    memset(&v, 0, sizeof v);
+    uint64_t h[5];
+    memcpy(h, bw.data(), 40);
+    v.primary = h[0];
+    v.L2[0] = 0;
+    for (int i = 1; i < 5; ++i) v.L2[i] = h[i];
+    v.bwt = (const uint32_t *)(bw.data() + 40);
+    v.bwt_size = (bw.size() - 40) / 4;
+    uint64_t sh[7];
+    memcpy(sh, sa.data(), 56);
+    if (sh[0] != v.primary) return bsb_fail(ctx, BSB_EIO, "SA-BWT inconsistency: primary");
+    if (sh[6] != v.L2[4]) return bsb_fail(ctx, BSB_EIO, "SA-BWT inconsistency: seq_len");
+    v.sa_intv = (int32_t)sh[5];
+    if (v.sa_intv < 1) return bsb_fail(ctx, BSB_EIO, "bad SA interval");
+    v.n_sa = (v.L2[4] + v.sa_intv) / v.sa_intv;
+    if ((sa.size() - 56) / 8 != v.n_sa - 1) return bsb_fail(ctx, BSB_EIO, "short .sa file");
+    std::vector<uint64_t> sav(v.n_sa);
+    sav[0] = (uint64_t)-1;
+    memcpy(sav.data() + 1, sa.data() + 56, (v.n_sa - 1) * 8);
+    v.sa = sav.data();
+    if (read_all((p + ".ann").c_str(), ann) && !ann.empty()) {
+        long long lp = 0;
+        if (sscanf(ann.data(), "%lld", &lp) == 1 && read_all((p + ".pac").c_str(), pac) &&
+            pac.size() >= (size_t)(lp + 3) / 4) {
+            v.l_pac = lp;
+            v.pac = (const uint8_t *)pac.data();
+        }
+    }
+    return bsb_index_upload(ctx, &v);
+}
+
+extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *d_seqs,
+                                     const int64_t *d_offs, int64_t total_bases, int32_t max_len,
+                                     bsb_intv_t *d_out, int64_t *d_out_off)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
+    if (!opt || n_reads < 0 || max_len < 0 || total_bases < 0) return bsb_fail(ctx, BSB_EINVAL, "bad seed arguments");
+    if (opt->min_seed_len < 1 || opt->split_width < 0)
+        return bsb_fail(ctx, BSB_EINVAL, "bad seeding options");
+    if (n_reads == 0) return 0;
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    const size_t padded = seed_padded_entries(total_bases, n_reads) * sizeof(DevIntv);
+    if (max_len > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "max_len %d > %d", max_len, BSB_SEED_MAX_LEN);
+    const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len), max_len);
+    const size_t need = padded + lists + 256 * 4 + sizeof(int) * ((size_t)n_reads + 64);
+    if ((rc = bsb_ensure(ctx, &ctx->seed_scratch, &ctx->seed_scratch_bytes, need, "seed scratch"))) return rc;
+    char *s = (char *)ctx->seed_scratch;
+    void *d_padded = s;
+    void *d_lists = s + ((padded + 255) & ~(size_t)255);
+    int *d_count = (int *)((char *)d_lists + ((lists + 255) & ~(size_t)255));
+    int *d_ctrl = d_count + ((n_reads + 63) & ~63);
+    const DevFM F = dev_fm(ctx);
+    cudaError_t e = seed_launch(F, opt->min_seed_len, opt->split_factor, opt->split_width, opt->max_mem_intv, n_reads,
+                                d_seqs, d_offs, max_len, d_padded, d_count, d_out_off, d_out, d_lists, d_ctrl,
+                                ctx->n_sm, ctx->stream);
+    ctx->seed_ctrl = d_ctrl;
+    return bsb_cuda(ctx, e, "seed launch");
+}
+
+extern "C" int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *seqs,
+                              const int64_t *offs, bsb_intv_t *out, int64_t max_out, int64_t *out_off)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
+    if (!opt || !offs || n_reads < 0 || (n_reads > 0 && (!seqs || !out || !out_off)))
+        return bsb_fail(ctx, BSB_EINVAL, "NULL argument");
+    if (n_reads == 0) {
+        if (out_off) out_off[0] = 0;
+        return 0;
+    }
+    int max_len = 0;
+    for (int r = 0; r < n_reads; ++r) {
+        const int64_t l = offs[r + 1] - offs[r];
+        if (l < 0) return bsb_fail(ctx, BSB_EINVAL, "read %d: negative length", r);
+        if (l > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld > %d", r, (long long)l, BSB_SEED_MAX_LEN);
+        if (l > max_len) max_len = (int)l;
+    }
+    const int64_t total = offs[n_reads] - offs[0];
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    const size_t off_b = sizeof(int64_t) * ((size_t)n_reads + 1);
+    const size_t seq_b = ((size_t)total + 255) & ~(size_t)255;
+    const size_t out_b = seed_padded_entries(total, n_reads) * sizeof(bsb_intv_t);
+    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, seq_b + 2 * off_b + 512, "seed input staging"))) return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, out_b + 256, "seed output staging"))) return rc;
+    uint8_t *d_seqs = (uint8_t *)ctx->d_in;
+    int64_t *d_offs = (int64_t *)((char *)ctx->d_in + seq_b);
+    int64_t *d_out_off = (int64_t *)((char *)d_offs + ((off_b + 255) & ~(size_t)255));
+    // reads are uploaded relative to offs[0]
+    std::vector<int64_t> rel(n_reads + 1);
+    for (int r = 0; r <= n_reads; ++r) rel[r] = offs[r] - offs[0];
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seqs, seqs + offs[0], total, cudaMemcpyHostToDevice, ctx->stream), "H2D reads")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_offs, rel.data(), off_b, cudaMemcpyHostToDevice, ctx->stream), "H2D offsets")))
+        return rc;
+    if ((rc = bsb_seed_batch_device(ctx, opt, n_reads, d_seqs, d_offs, total, max_len, (bsb_intv_t *)ctx->d_out, d_out_off)))
+        return rc;
+    int ctrl[2] = {0, 0};
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out_off, d_out_off, off_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H offsets")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream), "D2H ctrl")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seed batch"))) return rc;
+    if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
+    if (out_off[n_reads] > max_out)
+        return bsb_fail(ctx, BSB_EINVAL, "%lld seeds do not fit max_out %lld", (long long)out_off[n_reads], (long long)max_out);
+    if (out_off[n_reads] > 0 &&
+        (rc = bsb_cuda(ctx, cudaMemcpy(out, ctx->d_out, sizeof(bsb_intv_t) * out_off[n_reads], cudaMemcpyDeviceToHost), "D2H seeds")))
+        return rc;
+    return 0;
+}
+
+extern "C" int bsb_sa_batch(bsb_ctx *ctx, const uint64_t *rows, int64_t n, uint64_t *pos)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
+    if (n < 0 || (n > 0 && (!rows || !pos))) return bsb_fail(ctx, BSB_EINVAL, "bad SA arguments");
+    if (n == 0) return 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (rows[i] > ctx->seq_len) return bsb_fail(ctx, BSB_EINVAL, "row %lld beyond seq_len", (long long)i);
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, 8 * (size_t)n + 256, "SA staging"))) return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, 8 * (size_t)n + 256, "SA staging"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->d_in, rows, 8 * n, cudaMemcpyHostToDevice, ctx->stream), "H2D rows")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, sa_launch(dev_fm(ctx), (const uint64_t *)ctx->d_in, n, (uint64_t *)ctx->d_out, ctx->n_sm, ctx->stream),
+                       "SA launch")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(pos, ctx->d_out, 8 * n, cudaMemcpyDeviceToHost, ctx->stream), "D2H SA")))
+        return rc;
+    return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "SA batch");
+}
+
+extern "C" int bsb_sa_batch_device(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
+    if (n < 0) return bsb_fail(ctx, BSB_EINVAL, "bad SA arguments");
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    return bsb_cuda(ctx, sa_launch(dev_fm(ctx), d_rows, n, d_pos, ctx->n_sm, ctx->stream), "SA launch");
+}

@@ -10,8 +10,8 @@
 
 #define BSB_FULL_MASK 0xffffffffu
 
-// Largest query handled by the register-tiled extension kernels: 32 lanes x 32 slots - 1.
-#define BSB_KSW_MAX_QLEN 1023
+// Longest read the seeding kernels accept (bounds the per-thread interval lists).
+#define BSB_SEED_MAX_LEN 1024
 
 struct bsb_ctx {
     int device = 0;
@@ -30,7 +30,21 @@ struct bsb_ctx {
     size_t d_in_bytes = 0;
     void *d_out = nullptr;
     size_t d_out_bytes = 0;
+
+    // device-resident FM-index (reference layout) and its scalars
+    int has_index = 0;
+    void *idx_bwt = nullptr, *idx_sa = nullptr, *idx_pac = nullptr;
+    uint64_t primary = 0, seq_len = 0, n_sa = 0;
+    uint64_t L2[5] = {0, 0, 0, 0, 0};
+    int sa_intv = 0;
+    int64_t l_pac = 0;
+    // seeding scratch (padded per-read seed lists, interval lists, counters)
+    void *seed_scratch = nullptr;
+    size_t seed_scratch_bytes = 0;
+    int *seed_ctrl = nullptr;
 };
+
+void bsb_index_release(bsb_ctx *ctx);
 
 // Sets ctx->err and returns code.
 int bsb_fail(bsb_ctx *ctx, int code, const char *fmt, ...);

@@ -51,12 +51,31 @@ __host__ __device__ inline int tile_bin(int qlen)
     return -1;
 }
 
-__device__ __forceinline__ int sext8(uint32_t x, int shift)
+// Sign-extended byte of x chosen by a prmt selector (bit 3 of each selector
+// nibble replicates the sign of the chosen byte, PTX ISA prmt.b32 default mode).
+__device__ __forceinline__ int prmt_sext(uint32_t x, uint32_t sel)
 {
-    return (int)(int8_t)(uint8_t)(x >> shift);
+    uint32_t r;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "r"(sel));
+    return (int)r;
+}
+
+__device__ __forceinline__ uint32_t sext_selector(int byte)
+{
+    const uint32_t b = (uint32_t)byte, r = b | 8u;
+    return b | r << 4 | r << 8 | r << 12;
 }
 
 // Extends one job with the calling warp.  All control values are warp-uniform.
+//
+// Register state per lane, columns j = lane*C + s:
+//   Hs[s] = eh[j].h = H(i-1, j-1),  Es[s] = eh[j].e = E(i, j)   (ksw.c:376-378)
+// Invariant: every column left of the band (j < beg) holds H = E = 0.  The
+// reference never reads those cells again (beg only grows), and with them at
+// zero the F scan and the row maximum need no left-edge masks: a dead column
+// has M = 0, T = 0, V = e_ins*(j+1), F = 0 and H = 0.  The shrink step only
+// moves beg over cells that are already zero; when the band edge i-w moves
+// beg instead, the cells it passes are zeroed explicitly.
 template <int C>
 __device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t &jb,
                                         const uint8_t *__restrict__ seq, int lane,
@@ -117,7 +136,12 @@ __device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t 
             tnext = ti < tlen ? t[ti] : 4u;
         }
         // band of this row (ksw.c:416-419)
-        if (beg < i - w) beg = i - w;
+        if (beg < i - w) {
+            beg = i - w;
+#pragma unroll
+            for (int s = 0; s < C; ++s)
+                if (base + s < beg) Hs[s] = 0, Es[s] = 0;
+        }
         if (end > i + w + 1) end = i + w + 1;
         if (end > qlen) end = qlen;
         // H(i,-1) (ksw.c:421-424)
@@ -133,22 +157,20 @@ __device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t 
             break;
         }
 
-        // ---- pass 1: M, next-row E, and the F-scan operand V per column
+        // ---- pass 1: M, next-row E, and the F-scan operand V = T(j) + e_ins*(j+1)
         int Mv[C], En[C], Pf[C];
         int run = 0;
         if (tc < 4) {
-            const int sh = tc * 8;
+            const uint32_t sel = sext_selector(tc);
 #pragma unroll
             for (int s = 0; s < C; ++s) {
                 const int j = base + s;
-                const bool inb = j >= beg && j < end;
-                const int sc = sext8(prof[s], sh);
+                const int sc = prmt_sext(prof[s], sel);
                 const int Hp = Hs[s];
                 const int M = Hp ? Hp + sc : 0;
-                const int Ti = max(M - oe_ins, 0);
-                En[s] = max(Es[s] - e_del, max(M - oe_del, 0));
-                const int V = inb ? Ti + e_ins * (j + 1) : 0;
-                run = max(run, V);
+                const int Ti = __viaddmax_s32(M, -oe_ins, 0);
+                En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
+                run = max(run, Ti + e_ins * (j + 1));
                 Pf[s] = run;
                 Mv[s] = M;
             }
@@ -156,66 +178,55 @@ __device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t 
 #pragma unroll
             for (int s = 0; s < C; ++s) {
                 const int j = base + s;
-                const bool inb = j >= beg && j < end;
-                const int sc = sext8(profN[s >> 2], (s & 3) * 8);
+                const int sc = prmt_sext(profN[s >> 2], sext_selector(s & 3));
                 const int Hp = Hs[s];
                 const int M = Hp ? Hp + sc : 0;
-                const int Ti = max(M - oe_ins, 0);
-                En[s] = max(Es[s] - e_del, max(M - oe_del, 0));
-                const int V = inb ? Ti + e_ins * (j + 1) : 0;
-                run = max(run, V);
+                const int Ti = __viaddmax_s32(M, -oe_ins, 0);
+                En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
+                run = max(run, Ti + e_ins * (j + 1));
                 Pf[s] = run;
                 Mv[s] = M;
             }
         }
 
-        // ---- warp exclusive prefix max of the lane totals
+        // ---- warp exclusive prefix max of the lane totals (lane 0 starts from 0 = F at column 0)
         int incl = run;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) incl = max(incl, __shfl_up_sync(BSB_FULL_MASK, incl, d));
         const int excl = __shfl_up_sync(BSB_FULL_MASK, incl, 1);
-        const int basev = e_ins * beg;                 // F(i,beg) = 0
-        const int carry = lane == 0 ? basev : max(excl, basev);
+        const int carry = lane == 0 ? 0 : excl;
 
-        // ---- pass 2: H, row max, and the new eh[] (H shifted one column right)
-        int lmax = 0, lmj = -1, lfirst = INT_MAX, llast = -1, prevH = 0;
+        // ---- pass 2: H, the row-max key (H << 10 | j), and the new eh[] (H shifted one column)
+        int kmax = -1, prevH = 0;
+        uint32_t nzb = 0;
 #pragma unroll
         for (int s = 0; s < C; ++s) {
             const int j = base + s;
-            const bool inb = j >= beg && j < end;
             const int G = s == 0 ? carry : max(carry, Pf[s - 1]);
             const int F = G - e_ins * j;
-            const int H = max(max(Mv[s], Es[s]), F);
-            if (inb) {
-                if (H >= lmax) lmj = j;                 // ties move to the later column
-                lmax = max(lmax, H);
-            }
-            const int nE = inb ? En[s] : (j == end ? 0 : Es[s]);
+            const int H = __vimax3_s32(Mv[s], Es[s], F);
+            const bool lt = j < end;
+            if (lt) kmax = max(kmax, H * 1024 + j);     // ties keep the later column (ksw.c:437)
+            const int nE = lt ? En[s] : (j == end ? 0 : Es[s]);
             Es[s] = nE;
             if (s > 0) {
-                const int nH = j == beg ? h1_init : ((j > beg && j <= end) ? prevH : Hs[s]);
+                const int nH = j <= end ? prevH : Hs[s];
                 Hs[s] = nH;
-                if (j >= beg && j <= end && (nH | nE) != 0) {
-                    if (j < end && lfirst == INT_MAX) lfirst = j;
-                    llast = j;
-                }
+                if (j <= end && (nH | nE) != 0) nzb |= 1u << s;
             }
             prevH = H;
         }
         {
-            const int Hleft = __shfl_up_sync(BSB_FULL_MASK, prevH, 1);
-            const int j = base;
-            const int nH = j == beg ? h1_init : ((j > beg && j <= end) ? Hleft : Hs[0]);
+            int Hleft = __shfl_up_sync(BSB_FULL_MASK, prevH, 1);
+            if (lane == 0) Hleft = h1_init;
+            const int nH = base <= end ? Hleft : Hs[0];
             Hs[0] = nH;
-            if (j >= beg && j <= end && (nH | Es[0]) != 0) {
-                if (j < end) lfirst = j;
-                if (llast < 0) llast = j;
-            }
+            if (base <= end && (nH | Es[0]) != 0) nzb |= 1u;
         }
 
         ncell += end - beg;
-        const int m = __reduce_max_sync(BSB_FULL_MASK, lmax);
-        const int mj = __reduce_max_sync(BSB_FULL_MASK, lmax == m ? lmj : -1);
+        const int kw = __reduce_max_sync(BSB_FULL_MASK, kmax);
+        const int m = kw >> 10, mj = kw & 1023;
 
         if (end == qlen) {          // reached the query end: eh[qlen].h == H(i,qlen-1) (ksw.c:450-453)
             int hsel = 0;
@@ -238,7 +249,9 @@ __device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t 
                 if (best - m - (dj - di) * e_ins > P.zdrop) break;
             }
         }
-        // shrink to the non-zero cells (ksw.c:466-469)
+        // shrink to the non-zero cells (ksw.c:466-469); columns left of beg are zero
+        const int lfirst = nzb ? base + __ffs(nzb) - 1 : INT_MAX;
+        const int llast = nzb ? base + 31 - __clz(nzb) : -1;
         const int fnz = __reduce_min_sync(BSB_FULL_MASK, lfirst);
         const int lnz = __reduce_max_sync(BSB_FULL_MASK, llast);
         if (fnz < end) {
@@ -308,7 +321,7 @@ __global__ void ksw_sched_hist(const bsb_ext_job_t *__restrict__ jobs, int n, lo
         const bsb_ext_job_t jb = jobs[i];
         const int b = tile_bin(jb.qlen);
         const bool ok = b >= 0 && jb.qlen >= 0 && jb.tlen >= 0 && jb.w >= 0 && jb.h0 > 0 &&
-                        jb.h0 <= (1 << 24) && jb.flags == 0 && jb.qoff >= 0 && jb.toff >= 0 &&
+                        jb.h0 <= (1 << 20) && jb.flags == 0 && jb.qoff >= 0 && jb.toff >= 0 &&
                         jb.qoff + jb.qlen <= seq_bytes && jb.toff + jb.tlen <= seq_bytes;
         int key;
         if (!ok) {

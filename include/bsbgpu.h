@@ -73,7 +73,7 @@ typedef struct {
  * cells_out (optional, may be NULL) receives per job the number of DP cells
  * the reference visits (sum over rows of end-beg).  Requires qlen <= 1023,
  * 1 <= e_del, e_ins <= 65535, 0 <= o_del, o_ins <= 65535, matrix entries in
- * [-63, 63] and 0 < h0 <= 2^24 (the reference asserts h0 > 0); violations
+ * [-63, 63] and 0 < h0 <= 2^20 (the reference asserts h0 > 0); violations
  * return BSB_EINVAL / BSB_ETOOLONG before any device work. */
 int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param,
                      const bsb_ext_job_t *jobs, int64_t n_jobs,
@@ -93,7 +93,7 @@ int bsb_extend_batch_device(bsb_ctx *ctx, const bsb_ext_param_t *param,
                             bsb_ext_out_t *d_out, int64_t *d_cells);
 
 /* Waits for the context stream.  After a bsb_extend_batch_device call it
- * also reports jobs the device rejected (qlen > 1023, h0 outside [1, 2^24],
+ * also reports jobs the device rejected (qlen > 1023, h0 outside [1, 2^20],
  * ranges outside seq_bytes, nonzero flags) as BSB_EINVAL; those jobs' output
  * slots are left untouched. */
 int bsb_sync(bsb_ctx *ctx);
@@ -102,6 +102,73 @@ int bsb_sync(bsb_ctx *ctx);
  * events on the context stream around its scheduling and extension
  * kernels), in milliseconds; valid after bsb_sync. */
 float bsb_last_kernel_ms(const bsb_ctx *ctx);
+
+/* ---- FM-index (device resident) ----------------------------------------- */
+
+/* The index arrays as bwa_idx_load leaves them in memory (bwa.c:363-524,
+ * bwt.h:46-58): bwt = the interleaved occurrence array (bwt_size uint32
+ * words), sa = the sampled suffix array with sa[0] = (uint64_t)-1, pac = the
+ * forward bisulfite-converted 2-bit text (optional for seeding). */
+typedef struct {
+    uint64_t primary;
+    uint64_t L2[5];              /* L2[0] = 0, L2[4] = seq_len */
+    const uint32_t *bwt;
+    uint64_t bwt_size;
+    const uint64_t *sa;
+    uint64_t n_sa;
+    int32_t sa_intv;             /* power of two (bwt_cal_sa asserts it) */
+    int32_t pad_;
+    const uint8_t *pac;
+    int64_t l_pac;
+} bsb_index_view_t;
+
+/* Uploads an index the caller already holds (stands in for the host-side
+ * index of bwa_idx_load, bwa.c:363-524).  Replaces any loaded index. */
+int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *view);
+/* Reads <prefix>.bwt/.sa/.ann/.pac (bwt_restore_bwt, bwt_restore_sa,
+ * bwt.c:420-457) and uploads them.  BSB_EIO on a missing or short file. */
+int bsb_index_load(bsb_ctx *ctx, const char *prefix);
+
+/* ---- SMEM seeding: mem_collect_intv ------------------------------------- */
+
+/* The seeding fields of mem_opt_t (bwamem.h:33-40). */
+typedef struct {
+    int32_t min_seed_len;        /* -k, 19 */
+    float   split_factor;        /* -r, 1.5 */
+    int32_t split_width;         /* 10 */
+    int32_t max_mem_intv;        /* 20 */
+} bsb_seed_opt_t;
+
+/* bwtintv_t (bwt.h:60-62): x[0] forward start, x[1] reverse start, x[2]
+ * size, info = qbeg << 32 | qend. */
+typedef struct {
+    uint64_t x[3];
+    uint64_t info;
+} bsb_intv_t;
+
+/* Replaces mem_collect_intv (bwamem.c:118-166; bwt_smem1, bwt.c:289-356;
+ * bwt_seed_strategy1, bwt.c:358-379) for a batch of reads: nt4 codes,
+ * read r = seqs[offs[r] .. offs[r+1]).  out receives every read's seed list
+ * in the reference's order (sorted by info), out_off[r] .. out_off[r+1]
+ * (n_reads + 1 entries).  Reads shorter than min_seed_len get no seeds
+ * (mem_chain, bwamem.c:266).  Reads longer than 1024 give BSB_ETOOLONG. */
+int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads,
+                   const uint8_t *seqs, const int64_t *offs,
+                   bsb_intv_t *out, int64_t max_out, int64_t *out_off);
+/* Device-buffer form, asynchronous on the context stream.  d_offs must start
+ * at 0; d_out must hold 2*total_bases + 32*n_reads entries; max_len bounds
+ * every read length.  A read outside max_len is skipped and reported by
+ * bsb_sync as BSB_ETOOLONG. */
+int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads,
+                          const uint8_t *d_seqs, const int64_t *d_offs, int64_t total_bases,
+                          int32_t max_len, bsb_intv_t *d_out, int64_t *d_out_off);
+
+/* ---- suffix-array lookup: bwt_sa ---------------------------------------- */
+
+/* pos[i] = bwt_sa(bwt, rows[i]) (bwt.c:86-96) for every row; host buffers. */
+int bsb_sa_batch(bsb_ctx *ctx, const uint64_t *rows, int64_t n, uint64_t *pos);
+/* Device-buffer form; rows beyond seq_len give (uint64_t)-2. */
+int bsb_sa_batch_device(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos);
 
 /* ---- measurement helper (no reference counterpart) ---------------------- */
 

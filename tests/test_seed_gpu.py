@@ -1,0 +1,92 @@
+"""SMEM seeding and SA lookups on the GPU against the reference's seed lists
+(tests/golden/reads_*.npz) and the oracle, through the C ABI.  Bit-exact."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from bsbolt_gb300 import _lib, index, seed, synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
+import golden_data  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def idx(tmp_path_factory):
+    d = tmp_path_factory.mktemp("gidx")
+    fa = str(d / "ref.fa")
+    synth.write_fasta(fa, golden_data.golden_genome())
+    prefix = str(d / "ref")
+    index.build_index(fa, prefix)
+    return prefix
+
+
+@pytest.fixture(scope="module")
+def ctx_idx(gpu_ctx, idx):
+    seed.load_index(gpu_ctx, idx)
+    return gpu_ctx
+
+
+@pytest.mark.parametrize("name", ["L5", "L30"])
+def test_seeds_match_reference(ctx_idx, name):
+    d = np.load(os.path.join(GOLDEN, f"reads_{name}.npz"))
+    o = d["opts"]
+    got, off = seed.seed_batch(ctx_idx, d["reads"], d["read_off"], min_seed_len=int(o[10]),
+                               split_width=int(o[12]), max_mem_intv=int(o[13]))
+    ref, roff = d["smem"], d["smem_off"]
+    lens = d["read_off"][1:] - d["read_off"][:-1]
+    for r in range(len(lens)):
+        exp = ref[roff[r]:roff[r + 1]] if lens[r] >= int(o[10]) else ref[0:0]
+        assert np.array_equal(got[off[r]:off[r + 1]], exp), f"read {r}: seeds differ"
+
+
+def test_seeds_random_reads_vs_oracle(ctx_idx, idx):
+    """Reads with errors, N runs, repeats and every length 0..300 against the oracle."""
+    bi = index.BwaIndex(idx)
+    pac = bi.pac_codes()
+    rng = np.random.Generator(np.random.PCG64(11))
+    reads = []
+    for k in range(3000):
+        L = int(rng.integers(0, 301)) if k % 3 else 150
+        st = int(rng.integers(0, len(pac) - L - 1))
+        r = pac[st:st + L].copy()
+        if k % 2:
+            r = (3 - r[::-1]).astype(np.uint8)
+        e = rng.random(L) < 0.02
+        r[e] = rng.integers(0, 5, int(e.sum()))
+        reads.append(r.astype(np.uint8))
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    seqs = np.concatenate(reads)
+    got, off = seed.seed_batch(ctx_idx, seqs, offs)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    exp, eoff = ob.collect_intv(seqs, offs, n_threads=8)
+    assert np.array_equal(off, eoff)
+    assert np.array_equal(got, exp)
+
+
+def test_sa_lookup_vs_suffix_array(ctx_idx, idx):
+    bi = index.BwaIndex(idx)
+    pac = bi.pac_codes()
+    text = np.concatenate([pac, 3 - pac[::-1]]).astype(np.uint8)
+    full = index.suffix_array(text).astype(np.int64)
+    rng = np.random.Generator(np.random.PCG64(5))
+    rows = np.concatenate([np.arange(0, 200), rng.integers(0, len(full), 200000)]).astype(np.uint64)
+    got = seed.sa_batch(ctx_idx, rows).astype(np.int64)
+    exp = full[rows.astype(np.int64)]
+    exp = np.where(exp == len(text), -1, exp)
+    assert np.array_equal(got, exp)
+
+
+def test_seed_errors(gpu_ctx, ctx_idx):
+    with pytest.raises(_lib.BsbError) as e:
+        seed.seed_batch(ctx_idx, np.zeros(2000, np.uint8), np.array([0, 2000]))
+    assert e.value.code == _lib.BSB_ETOOLONG
+    with pytest.raises(_lib.BsbError) as e:
+        seed.sa_batch(ctx_idx, np.array([1 << 60], np.uint64))
+    assert e.value.code == _lib.BSB_EINVAL
