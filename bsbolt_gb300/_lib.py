@@ -20,6 +20,8 @@ BSB_EIO = -4
 BSB_ETIMEOUT = -5
 BSB_ETOOLONG = -6
 BSB_ENOINDEX = -7
+BSB_ECAPACITY = -8
+BSB_NOALLOC_MAX_JOBS = 1 << 18
 
 # every extern "C" symbol include/bsbgpu.h declares
 EXPORTS = (
@@ -27,7 +29,7 @@ EXPORTS = (
     "bsb_extend_batch", "bsb_extend_batch_device", "bsb_sync", "bsb_last_kernel_ms",
     "bsb_probe_int_peak",
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
-    "bsb_sa_batch", "bsb_sa_batch_device",
+    "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc",
 )
 
 
@@ -103,6 +105,8 @@ def load(path: str = LIB_PATH):
     L.bsb_sa_batch.restype = I32
     L.bsb_sa_batch_device.argtypes = [P, P, I64, P]
     L.bsb_sa_batch_device.restype = I32
+    L.bsb_extend_batch_noalloc.argtypes = [P, P, I64, P, I64, P, P, P]
+    L.bsb_extend_batch_noalloc.restype = I32
     L.bsb_last_kernel_ms.argtypes = [P]
     L.bsb_last_kernel_ms.restype = ctypes.c_float
     _lib = L

@@ -29,6 +29,7 @@ extern "C" {
 #define BSB_ETIMEOUT   -5   /* a bounded device wait ran out                  */
 #define BSB_ETOOLONG   -6   /* a sequence exceeds the supported length        */
 #define BSB_ENOINDEX   -7   /* call needs an index and none is loaded         */
+#define BSB_ECAPACITY  -8   /* batch larger than a fixed-size buffer allows   */
 
 typedef struct bsb_ctx bsb_ctx;
 
@@ -169,6 +170,35 @@ int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_rea
 int bsb_sa_batch(bsb_ctx *ctx, const uint64_t *rows, int64_t n, uint64_t *pos);
 /* Device-buffer form; rows beyond seq_len give (uint64_t)-2. */
 int bsb_sa_batch_device(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos);
+
+/* ---- extension without any device allocation ---------------------------- */
+
+/* No counterpart in the reference: BWA allocates freely on the host and has
+ * no device.  This entry point is for callers that may not call cudaMalloc
+ * -- code running under a host application whose memory manager owns all
+ * device memory, or on a path where the implicit synchronisation of
+ * cudaMalloc/cudaFree is not allowed.  It runs the same extension as
+ * bsb_extend_batch_device, but its scheduling scratch is one fixed array of
+ * the library's own device memory (about 2 MiB, held on every GPU that loads
+ * the library until the process exits), so it calls no cudaMalloc, cudaFree
+ * or other allocating routine and needs no context.
+ *   - All buffers are the caller's device memory; the call is asynchronous
+ *     on `stream` (a cudaStream_t; NULL = the legacy default stream) on the
+ *     current device.
+ *   - At most BSB_NOALLOC_MAX_JOBS jobs per call; a larger n_jobs returns
+ *     BSB_ECAPACITY before any work is queued.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream
+ *     capture.
+ *   - Every call shares the array and it keeps the last call's contents
+ *     (the launch clears what must start at zero).  Calls whose work
+ *     overlaps on the GPU race on it: order them on one stream.
+ *   - Jobs that fail the preconditions of bsb_extend_batch are skipped and
+ *     their output slots left untouched. */
+#define BSB_NOALLOC_MAX_JOBS (1 << 18)
+int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_ext_job_t *d_jobs,
+                             int64_t n_jobs, const uint8_t *d_seq, int64_t seq_bytes,
+                             bsb_ext_out_t *d_out, int64_t *d_cells, void *stream);
 
 /* ---- measurement helper (no reference counterpart) ---------------------- */
 
