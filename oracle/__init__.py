@@ -21,16 +21,19 @@ _SO = os.path.join(_HERE, "_build", "liborc.so")
 _lib = None
 
 
+_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c")
+_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h")
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle restatement into oracle/_build/liborc.so (gcc -O2)."""
-    src = os.path.join(_HERE, "bsb_oracle.c")
-    if (not force and os.path.exists(_SO)
-            and os.path.getmtime(_SO) >= os.path.getmtime(src)
-            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.join(_HERE, "bsb_oracle.h"))):
+    deps = [os.path.join(_HERE, f) for f in _SRC + _HDR]
+    if not force and os.path.exists(_SO) and all(os.path.getmtime(_SO) >= os.path.getmtime(d) for d in deps):
         return _SO
     os.makedirs(os.path.dirname(_SO), exist_ok=True)
     tmp = _SO + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-o", tmp, src])
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-o", tmp]
+                          + [os.path.join(_HERE, f) for f in _SRC] + ["-lm"])
     os.replace(tmp, _SO)
     return _SO
 
@@ -118,3 +121,86 @@ class OracleBwt:
         pos = np.zeros(len(k), np.uint64)
         lib().orc_bwt_sa_batch(self.ptr, len(k), _p(k), _p(pos), n_threads)
         return pos
+
+
+# ---------------------------------------------------------------- chaining / extension
+
+CHAIN_DTYPE = np.dtype([("n", "<i4"), ("rid", "<i4"), ("first", "<i4"), ("kept", "<i4"), ("w", "<i4"),
+                        ("is_alt", "<i4"), ("frac_rep", "<f4"), ("seed_off", "<i4"), ("pos", "<i8")])
+SEED_DTYPE = np.dtype([("rbeg", "<i8"), ("qbeg", "<i4"), ("len", "<i4"), ("score", "<i4"), ("pad", "<i4")])
+REG_DTYPE = np.dtype([("rb", "<i8"), ("re", "<i8"), ("qb", "<i4"), ("qe", "<i4"), ("rid", "<i4"),
+                      ("score", "<i4"), ("truesc", "<i4"), ("w", "<i4"), ("seedcov", "<i4"),
+                      ("seedlen0", "<i4"), ("frac_rep", "<f4"), ("pad", "<i4")])
+ANN_DTYPE = np.dtype([("offset", "<i8"), ("len", "<i4"), ("is_alt", "<i4")])
+
+
+class Opt(ctypes.Structure):
+    """orc_opt_t: the mem_opt_t fields of the path (BWA defaults, bwamem.c:50-88)."""
+    _fields_ = [(f, ctypes.c_int32) for f in ("a", "b", "o_del", "e_del", "o_ins", "e_ins", "w", "zdrop",
+                                               "pen_clip5", "pen_clip3", "min_seed_len", "max_occ",
+                                               "max_chain_gap", "min_chain_weight", "max_chain_extend")] + \
+               [("mask_level", ctypes.c_float), ("drop_ratio", ctypes.c_float), ("split_factor", ctypes.c_float),
+                ("split_width", ctypes.c_int32), ("max_mem_intv", ctypes.c_int32),
+                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3)]
+
+    @classmethod
+    def from_list(cls, o):
+        """From [a, b, o_del, e_del, o_ins, e_ins, w, zdrop, pen_clip5, pen_clip3,
+        min_seed_len, max_occ, split_width, max_mem_intv, max_chain_gap]."""
+        o = [int(x) for x in o]
+        opt = cls(a=o[0], b=o[1], o_del=o[2], e_del=o[3], o_ins=o[4], e_ins=o[5], w=o[6], zdrop=o[7],
+                  pen_clip5=o[8], pen_clip3=o[9], min_seed_len=o[10], max_occ=o[11], max_chain_gap=o[14],
+                  min_chain_weight=0, max_chain_extend=1 << 30, mask_level=0.5, drop_ratio=0.5,
+                  split_factor=1.5, split_width=o[12], max_mem_intv=o[13])
+        for i in range(4):
+            for j in range(4):
+                opt.mat[i * 5 + j] = o[0] if i == j else -o[1]
+        for k in range(25):
+            if k % 5 == 4 or k >= 20:
+                opt.mat[k] = -1
+        return opt
+
+
+class _Bns(ctypes.Structure):
+    _fields_ = [("l_pac", ctypes.c_int64), ("n_seqs", ctypes.c_int32), ("anns", ctypes.c_void_p),
+                ("pac", ctypes.c_void_p)]
+
+
+class _AlignOut(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("chain0", "chain0_off", "seeds0", "seeds0_off", "chain1",
+                                              "chain1_off", "regs", "regs_off")] + [("cells", ctypes.c_int64)]
+
+
+def align_regs(obwt: "OracleBwt", anns: np.ndarray, pac: np.ndarray, l_pac: int, opt: Opt,
+               seqs: np.ndarray, offs: np.ndarray, n_threads: int = 1):
+    """Seeds -> chains -> filter -> mem_chain2aln per read (bwamem.c:1157-1180, before dedup).
+
+    Returns a dict of numpy arrays: chain0/seeds0 (mem_chain output in tree order),
+    chain1 (after mem_chain_flt), regs (pre-dedup regions), each with *_off[n+1]."""
+    L = lib()
+    L.orc_align_regs_batch.restype = ctypes.c_int
+    L.orc_align_regs_batch.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                               ctypes.c_void_p, ctypes.c_int]
+    L.orc_align_out_free.argtypes = [ctypes.c_void_p]
+    anns = np.ascontiguousarray(anns, dtype=ANN_DTYPE)
+    pac = np.ascontiguousarray(pac, dtype=np.uint8)
+    bns = _Bns(l_pac, len(anns), anns.ctypes.data, pac.ctypes.data)
+    seqs = np.ascontiguousarray(seqs, dtype=np.uint8)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    n = len(offs) - 1
+    out = _AlignOut()
+    rc = L.orc_align_regs_batch(obwt.ptr, ctypes.byref(bns), ctypes.byref(opt), n, _p(seqs), _p(offs),
+                                ctypes.byref(out), n_threads)
+    res = {}
+    for name, dt in (("chain0", CHAIN_DTYPE), ("seeds0", SEED_DTYPE), ("chain1", CHAIN_DTYPE), ("regs", REG_DTYPE)):
+        off = np.ctypeslib.as_array(ctypes.cast(getattr(out, name + "_off"), ctypes.POINTER(ctypes.c_int64)),
+                                    (n + 1,)).copy()
+        cnt = int(off[-1])
+        buf = ctypes.string_at(getattr(out, name), cnt * dt.itemsize) if cnt else b""
+        res[name] = np.frombuffer(buf, dt).copy()
+        res[name + "_off"] = off
+    res["cells"] = int(out.cells)
+    L.orc_align_out_free(ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle align_regs failed ({rc})")
+    return res

@@ -53,3 +53,59 @@ def golden_reads(n_pairs=700, seed=20261203 + 7):
     return reads
 
 
+
+
+# ------------------------------------------------------------ repeat stress
+
+GENOME_REP = dict(seed=20261203 + 99)
+
+
+def golden_genome_rep():
+    """A 2 x 150 kb reference where 60 copies of a 300 bp element (0-3 %
+    divergence) and 40 exact copies of a 120 bp element are scattered, so
+    reads hit dozens of loci: many chains per read (B-tree splits), chains
+    of equal weight (sort ties) and heavy SA sampling (max_occ)."""
+    rng = np.random.Generator(np.random.PCG64(GENOME_REP["seed"]))
+    contigs = synth.bs_genome(2, 150_000, seed=GENOME_REP["seed"])
+    elem = contigs[0][1][1000:1300].copy()
+    small = contigs[1][1][2000:2120].copy()
+    for k in range(60):
+        c = contigs[k % 2][1]
+        at = int(rng.integers(5000, len(c) - 400))
+        e = elem.copy()
+        mut = rng.random(len(e)) < (k % 4) * 0.01
+        e[mut] = rng.integers(0, 4, int(mut.sum()))
+        c[at:at + len(e)] = e
+    for k in range(40):
+        c = contigs[k % 2][1]
+        at = int(rng.integers(5000, len(c) - 200))
+        c[at:at + len(small)] = small
+    return contigs
+
+
+def golden_reads_rep(n=400, seed=20261203 + 100):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    contigs = golden_genome_rep()
+    elem = contigs[0][1][1000:1300]
+    reads = []
+    for k in range(n):
+        kind = k % 4
+        c = contigs[int(rng.integers(0, 2))][1]
+        if kind == 0:        # a read inside a repeat element
+            st = int(rng.integers(0, 200))
+            r = elem[st:st + 100].copy()
+        elif kind == 1:      # a genomic read that crosses into repeats
+            L = int(rng.integers(100, 251))
+            st = int(rng.integers(0, len(c) - L))
+            r = c[st:st + L].copy()
+        elif kind == 2:      # the same 40-mer twice, 150 bp apart: chains with equal keys
+            st = int(rng.integers(0, len(c) - 60))
+            u = c[st:st + 40].copy()
+            r = np.concatenate([u, rng.integers(0, 4, 110), u, rng.integers(0, 4, 60)]).astype(np.uint8)
+        else:                # a strand-flipped repeat read with errors
+            st = int(rng.integers(0, 150))
+            r = (3 - elem[st:st + 150][::-1]).astype(np.uint8)
+        e = rng.random(len(r)) < 0.01
+        r[e] = rng.integers(0, 4, int(e.sum()))
+        reads.append(synth.bs_convert(r.astype(np.uint8), g2a=bool(k & 1)))
+    return reads

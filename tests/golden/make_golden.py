@@ -28,7 +28,8 @@ sys.path.insert(0, ROOT)
 from bsbolt_gb300 import synth  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from golden_data import GENOME, OPTS, golden_genome, golden_reads  # noqa: E402
+from golden_data import (GENOME, GENOME_REP, OPTS, golden_genome, golden_genome_rep,  # noqa: E402
+                         golden_reads, golden_reads_rep)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
@@ -142,17 +143,17 @@ def sha256(fn):
 
 # ------------------------------------------------------------------ index
 
-def make_index(td):
-    fa = os.path.join(td, "ref.fa")
-    synth.write_fasta(fa, golden_genome())
-    prefix = os.path.join(td, "ref")
+def make_index(td, tag="", genome=golden_genome, meta=GENOME):
+    fa = os.path.join(td, f"ref{tag}.fa")
+    synth.write_fasta(fa, genome())
+    prefix = os.path.join(td, f"ref{tag}")
     subprocess.check_call([os.path.join(REF, "bwa"), "index", "-a", "bwtsw", "-p", prefix, fa],
                           stderr=subprocess.DEVNULL)
     sums = {ext: sha256(prefix + "." + ext) for ext in ("pac", "opac", "ann", "amb", "bwt", "sa")}
     import json
-    fn = os.path.join(HERE, "index_sha256.json")
+    fn = os.path.join(HERE, f"index{tag}_sha256.json")
     with open(fn, "w") as f:
-        json.dump({"genome": GENOME, "files": sums}, f, indent=1)
+        json.dump({"genome": meta, "files": sums}, f, indent=1)
     print(fn)
     return prefix
 
@@ -218,8 +219,8 @@ def parse_dump(prefix, n_reads):
     return out
 
 
-def make_reads(td, prefix):
-    reads = golden_reads()
+def make_reads(td, prefix, reads=None, names=("L5", "L30"), tag=""):
+    reads = golden_reads() if reads is None else reads
     offs = np.zeros(len(reads) + 1, np.int64)
     offs[1:] = np.cumsum([len(r) for r in reads])
     fin = os.path.join(td, "reads.bin")
@@ -227,13 +228,14 @@ def make_reads(td, prefix):
         f.write(np.array([len(reads), offs[-1]], np.int64).tobytes())
         f.write(offs.tobytes())
         f.write(np.concatenate(reads).astype(np.uint8).tobytes())
-    for name, o in OPTS.items():
+    for name in names:
+        o = OPTS[name]
         fo = os.path.join(td, f"opt_{name}.bin")
         np.array(o, np.int32).tofile(fo)
         outp = os.path.join(td, f"dump_{name}")
         subprocess.check_call([os.path.join(REF, "golden_dump"), "reads", prefix, fin, outp, fo])
         d = parse_dump(outp, len(reads))
-        fn = os.path.join(HERE, f"reads_{name}.npz")
+        fn = os.path.join(HERE, f"reads{tag}_{name}.npz")
         np.savez_compressed(fn, reads=np.concatenate(reads), read_off=offs, opts=np.array(o, np.int32), **d)
         print(fn, os.path.getsize(fn), "smem", len(d["smem"]), "regs", len(d["regs"]), "ksw", len(d["ksw_out"]))
 
@@ -247,3 +249,6 @@ if __name__ == "__main__":
             prefix = make_index(td)
             if "reads" in what:
                 make_reads(td, prefix)
+            prefix = make_index(td, "_rep", golden_genome_rep, GENOME_REP)
+            if "reads" in what:
+                make_reads(td, prefix, golden_reads_rep(), ("L5",), "_rep")

@@ -44,6 +44,15 @@ def test_index_files_match_reference(idx):
         assert sha(idx + "." + ext) == h, f".{ext} differs from the reference bwa index"
 
 
+def test_repeat_index_files_match_reference(tmp_path):
+    fa = str(tmp_path / "rep.fa")
+    synth.write_fasta(fa, golden_data.golden_genome_rep())
+    index.build_index(fa, str(tmp_path / "rep"))
+    want = json.load(open(os.path.join(GOLDEN, "index_rep_sha256.json")))["files"]
+    for ext, h in want.items():
+        assert sha(str(tmp_path / "rep") + "." + ext) == h, f".{ext} differs from the reference bwa index"
+
+
 def test_suffix_array_small_exhaustive():
     rng = np.random.Generator(np.random.PCG64(1))
     for n in list(range(1, 40)) + [200, 1000]:
