@@ -29,7 +29,7 @@ EXPORTS = (
     "bsb_extend_batch", "bsb_extend_batch_device", "bsb_sync", "bsb_last_kernel_ms",
     "bsb_probe_int_peak",
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
-    "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc",
+    "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
 )
 
 
@@ -59,7 +59,32 @@ class IndexView(ctypes.Structure):
                 ("bwt", ctypes.c_void_p), ("bwt_size", ctypes.c_uint64),
                 ("sa", ctypes.c_void_p), ("n_sa", ctypes.c_uint64),
                 ("sa_intv", ctypes.c_int32), ("pad_", ctypes.c_int32),
-                ("pac", ctypes.c_void_p), ("l_pac", ctypes.c_int64)]
+                ("pac", ctypes.c_void_p), ("l_pac", ctypes.c_int64),
+                ("n_seqs", ctypes.c_int32), ("pad2_", ctypes.c_int32),
+                ("ann_offset", ctypes.c_void_p), ("ann_len", ctypes.c_void_p)]
+
+
+class AlignOpt(ctypes.Structure):
+    """bsb_align_opt_t (mem_opt_t fields; BWA defaults as in mem_opt_init, bwamem.c:50-88)"""
+    _fields_ = [(f, ctypes.c_int32) for f in ("a", "b", "o_del", "e_del", "o_ins", "e_ins", "w", "zdrop",
+                                               "pen_clip5", "pen_clip3", "min_seed_len", "max_occ",
+                                               "max_chain_gap", "min_chain_weight", "max_chain_extend")] + \
+               [("mask_level", ctypes.c_float), ("drop_ratio", ctypes.c_float), ("split_factor", ctypes.c_float),
+                ("split_width", ctypes.c_int32), ("max_mem_intv", ctypes.c_int32),
+                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3)]
+
+    @classmethod
+    def bwa_defaults(cls, a=1, b=4, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, zdrop=100, pen_clip5=5,
+                     pen_clip3=5, min_seed_len=19, max_occ=500, split_width=10, max_mem_intv=20,
+                     max_chain_gap=10000):
+        o = cls(a=a, b=b, o_del=o_del, e_del=e_del, o_ins=o_ins, e_ins=e_ins, w=w, zdrop=zdrop,
+                pen_clip5=pen_clip5, pen_clip3=pen_clip3, min_seed_len=min_seed_len, max_occ=max_occ,
+                max_chain_gap=max_chain_gap, min_chain_weight=0, max_chain_extend=1 << 30, mask_level=0.5,
+                drop_ratio=0.5, split_factor=1.5, split_width=split_width, max_mem_intv=max_mem_intv)
+        for i in range(5):
+            for j in range(5):
+                o.mat[i * 5 + j] = -1 if (i == 4 or j == 4) else (a if i == j else -b)
+        return o
 
 
 _lib = None
@@ -107,6 +132,8 @@ def load(path: str = LIB_PATH):
     L.bsb_sa_batch_device.restype = I32
     L.bsb_extend_batch_noalloc.argtypes = [P, P, I64, P, I64, P, P, P]
     L.bsb_extend_batch_noalloc.restype = I32
+    L.bsb_align_regs_batch.argtypes = [P, P, ctypes.c_int32, P, P, P, I64, P]
+    L.bsb_align_regs_batch.restype = I32
     L.bsb_last_kernel_ms.argtypes = [P]
     L.bsb_last_kernel_ms.restype = ctypes.c_float
     _lib = L

@@ -101,6 +101,8 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->d_in) cudaFree(ctx->d_in);
     if (ctx->d_out) cudaFree(ctx->d_out);
     if (ctx->seed_scratch) cudaFree(ctx->seed_scratch);
+    if (ctx->arena0) cudaFree(ctx->arena0);
+    if (ctx->arena1) cudaFree(ctx->arena1);
     bsb_index_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

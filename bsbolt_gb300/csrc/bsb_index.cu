@@ -27,7 +27,10 @@ void bsb_index_release(bsb_ctx *ctx)
     if (ctx->idx_bwt) cudaFree(ctx->idx_bwt);
     if (ctx->idx_sa) cudaFree(ctx->idx_sa);
     if (ctx->idx_pac) cudaFree(ctx->idx_pac);
-    ctx->idx_bwt = ctx->idx_sa = ctx->idx_pac = nullptr;
+    if (ctx->idx_ann_off) cudaFree(ctx->idx_ann_off);
+    if (ctx->idx_ann_len) cudaFree(ctx->idx_ann_len);
+    ctx->idx_bwt = ctx->idx_sa = ctx->idx_pac = ctx->idx_ann_off = ctx->idx_ann_len = nullptr;
+    ctx->n_seqs = 0;
     ctx->has_index = 0;
 }
 
@@ -78,6 +81,17 @@ extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
         if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_pac, v->pac, pb, cudaMemcpyHostToDevice, ctx->stream),
                            "index: pac upload")))
             return rc;
+    }
+    if (v->n_seqs > 0 && v->ann_offset && v->ann_len) {
+        if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_ann_off, 8 * (size_t)v->n_seqs), "index: contig offsets"))) return rc;
+        if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_ann_len, 4 * (size_t)v->n_seqs), "index: contig lengths"))) return rc;
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_ann_off, v->ann_offset, 8 * (size_t)v->n_seqs,
+                                                cudaMemcpyHostToDevice, ctx->stream), "index: contig upload")))
+            return rc;
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_ann_len, v->ann_len, 4 * (size_t)v->n_seqs,
+                                                cudaMemcpyHostToDevice, ctx->stream), "index: contig upload")))
+            return rc;
+        ctx->n_seqs = v->n_seqs;
     }
     ctx->primary = v->primary;
     for (int i = 0; i < 5; ++i) ctx->L2[i] = v->L2[i];
@@ -135,10 +149,37 @@ extern "C" int bsb_index_load(bsb_ctx *ctx, const char *prefix)
     sav[0] = (uint64_t)-1;
     memcpy(sav.data() + 1, sa.data() + 56, (v.n_sa - 1) * 8);
     v.sa = sav.data();
+    std::vector<int64_t> aoff;
+    std::vector<int32_t> alen;
     if (read_all((p + ".ann").c_str(), ann) && !ann.empty()) {
+        // .ann (bns_dump, bntseq.c:67-84): "l_pac n_seqs seed", then per contig a
+        // "gi name [anno]" line and an "offset len n_ambs" line
+        ann.push_back(0);
         long long lp = 0;
-        if (sscanf(ann.data(), "%lld", &lp) == 1 && read_all((p + ".pac").c_str(), pac) &&
-            pac.size() >= (size_t)(lp + 3) / 4) {
+        int ns = 0;
+        unsigned seed = 0;
+        const char *c = ann.data();
+        int used = 0;
+        if (sscanf(c, "%lld %d %u%n", &lp, &ns, &seed, &used) == 3 && ns > 0) {
+            c += used;
+            for (int i = 0; i < ns && c; ++i) {
+                c = strchr(c, '\n');                      // end of the previous line
+                if (!c) break;
+                c = strchr(c + 1, '\n');                  // skip the name line
+                if (!c) break;
+                long long off = 0;
+                int ln = 0, na = 0;
+                if (sscanf(c + 1, "%lld %d %d%n", &off, &ln, &na, &used) != 3) break;
+                aoff.push_back(off);
+                alen.push_back(ln);
+                c += 1 + used;
+            }
+            if ((int)aoff.size() != ns) return bsb_fail(ctx, BSB_EIO, "cannot parse %s.ann", prefix);
+            v.n_seqs = ns;
+            v.ann_offset = aoff.data();
+            v.ann_len = alen.data();
+        }
+        if (lp > 0 && read_all((p + ".pac").c_str(), pac) && pac.size() >= (size_t)(lp + 3) / 4) {
             v.l_pac = lp;
             v.pac = (const uint8_t *)pac.data();
         }
@@ -249,6 +290,11 @@ extern "C" int bsb_sa_batch(bsb_ctx *ctx, const uint64_t *rows, int64_t n, uint6
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(pos, ctx->d_out, 8 * n, cudaMemcpyDeviceToHost, ctx->stream), "D2H SA")))
         return rc;
     return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "SA batch");
+}
+
+cudaError_t bsb_sa_launch_ctx(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos)
+{
+    return sa_launch(dev_fm(ctx), d_rows, n, d_pos, ctx->n_sm, ctx->stream);
 }
 
 extern "C" int bsb_sa_batch_device(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos)

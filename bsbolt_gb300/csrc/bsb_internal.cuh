@@ -12,6 +12,8 @@
 
 // Longest read the seeding kernels accept (bounds the per-thread interval lists).
 #define BSB_SEED_MAX_LEN 1024
+// Longest read the full seed-chain-extend batch accepts (extension tiles up to 16 columns per lane).
+#define BSB_ALIGN_MAX_LEN 512
 
 struct bsb_ctx {
     int device = 0;
@@ -38,11 +40,20 @@ struct bsb_ctx {
     uint64_t L2[5] = {0, 0, 0, 0, 0};
     int sa_intv = 0;
     int64_t l_pac = 0;
+    // contig table (bntann1_t offsets and lengths) for chain extension
+    void *idx_ann_off = nullptr, *idx_ann_len = nullptr;
+    int n_seqs = 0;
     // seeding scratch (padded per-read seed lists, interval lists, counters)
     void *seed_scratch = nullptr;
     size_t seed_scratch_bytes = 0;
     int *seed_ctrl = nullptr;
+    // chaining / chain-extension scratch
+    void *arena0 = nullptr, *arena1 = nullptr;
+    size_t arena0_bytes = 0, arena1_bytes = 0;
 };
+
+// SA lookups of device rows with the context's index (bwt_sa, bwt.c:86-96).
+cudaError_t bsb_sa_launch_ctx(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos);
 
 void bsb_index_release(bsb_ctx *ctx);
 

@@ -1,0 +1,974 @@
+// chain.cu -- seeds -> chains -> filtered chains -> alignment regions, on sm_103a.
+//
+// The pre-dedup part of mem_align1_core (bsbolt/External/BWA/bwamem.c:1157-1180)
+// after seeding:
+//   rows_count / rows_fill  the SA rows mem_chain samples per seed interval
+//                           (bwamem.c:280-283), then sa_kernel (seed.cu) maps them
+//                           to reference positions;
+//   chain_kernel            one thread per read: mem_chain with the reference's
+//                           B-tree of chains (kbtree.h, t = 5) so equal keys land
+//                           where the reference puts them, then mem_chain_weight
+//                           and mem_chain_flt with ks_introsort's exact order;
+//   chain2aln_kernel        one warp per read: mem_chain2aln (bwamem.c:636-790),
+//                           each ksw_extend2 run by the warp (ksw_core.cuh) on the
+//                           read and the device 2-bit reference directly, so no
+//                           reversed copies or target windows are materialised.
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bsb_internal.cuh"
+#include "fm_index.cuh"
+#include "ksw_core.cuh"
+
+namespace {
+
+constexpr int kBT = 5;                  // kbtree order for 40-byte keys in 512-byte nodes
+constexpr int kBTMax = 2 * kBT - 1;
+
+struct BtNode {
+    int n, internal;
+    int key[kBTMax];
+    int child[kBTMax + 1];
+};
+
+struct ChainRec {                       // a chain while it is being built
+    int64_t pos;                        // first seed's rbeg (the tree key)
+    int64_t first_rbeg, last_rbeg;
+    int first_qbeg, last_qbeg, last_len;
+    int n, rid;
+};
+
+struct DevSeed {                        // mem_seed_t (bwamem.c:171-174)
+    int64_t rbeg;
+    int32_t qbeg, len, score, pad;
+};
+
+struct DevChain {                       // a kept chain, in mem_chain_flt's order
+    int32_t n, rid, w, kept;
+    int32_t seed_off, first;
+    float frac_rep;
+    int32_t pad;
+};
+
+struct AlnOpt {
+    int a, o_del, e_del, o_ins, e_ins, w, zdrop, pen_clip5, pen_clip3;
+    int min_seed_len, max_occ, max_chain_gap, min_chain_weight, max_chain_extend;
+    float mask_level, drop_ratio;
+};
+
+struct DevBns {
+    const int64_t *ann_offset;
+    const int32_t *ann_len;
+    int n_seqs;
+    int64_t l_pac;
+    const uint8_t *pac;
+};
+
+// ---------------------------------------------------------------- bns lookups
+
+__device__ int pos2rid(const DevBns &B, int64_t pos_f)              // bntseq.c:364-379
+{
+    int left = 0, mid = 0, right = B.n_seqs;
+    if (pos_f >= B.l_pac) return -1;
+    while (left < right) {
+        mid = (left + right) >> 1;
+        if (pos_f >= B.ann_offset[mid]) {
+            if (mid == B.n_seqs - 1) break;
+            if (pos_f < B.ann_offset[mid + 1]) break;
+            left = mid + 1;
+        } else right = mid;
+    }
+    return mid;
+}
+
+__device__ __forceinline__ int64_t depos(const DevBns &B, int64_t pos, int &is_rev)
+{
+    is_rev = pos >= B.l_pac;
+    return is_rev ? (B.l_pac << 1) - 1 - pos : pos;
+}
+
+__device__ int intv2rid(const DevBns &B, int64_t rb, int64_t re)    // bntseq.c:381-389
+{
+    int is_rev;
+    if (rb < B.l_pac && re > B.l_pac) return -2;
+    const int rid_b = pos2rid(B, depos(B, rb, is_rev));
+    const int rid_e = rb < re ? pos2rid(B, depos(B, re - 1, is_rev)) : rid_b;
+    return rid_b == rid_e ? rid_b : -1;
+}
+
+// base at position p of the forward-reverse text (bns_get_seq, bntseq.c:414-434)
+__device__ __forceinline__ int text_base(const DevBns &B, int64_t p)
+{
+    if (p < B.l_pac) return __ldg(B.pac + (p >> 2)) >> ((~p & 3) << 1) & 3;
+    p = (B.l_pac << 1) - 1 - p;
+    return 3 - (__ldg(B.pac + (p >> 2)) >> ((~p & 3) << 1) & 3);
+}
+
+// ---------------------------------------------------------------- SA rows
+
+__device__ __forceinline__ int rows_of(uint64_t x2, int max_occ, uint64_t &step)
+{
+    step = x2 > (uint64_t)max_occ ? x2 / (uint64_t)max_occ : 1;
+    const uint64_t n = (x2 + step - 1) / step;                       // k = 0, step, ... < x2
+    return (int)(n < (uint64_t)max_occ ? n : (uint64_t)max_occ);
+}
+
+__global__ void rows_count(const DevIntv *__restrict__ seeds, int64_t n, int max_occ, int *__restrict__ cnt)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t step;
+        cnt[i] = rows_of(seeds[i].x2, max_occ, step);
+    }
+}
+
+__global__ void rows_fill(const DevIntv *__restrict__ seeds, int64_t n, int max_occ, const int64_t *__restrict__ roff,
+                          uint64_t *__restrict__ rows)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t step;
+        const int m = rows_of(seeds[i].x2, max_occ, step);
+        uint64_t *dst = rows + roff[i];
+        for (int c = 0; c < m; ++c) dst[c] = seeds[i].x0 + (uint64_t)c * step;
+    }
+}
+
+// Exclusive scan of int counts into int64 offsets (one block, chunked per thread).
+__global__ void scan_i32(const int *__restrict__ cnt, int64_t n, int64_t *__restrict__ off)
+{
+    __shared__ int64_t part[1024];
+    const int t = threadIdx.x, T = blockDim.x;
+    const int64_t per = (n + T - 1) / T;
+    const int64_t lo = t * per, hi = min(n, lo + per);
+    int64_t s = 0;
+    for (int64_t i = lo; i < hi; ++i) s += cnt[i];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        int64_t acc = 0;
+        for (int i = 0; i < T; ++i) {
+            const int64_t v = part[i];
+            part[i] = acc;
+            acc += v;
+        }
+        off[n] = acc;
+    }
+    __syncthreads();
+    int64_t acc = part[t];
+    for (int64_t i = lo; i < hi; ++i) {
+        off[i] = acc;
+        acc += cnt[i];
+    }
+}
+
+// ---------------------------------------------------------------- chaining
+
+struct Bt {
+    BtNode *nodes;
+    int n_nodes, root;
+    const ChainRec *ch;
+    __device__ int64_t key(int c) const { return ch[c].pos; }
+    __device__ int fresh()
+    {
+        BtNode &x = nodes[n_nodes];
+        x.n = 0;
+        x.internal = 0;
+        return n_nodes++;
+    }
+    // lower bound stepped back unless equal (kbtree.h:116-130); r = 0 when equal
+    __device__ int find(const BtNode &x, int64_t k, int &r) const
+    {
+        int begin = 0, end = x.n;
+        if (x.n == 0) return -1;
+        while (begin < end) {
+            const int mid = (begin + end) >> 1;
+            if (key(x.key[mid]) < k) begin = mid + 1;
+            else end = mid;
+        }
+        if (begin == x.n) { r = 1; return x.n - 1; }
+        const int64_t kb = key(x.key[begin]);
+        r = k < kb ? -1 : (k > kb ? 1 : 0);
+        if (r < 0) --begin;
+        return begin;
+    }
+    __device__ int lower(int64_t k) const                             // kb_intervalp
+    {
+        int lo = -1, xi = root;
+        for (;;) {
+            const BtNode &x = nodes[xi];
+            int r = 0;
+            const int i = find(x, k, r);
+            if (i >= 0 && r == 0) return x.key[i];
+            if (i >= 0) lo = x.key[i];
+            if (!x.internal) return lo;
+            xi = x.child[i + 1];
+        }
+    }
+    __device__ void split(int xi, int i, int yi)                      // kbtree.h:173-190
+    {
+        const int zi = fresh();
+        BtNode &x = nodes[xi], &y = nodes[yi], &z = nodes[zi];
+        z.internal = y.internal;
+        z.n = kBT - 1;
+        for (int j = 0; j < kBT - 1; ++j) z.key[j] = y.key[kBT + j];
+        if (y.internal)
+            for (int j = 0; j < kBT; ++j) z.child[j] = y.child[kBT + j];
+        y.n = kBT - 1;
+        for (int j = x.n; j >= i + 1; --j) x.child[j + 1] = x.child[j];
+        x.child[i + 1] = zi;
+        for (int j = x.n - 1; j >= i; --j) x.key[j + 1] = x.key[j];
+        x.key[i] = y.key[kBT - 1];
+        ++x.n;
+    }
+    __device__ void insert(int c)                                     // kbtree.h:191-223
+    {
+        const int64_t k = key(c);
+        if (nodes[root].n == kBTMax) {
+            const int si = fresh();
+            nodes[si].internal = 1;
+            nodes[si].child[0] = root;
+            root = si;
+            split(si, 0, nodes[si].child[0]);
+        }
+        int xi = root;
+        for (;;) {
+            BtNode &x = nodes[xi];
+            int r;
+            if (!x.internal) {
+                const int i = find(x, k, r);
+                for (int j = x.n - 1; j > i; --j) x.key[j + 1] = x.key[j];
+                x.key[i + 1] = c;
+                ++x.n;
+                return;
+            }
+            int i = find(x, k, r) + 1;
+            if (nodes[x.child[i]].n == kBTMax) {
+                split(xi, i, x.child[i]);
+                if (k > key(nodes[xi].key[i])) ++i;
+            }
+            xi = nodes[xi].child[i];
+        }
+    }
+};
+
+// ks_introsort over chain indices with the comparison w[a] > w[b] (ksort.h:146-226):
+// restated step for step, since chains of equal weight keep the order it leaves.
+struct FltSort {
+    int *a;
+    const int *w;
+    __device__ bool lt(int x, int y) const { return w[x] > w[y]; }
+    __device__ void insertsort(int s, int t)
+    {
+        for (int i = s + 1; i < t; ++i)
+            for (int j = i; j > s && lt(a[j], a[j - 1]); --j) { int tmp = a[j]; a[j] = a[j - 1]; a[j - 1] = tmp; }
+    }
+    __device__ void combsort(int s, size_t n)
+    {
+        const double shrink_factor = 1.2473309501039786540366528676643;
+        int do_swap;
+        size_t gap = n;
+        do {
+            if (gap > 2) {
+                gap = (size_t)(gap / shrink_factor);
+                if (gap == 9 || gap == 10) gap = 11;
+            }
+            do_swap = 0;
+            for (size_t i = 0; i + gap < n; ++i) {
+                const int ii = s + (int)i, jj = ii + (int)gap;
+                if (lt(a[jj], a[ii])) { int tmp = a[ii]; a[ii] = a[jj]; a[jj] = tmp; do_swap = 1; }
+            }
+        } while (do_swap || gap > 2);
+        if (gap != 1) insertsort(s, s + (int)n);
+    }
+    __device__ void sort(int n, int *stk_l, int *stk_r, int *stk_d)
+    {
+        if (n < 1) return;
+        if (n == 2) {
+            if (lt(a[1], a[0])) { int tmp = a[0]; a[0] = a[1]; a[1] = tmp; }
+            return;
+        }
+        int d;
+        for (d = 2; 1ul << d < (unsigned long)n; ++d) ;
+        int top = 0, s = 0, t = n - 1;
+        d <<= 1;
+        for (;;) {
+            if (s < t) {
+                if (--d == 0) {
+                    combsort(s, (size_t)(t - s + 1));
+                    t = s;
+                    continue;
+                }
+                int i = s, j = t, k = i + ((j - i) >> 1) + 1;
+                if (lt(a[k], a[i])) {
+                    if (lt(a[k], a[j])) k = j;
+                } else k = lt(a[j], a[i]) ? i : j;
+                const int rp = a[k];
+                if (k != t) { int tmp = a[k]; a[k] = a[t]; a[t] = tmp; }
+                for (;;) {
+                    do ++i; while (lt(a[i], rp));
+                    do --j; while (i <= j && lt(rp, a[j]));
+                    if (j <= i) break;
+                    int tmp = a[i]; a[i] = a[j]; a[j] = tmp;
+                }
+                { int tmp = a[i]; a[i] = a[t]; a[t] = tmp; }
+                if (i - s > t - i) {
+                    if (i - s > 16) { stk_l[top] = s; stk_r[top] = i - 1; stk_d[top] = d; ++top; }
+                    s = t - i > 16 ? i + 1 : t;
+                } else {
+                    if (t - i > 16) { stk_l[top] = i + 1; stk_r[top] = t; stk_d[top] = d; ++top; }
+                    t = i - s > 16 ? i - 1 : s;
+                }
+            } else {
+                if (top == 0) {
+                    insertsort(0, n);
+                    return;
+                }
+                --top;
+                s = stk_l[top]; t = stk_r[top]; d = stk_d[top];
+            }
+        }
+    }
+};
+
+// One thread per read.  Per-read scratch is carved from arrays sized by the
+// read's SA-row count R (a read never has more chains, seeds or tree nodes
+// than rows).  Outputs the kept chains in mem_chain_flt's order and their
+// seeds (in insertion order) at the read's row offset.
+__global__ void __launch_bounds__(128)
+chain_kernel(AlnOpt opt, DevBns B, int n_reads, const int64_t *__restrict__ read_off,
+             const DevIntv *__restrict__ seeds, const int64_t *__restrict__ seed_off,
+             const int64_t *__restrict__ row_off_of_seed, const uint64_t *__restrict__ pos,
+             ChainRec *__restrict__ chains, BtNode *__restrict__ nodes, int *__restrict__ row_chain,
+             int *__restrict__ iwork, DevSeed *__restrict__ out_seeds, DevChain *__restrict__ out_chains,
+             int *__restrict__ n_chains, int *__restrict__ next)
+{
+    for (;;) {
+        const int r = atomicAdd(next, 1);
+        if (r >= n_reads) break;
+        const int len = (int)(read_off[r + 1] - read_off[r]);
+        const int64_t s0 = seed_off[r], s1 = seed_off[r + 1];
+        const int64_t R0 = row_off_of_seed[s0], R = row_off_of_seed[s1] - R0;
+        n_chains[r] = 0;
+        if (len < opt.min_seed_len || R == 0) continue;
+        ChainRec *ch = chains + R0;
+        BtNode *nd = nodes + R0;
+        int *rc = row_chain + R0;
+        // frac_rep (bwamem.c:271-278)
+        int b = 0, e = 0, l_rep = 0;
+        for (int64_t i = s0; i < s1; ++i) {
+            const int sb = (int)(seeds[i].info >> 32), se = (int)(uint32_t)seeds[i].info;
+            if (seeds[i].x2 <= (uint64_t)opt.max_occ) continue;
+            if (sb > e) l_rep += e - b, b = sb, e = se;
+            else e = e > se ? e : se;
+        }
+        l_rep += e - b;
+        const float frac_rep = (float)l_rep / len;
+        // mem_chain (bwamem.c:279-305)
+        Bt bt;
+        bt.nodes = nd;
+        bt.n_nodes = 0;
+        bt.ch = ch;
+        bt.root = bt.fresh();
+        int n_chn = 0;
+        for (int64_t i = s0; i < s1; ++i) {
+            const DevIntv p = seeds[i];
+            const int slen = (int)((uint32_t)p.info - (uint32_t)(p.info >> 32));
+            const int qbeg = (int)(p.info >> 32);
+            const int64_t rlo = row_off_of_seed[i] - R0, rhi = row_off_of_seed[i + 1] - R0;
+            for (int64_t k = rlo; k < rhi; ++k) {
+                const int64_t rbeg = (int64_t)pos[R0 + k];
+                rc[k] = -1;
+                const int rid = intv2rid(B, rbeg, rbeg + slen);
+                if (rid < 0) continue;
+                bool to_add = true;
+                if (n_chn > 0) {
+                    const int lo = bt.lower(rbeg);
+                    if (lo >= 0) {                               // test_and_merge (bwamem.c:203-227)
+                        ChainRec &c = ch[lo];
+                        const int64_t qend = c.last_qbeg + c.last_len, rend = c.last_rbeg + c.last_len;
+                        if (rid != c.rid) {
+                        } else if (qbeg >= c.first_qbeg && qbeg + slen <= qend && rbeg >= c.first_rbeg &&
+                                   rbeg + slen <= rend) {
+                            to_add = false;                      // contained: the seed is dropped
+                        } else if ((c.last_rbeg < B.l_pac || c.first_rbeg < B.l_pac) && rbeg >= B.l_pac) {
+                        } else {
+                            const int64_t x = qbeg - c.last_qbeg, y = rbeg - c.last_rbeg;
+                            if (y >= 0 && x - y <= opt.w && y - x <= opt.w && x - c.last_len < opt.max_chain_gap &&
+                                y - c.last_len < opt.max_chain_gap) {
+                                c.last_qbeg = qbeg; c.last_rbeg = rbeg; c.last_len = slen;
+                                ++c.n;
+                                rc[k] = lo;
+                                to_add = false;
+                            }
+                        }
+                    }
+                }
+                if (to_add) {
+                    ChainRec &c = ch[n_chn];
+                    c.pos = rbeg; c.first_rbeg = c.last_rbeg = rbeg;
+                    c.first_qbeg = c.last_qbeg = qbeg; c.last_len = slen;
+                    c.n = 1; c.rid = rid;
+                    rc[k] = n_chn;
+                    bt.insert(n_chn);
+                    ++n_chn;
+                }
+            }
+        }
+        if (n_chn == 0) continue;
+        // iwork layout (R ints each): order | seed start | weight | sort stack (3 x 64)
+        int *order = iwork + R0 * 3, *sstart = order + R, *wgt = order + 2 * R;
+        // in-order traversal (__kb_traverse); a t = 5 B-tree over < 2^31 keys is < 16 levels deep
+        {
+            int n_ord = 0;
+            int stk_x[40], stk_i[40];
+            int sp = 0;
+            stk_x[0] = bt.root; stk_i[0] = 0;
+            for (;;) {
+                while (stk_x[sp] >= 0 && stk_i[sp] <= nd[stk_x[sp]].n) {
+                    const BtNode &x = nd[stk_x[sp]];
+                    stk_x[sp + 1] = x.internal ? x.child[stk_i[sp]] : -1;
+                    stk_i[sp + 1] = 0;
+                    ++sp;
+                }
+                --sp;
+                if (sp >= 0) {
+                    const int xi = stk_x[sp];
+                    if (xi >= 0 && stk_i[sp] < nd[xi].n) order[n_ord++] = nd[xi].key[stk_i[sp]];
+                    ++stk_i[sp];
+                } else break;
+            }
+        }
+        // seeds grouped by chain in insertion order: chain c's seeds start at sstart[c]
+        for (int c = 0; c < n_chn; ++c) sstart[c] = 0;
+        for (int64_t k = 0; k < R; ++k) if (rc[k] >= 0) ++sstart[rc[k]];
+        {
+            int acc = 0;
+            for (int c = 0; c < n_chn; ++c) { const int v = sstart[c]; sstart[c] = acc; acc += v; }
+        }
+        DevSeed *sd = out_seeds + R0;
+        {
+            // place seeds; wgt[] counts per chain while placing
+            for (int c = 0; c < n_chn; ++c) wgt[c] = 0;
+            for (int64_t i = s0; i < s1; ++i) {
+                const DevIntv p = seeds[i];
+                const int slen = (int)((uint32_t)p.info - (uint32_t)(p.info >> 32));
+                const int64_t rlo = row_off_of_seed[i] - R0, rhi = row_off_of_seed[i + 1] - R0;
+                for (int64_t k = rlo; k < rhi; ++k) {
+                    const int c = rc[k];
+                    if (c < 0) continue;
+                    DevSeed s;
+                    s.rbeg = (int64_t)pos[R0 + k];
+                    s.qbeg = (int)(p.info >> 32);
+                    s.len = s.score = slen;
+                    s.pad = 0;
+                    sd[sstart[c] + wgt[c]++] = s;
+                }
+            }
+        }
+        // mem_chain_weight (bwamem.c:229-250) per chain, indexed by tree order
+        for (int c = 0; c < n_chn; ++c) {
+            const DevSeed *s = sd + sstart[c];
+            const int n = ch[c].n;
+            int64_t end = 0;
+            int w = 0, tmp;
+            for (int j = 0; j < n; ++j) {
+                if (s[j].qbeg >= end) w += s[j].len;
+                else if (s[j].qbeg + s[j].len > end) w += (int)(s[j].qbeg + s[j].len - end);
+                end = end > s[j].qbeg + s[j].len ? end : s[j].qbeg + s[j].len;
+            }
+            tmp = w; w = 0; end = 0;
+            for (int j = 0; j < n; ++j) {
+                if (s[j].rbeg >= end) w += s[j].len;
+                else if (s[j].rbeg + s[j].len > end) w += (int)(s[j].rbeg + s[j].len - end);
+                end = end > s[j].rbeg + s[j].len ? end : s[j].rbeg + s[j].len;
+            }
+            w = w < tmp ? w : tmp;
+            wgt[c] = w < (1 << 30) ? w : (1 << 30) - 1;
+        }
+        // mem_chain_flt (bwamem.c:331-389): drop light chains, sort by weight, mark kept
+        int n = 0;
+        for (int k = 0; k < n_chn; ++k)
+            if (wgt[order[k]] >= opt.min_chain_weight) order[n++] = order[k];
+        if (n == 0) continue;
+        {
+            int stk_l[64], stk_r[64], stk_d[64];
+            FltSort fs{order, wgt};
+            fs.sort(n, stk_l, stk_r, stk_d);
+        }
+        DevChain *oc = out_chains + R0;              // working copy, compacted at the end
+        for (int k = 0; k < n; ++k) {
+            const int c = order[k];
+            oc[k].n = ch[c].n; oc[k].rid = ch[c].rid; oc[k].w = wgt[c];
+            oc[k].kept = 0; oc[k].first = -1; oc[k].seed_off = sstart[c];
+            oc[k].frac_rep = frac_rep; oc[k].pad = 0;
+        }
+        {
+            // kept chain indices reuse rc[] (rows are no longer needed)
+            int *kept = rc, n_kept = 0;
+            oc[0].kept = 3;
+            kept[n_kept++] = 0;
+            for (int i = 1; i < n; ++i) {
+                int large_ovlp = 0, k;
+                const DevSeed *si = sd + oc[i].seed_off;
+                const int bi = si[0].qbeg, ei = si[oc[i].n - 1].qbeg + si[oc[i].n - 1].len;
+                for (k = 0; k < n_kept; ++k) {
+                    const int j = kept[k];
+                    const DevSeed *sj = sd + oc[j].seed_off;
+                    const int bj = sj[0].qbeg, ej = sj[oc[j].n - 1].qbeg + sj[oc[j].n - 1].len;
+                    const int b_max = bj > bi ? bj : bi, e_min = ej < ei ? ej : ei;
+                    if (e_min > b_max) {                  // no ALT contigs: the is_alt test always passes
+                        const int li = ei - bi, lj = ej - bj, min_l = li < lj ? li : lj;
+                        if (e_min - b_max >= min_l * opt.mask_level && min_l < opt.max_chain_gap) {
+                            large_ovlp = 1;
+                            if (oc[j].first < 0) oc[j].first = i;
+                            if (oc[i].w < oc[j].w * opt.drop_ratio && oc[j].w - oc[i].w >= opt.min_seed_len << 1)
+                                break;
+                        }
+                    }
+                }
+                if (k == n_kept) {
+                    kept[n_kept++] = i;
+                    oc[i].kept = large_ovlp ? 2 : 3;
+                }
+            }
+            for (int i = 0; i < n_kept; ++i)
+                if (oc[kept[i]].first >= 0) oc[oc[kept[i]].first].kept = 1;
+            int i, k = 0;
+            for (i = 0; i < n; ++i) {
+                if (oc[i].kept == 0 || oc[i].kept == 3) continue;
+                if (++k >= opt.max_chain_extend) break;
+            }
+            for (; i < n; ++i)
+                if (oc[i].kept < 3) oc[i].kept = 0;
+            for (i = k = 0; i < n; ++i)
+                if (oc[i].kept != 0) oc[k++] = oc[i];
+            n_chains[r] = k;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- chain2aln
+
+// Query base j and target base i of one extension: q(j) = read[q0 + qdir*j],
+// t(i) = text base at t0 + tdir*i.  Left extensions run on both reversed,
+// as the reference's reversed copies do (bwamem.c:721-724).
+struct ReadRefAcc {
+    const uint8_t *read;
+    int q0, qdir;
+    int64_t t0;
+    int tdir;
+    DevBns B;
+    __device__ __forceinline__ int q(int j) const { return read[q0 + qdir * j]; }
+    __device__ __forceinline__ int t(int i) const { return text_base(B, t0 + (int64_t)tdir * i); }
+};
+
+__device__ __forceinline__ int cal_max_gap(const AlnOpt &o, int qlen)         // bwamem.c:625-632
+{
+    const int l_del = (int)((double)(qlen * o.a - o.o_del) / o.e_del + 1.);
+    const int l_ins = (int)((double)(qlen * o.a - o.o_ins) / o.e_ins + 1.);
+    int l = l_del > l_ins ? l_del : l_ins;
+    l = l > 1 ? l : 1;
+    return l < o.w << 1 ? l : o.w << 1;
+}
+
+template <int C>
+__device__ KswResult run_ext(const KswParams &P, int qlen, int tlen, int h0, int w, int eb, const ReadRefAcc &acc,
+                             int lane)
+{
+    return ksw_warp<C>(P, qlen, tlen, h0, w, eb, acc, lane);
+}
+
+__device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, int w, int eb, const ReadRefAcc &acc,
+                                int lane)
+{
+    const int need = (qlen + 32) >> 5;
+    switch (need) {
+    case 1: return run_ext<1>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 2: return run_ext<2>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 3: return run_ext<3>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 4: return run_ext<4>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 5: return run_ext<5>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 6: return run_ext<6>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 7: return run_ext<7>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 8: return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
+    case 9: case 10: case 11: case 12: return run_ext<12>(P, qlen, tlen, h0, w, eb, acc, lane);
+    default: return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
+    }
+}
+
+// One warp per read.  regs: the read's region slots start at its row offset.
+__global__ void __launch_bounds__(128)
+chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *__restrict__ reads,
+                 const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
+                 const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
+                 const DevChain *__restrict__ chains, const int *__restrict__ n_chains, uint64_t *__restrict__ srt_buf,
+                 bsb_reg_t *__restrict__ regs, int *__restrict__ n_regs, int *__restrict__ next)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(next, 1);
+        r = __shfl_sync(BSB_FULL_MASK, r, 0);
+        if (r >= n_reads) break;
+        const int64_t R0 = row_off_of_seed[seed_off[r]];
+        const int nc = n_chains[r];
+        const int l_query = (int)(read_off[r + 1] - read_off[r]);
+        const uint8_t *query = reads + read_off[r];
+        const DevSeed *sd = seeds + R0;
+        const DevChain *chn = chains + R0;
+        bsb_reg_t *av = regs + R0;
+        uint64_t *srt = srt_buf + R0;
+        int nav = 0;
+        const int64_t l_pac = B.l_pac;
+        for (int ci = 0; ci < nc; ++ci) {
+            const DevChain c = chn[ci];
+            const DevSeed *cs = sd + c.seed_off;
+            if (c.n == 0) continue;
+            // the widest target span any seed can use (bwamem.c:646-661)
+            int64_t rmax0 = l_pac << 1, rmax1 = 0;
+            for (int i = 0; i < c.n; ++i) {
+                const DevSeed t = cs[i];
+                const int64_t b = t.rbeg - (t.qbeg + cal_max_gap(opt, t.qbeg));
+                const int64_t e = t.rbeg + t.len + ((l_query - t.qbeg - t.len) + cal_max_gap(opt, l_query - t.qbeg - t.len));
+                rmax0 = rmax0 < b ? rmax0 : b;
+                rmax1 = rmax1 > e ? rmax1 : e;
+            }
+            rmax0 = rmax0 > 0 ? rmax0 : 0;
+            rmax1 = rmax1 < l_pac << 1 ? rmax1 : l_pac << 1;
+            if (rmax0 < l_pac && l_pac < rmax1) {
+                if (cs[0].rbeg < l_pac) rmax1 = l_pac;
+                else rmax0 = l_pac;
+            }
+            {   // bns_fetch_seq's clip to the contig of the first seed (bntseq.c:436-461)
+                int is_rev;
+                const int rid = pos2rid(B, depos(B, cs[0].rbeg, is_rev));
+                int64_t far_beg = B.ann_offset[rid], far_end = far_beg + B.ann_len[rid];
+                if (is_rev) {
+                    const int64_t t = far_beg;
+                    far_beg = (l_pac << 1) - far_end;
+                    far_end = (l_pac << 1) - t;
+                }
+                rmax0 = rmax0 > far_beg ? rmax0 : far_beg;
+                rmax1 = rmax1 < far_end ? rmax1 : far_end;
+            }
+            // seeds by (score, index) ascending; keys are distinct, so ranks give ks_introsort_64's order
+            for (int i = lane; i < c.n; i += 32) {
+                const uint64_t ki = (uint64_t)(uint32_t)cs[i].score << 32 | (uint32_t)i;
+                int rank = 0;
+                for (int j = 0; j < c.n; ++j)
+                    rank += ((uint64_t)(uint32_t)cs[j].score << 32 | (uint32_t)j) < ki;
+                srt[rank] = ki;
+            }
+            __syncwarp();
+            for (int k = c.n - 1; k >= 0; --k) {
+                const DevSeed s = cs[(uint32_t)srt[k]];
+                // is the seed (almost) contained in a region of this read already? (bwamem.c:675-690)
+                int hit = nav;
+                for (int i0 = 0; i0 < nav && hit == nav; i0 += 32) {
+                    const int i = i0 + lane;
+                    bool ok = false;
+                    if (i < nav) {
+                        const bsb_reg_t p = av[i];
+                        if (!(s.rbeg < p.rb || s.rbeg + s.len > p.re || s.qbeg < p.qb || s.qbeg + s.len > p.qe) &&
+                            !(s.len - p.seedlen0 > .1 * l_query)) {
+                            int qd = s.qbeg - p.qb;
+                            int64_t rd = s.rbeg - p.rb;
+                            int max_gap = cal_max_gap(opt, qd < rd ? qd : (int)rd);
+                            int w = max_gap < p.w ? max_gap : p.w;
+                            if (qd - rd < w && rd - qd < w) ok = true;
+                            else {
+                                qd = p.qe - (s.qbeg + s.len);
+                                rd = p.re - (s.rbeg + s.len);
+                                max_gap = cal_max_gap(opt, qd < rd ? qd : (int)rd);
+                                w = max_gap < p.w ? max_gap : p.w;
+                                ok = qd - rd < w && rd - qd < w;
+                            }
+                        }
+                    }
+                    const unsigned m = __ballot_sync(BSB_FULL_MASK, ok);
+                    if (m) hit = i0 + __ffs(m) - 1;
+                }
+                if (hit < nav) {   // contained: extend only if an overlapping seed may lead elsewhere (bwamem.c:691-707)
+                    int found = c.n;
+                    for (int i0 = k + 1; i0 < c.n && found == c.n; i0 += 32) {
+                        const int i = i0 + lane;
+                        bool ok = false;
+                        if (i < c.n && srt[i] != 0) {
+                            const DevSeed t = cs[(uint32_t)srt[i]];
+                            if (!(t.len < s.len * .95)) {
+                                if (s.qbeg <= t.qbeg && s.qbeg + s.len - t.qbeg >= s.len >> 2 &&
+                                    t.qbeg - s.qbeg != t.rbeg - s.rbeg)
+                                    ok = true;
+                                else if (t.qbeg <= s.qbeg && t.qbeg + t.len - s.qbeg >= s.len >> 2 &&
+                                         s.qbeg - t.qbeg != s.rbeg - t.rbeg)
+                                    ok = true;
+                            }
+                        }
+                        const unsigned m = __ballot_sync(BSB_FULL_MASK, ok);
+                        if (m) found = i0 + __ffs(m) - 1;
+                    }
+                    if (found == c.n) {
+                        __syncwarp();
+                        if (lane == 0) srt[k] = 0;
+                        __syncwarp();
+                        continue;
+                    }
+                }
+                bsb_reg_t a;
+                memset(&a, 0, sizeof a);
+                int aw0 = opt.w, aw1 = opt.w;
+                a.w = opt.w;
+                a.score = a.truesc = -1;
+                a.rid = c.rid;
+                if (s.qbeg) {      // left extension (bwamem.c:715-748)
+                    ReadRefAcc acc{query, s.qbeg - 1, -1, s.rbeg - 1, -1, B};
+                    const int tlen = (int)(s.rbeg - rmax0);
+                    KswResult x;
+                    for (int i = 0; i < 2; ++i) {
+                        const int prev = a.score;
+                        aw0 = opt.w << i;
+                        x = extend_any(P, s.qbeg, tlen, s.len * opt.a, aw0, opt.pen_clip5, acc, lane);
+                        a.score = x.score;
+                        if (a.score == prev || x.max_off < (aw0 >> 1) + (aw0 >> 2)) break;
+                    }
+                    if (x.gscore <= 0 || x.gscore <= a.score - opt.pen_clip5) {
+                        a.qb = s.qbeg - x.qle, a.rb = s.rbeg - x.tle;
+                        a.truesc = a.score;
+                    } else {
+                        a.qb = 0, a.rb = s.rbeg - x.gtle;
+                        a.truesc = x.gscore;
+                    }
+                } else a.score = a.truesc = s.len * opt.a, a.qb = 0, a.rb = s.rbeg;
+                if (s.qbeg + s.len != l_query) {   // right extension (bwamem.c:750-775)
+                    const int qe = s.qbeg + s.len, sc0 = a.score;
+                    const int re = (int)(s.rbeg + s.len - rmax0);
+                    ReadRefAcc acc{query, qe, 1, rmax0 + re, 1, B};
+                    const int tlen = (int)(rmax1 - rmax0 - re);
+                    KswResult x;
+                    for (int i = 0; i < 2; ++i) {
+                        const int prev = a.score;
+                        aw1 = opt.w << i;
+                        x = extend_any(P, l_query - qe, tlen, sc0, aw1, opt.pen_clip3, acc, lane);
+                        a.score = x.score;
+                        if (a.score == prev || x.max_off < (aw1 >> 1) + (aw1 >> 2)) break;
+                    }
+                    if (x.gscore <= 0 || x.gscore <= a.score - opt.pen_clip3) {
+                        a.qe = qe + x.qle, a.re = rmax0 + re + x.tle;
+                        a.truesc += a.score - sc0;
+                    } else {
+                        a.qe = l_query, a.re = rmax0 + re + x.gtle;
+                        a.truesc += x.gscore - sc0;
+                    }
+                } else a.qe = l_query, a.re = s.rbeg + s.len;
+                int cov = 0;      // seedcov (bwamem.c:779-783)
+                for (int i = lane; i < c.n; i += 32) {
+                    const DevSeed t = cs[i];
+                    if (t.qbeg >= a.qb && t.qbeg + t.len <= a.qe && t.rbeg >= a.rb && t.rbeg + t.len <= a.re) cov += t.len;
+                }
+                a.seedcov = __reduce_add_sync(BSB_FULL_MASK, cov);
+                a.w = aw0 > aw1 ? aw0 : aw1;
+                a.seedlen0 = s.len;
+                a.frac_rep = c.frac_rep;
+                if (lane == 0) av[nav] = a;
+                ++nav;
+                __syncwarp();
+            }
+        }
+        if (lane == 0) n_regs[r] = nav;
+    }
+}
+
+__global__ void compact_regs(const bsb_reg_t *__restrict__ regs, const int64_t *__restrict__ seed_off,
+                             const int64_t *__restrict__ row_off_of_seed, int n_reads, const int *__restrict__ n_regs,
+                             const int64_t *__restrict__ out_off, bsb_reg_t *__restrict__ out)
+{
+    for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
+        const bsb_reg_t *src = regs + row_off_of_seed[seed_off[r]];
+        for (int i = threadIdx.x; i < n_regs[r]; i += blockDim.x) out[out_off[r] + i] = src[i];
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host driver
+
+struct AlignScratch {
+    int *rcnt;                   // per seed interval: SA rows
+    int64_t *roff;               // n_seeds + 1
+    uint64_t *rows, *pos;
+    ChainRec *chains;
+    BtNode *nodes;
+    int *row_chain, *iwork;
+    DevSeed *cseeds;
+    DevChain *cchains;
+    uint64_t *srt;
+    bsb_reg_t *regs;
+    int *n_chains, *n_regs, *ctrl;
+    int64_t *reg_off;
+};
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_reads, const uint8_t *d_reads,
+                       const int64_t *d_read_off, const bsb_intv_t *d_seeds, const int64_t *d_seed_off,
+                       int64_t n_seeds, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out, int64_t *n_regs_total)
+{
+    int rc;
+    cudaStream_t st = ctx->stream;
+    const int nb = ctx->n_sm * 4;
+    // rows per seed interval and their offsets
+    size_t need = al(sizeof(int) * (n_seeds + 1)) + al(sizeof(int64_t) * (n_seeds + 1));
+    if ((rc = bsb_ensure(ctx, &ctx->arena0, &ctx->arena0_bytes, need, "chain scratch (rows)"))) return rc;
+    int *rcnt = (int *)ctx->arena0;
+    int64_t *roff = (int64_t *)((char *)ctx->arena0 + al(sizeof(int) * (n_seeds + 1)));
+    if (n_seeds > 0) {
+        rows_count<<<nb, 256, 0, st>>>((const DevIntv *)d_seeds, n_seeds, o->max_occ, rcnt);
+    }
+    scan_i32<<<1, 1024, 0, st>>>(rcnt, n_seeds, roff);
+    int64_t R = 0;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&R, roff + n_seeds, 8, cudaMemcpyDeviceToHost, st), "row total"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "row count"))) return rc;
+    // per-row arrays (all sized by R)
+    const size_t Rb = (size_t)(R > 0 ? R : 1);
+    size_t off = 0;
+    const size_t o_rows = off; off += al(8 * Rb);
+    const size_t o_pos = off; off += al(8 * Rb);
+    const size_t o_chains = off; off += al(sizeof(ChainRec) * Rb);
+    const size_t o_nodes = off; off += al(sizeof(BtNode) * (Rb + 2));
+    const size_t o_rowc = off; off += al(sizeof(int) * Rb);
+    const size_t o_iwork = off; off += al(sizeof(int) * 3 * Rb);
+    const size_t o_cseeds = off; off += al(sizeof(DevSeed) * Rb);
+    const size_t o_cchains = off; off += al(sizeof(DevChain) * Rb);
+    const size_t o_srt = off; off += al(8 * Rb);
+    const size_t o_regs = off; off += al(sizeof(bsb_reg_t) * Rb);
+    const size_t o_nch = off; off += al(sizeof(int) * (n_reads + 1));
+    const size_t o_nreg = off; off += al(sizeof(int) * (n_reads + 1));
+    const size_t o_ctrl = off; off += al(sizeof(int) * 4);
+    const size_t o_regoff = off; off += al(sizeof(int64_t) * (n_reads + 1));
+    const size_t o_out = off; off += al(sizeof(bsb_reg_t) * Rb);
+    if ((rc = bsb_ensure(ctx, &ctx->arena1, &ctx->arena1_bytes, off, "chain scratch"))) return rc;
+    char *A = (char *)ctx->arena1;
+    uint64_t *rows = (uint64_t *)(A + o_rows), *pos = (uint64_t *)(A + o_pos);
+    ChainRec *chains = (ChainRec *)(A + o_chains);
+    BtNode *nodes = (BtNode *)(A + o_nodes);
+    int *row_chain = (int *)(A + o_rowc), *iwork = (int *)(A + o_iwork);
+    DevSeed *cseeds = (DevSeed *)(A + o_cseeds);
+    DevChain *cchains = (DevChain *)(A + o_cchains);
+    uint64_t *srt = (uint64_t *)(A + o_srt);
+    bsb_reg_t *regs = (bsb_reg_t *)(A + o_regs), *regs_out = (bsb_reg_t *)(A + o_out);
+    int *n_chains = (int *)(A + o_nch), *n_regs = (int *)(A + o_nreg), *ctrl = (int *)(A + o_ctrl);
+    int64_t *reg_off = (int64_t *)(A + o_regoff);
+    if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ctrl, 0, sizeof(int) * 4, st), "ctrl"))) return rc;
+    if (n_seeds > 0 && R > 0) {
+        rows_fill<<<nb, 256, 0, st>>>((const DevIntv *)d_seeds, n_seeds, o->max_occ, roff, rows);
+        cudaError_t e = bsb_sa_launch_ctx(ctx, rows, R, pos);
+        if (e != cudaSuccess) return bsb_cuda(ctx, e, "SA rows");
+    }
+    AlnOpt ao;
+    ao.a = o->a; ao.o_del = o->o_del; ao.e_del = o->e_del; ao.o_ins = o->o_ins; ao.e_ins = o->e_ins;
+    ao.w = o->w; ao.zdrop = o->zdrop; ao.pen_clip5 = o->pen_clip5; ao.pen_clip3 = o->pen_clip3;
+    ao.min_seed_len = o->min_seed_len; ao.max_occ = o->max_occ; ao.max_chain_gap = o->max_chain_gap;
+    ao.min_chain_weight = o->min_chain_weight; ao.max_chain_extend = o->max_chain_extend;
+    ao.mask_level = o->mask_level; ao.drop_ratio = o->drop_ratio;
+    DevBns B;
+    B.ann_offset = (const int64_t *)ctx->idx_ann_off;
+    B.ann_len = (const int32_t *)ctx->idx_ann_len;
+    B.n_seqs = ctx->n_seqs;
+    B.l_pac = ctx->l_pac;
+    B.pac = (const uint8_t *)ctx->idx_pac;
+    KswParams P;
+    memcpy(P.mat, o->mat, 25);
+    P.o_del = o->o_del; P.e_del = o->e_del; P.o_ins = o->o_ins; P.e_ins = o->e_ins; P.zdrop = o->zdrop;
+    int mx = 0;
+    for (int i = 0; i < 25; ++i) mx = mx > o->mat[i] ? mx : o->mat[i];
+    P.mat_max = mx;
+    chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
+                                                 pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
+    chain2aln_kernel<<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff, cseeds,
+                                                     cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+    scan_i32<<<1, 1024, 0, st>>>(n_regs, n_reads, reg_off);
+    compact_regs<<<ctx->n_sm * 4, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return bsb_cuda(ctx, e, "chain/extension launch");
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(n_regs_total, reg_off + n_reads, 8, cudaMemcpyDeviceToHost, st), "reg total")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "chain/extension"))) return rc;
+    *d_regs_out = regs_out;
+    *d_reg_off_out = reg_off;
+    return 0;
+}
+
+extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                                    const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index || !ctx->idx_pac || !ctx->idx_ann_off)
+        return bsb_fail(ctx, BSB_ENOINDEX, "no index with pac and contig table loaded");
+    if (!o || !offs || n_reads < 0 || (n_reads > 0 && (!seqs || !regs || !regs_off)))
+        return bsb_fail(ctx, BSB_EINVAL, "NULL argument");
+    if (o->e_del < 1 || o->e_ins < 1 || o->o_del < 0 || o->o_ins < 0 || o->a < 1 || o->w < 0 || o->max_occ < 1 ||
+        o->min_seed_len < 1 || o->max_chain_extend < 1)
+        return bsb_fail(ctx, BSB_EINVAL, "unsupported options");
+    if (n_reads == 0) {
+        regs_off[0] = 0;
+        return 0;
+    }
+    int max_len = 0;
+    for (int r = 0; r < n_reads; ++r) {
+        const int64_t l = offs[r + 1] - offs[r];
+        if (l < 0) return bsb_fail(ctx, BSB_EINVAL, "read %d: negative length", r);
+        if (l > BSB_ALIGN_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld > %d", r, (long long)l, BSB_ALIGN_MAX_LEN);
+        // mem_flt_chained_seeds (bwamem.c:604-606) runs its seed-level SW only past this
+        // point; reads shorter than min_seed_len never have chains (bwamem.c:266)
+        const double min_l = o->min_chain_weight ? 1.1f * o->min_chain_weight : 5.5f * log((double)l);
+        if (l >= o->min_seed_len && !(min_l > 0.05f * l))
+            return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld needs the seed-level SW filter", r, (long long)l);
+        if (l > max_len) max_len = (int)l;
+    }
+    const int64_t total = offs[n_reads] - offs[0];
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    const size_t off_b = sizeof(int64_t) * ((size_t)n_reads + 1);
+    const size_t seq_b = al((size_t)total);
+    const size_t seeds_b = al(((size_t)2 * total + 32 * (size_t)n_reads) * sizeof(bsb_intv_t));
+    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, seq_b + 2 * al(off_b) + 256, "align input staging")))
+        return rc;
+    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, seeds_b + 256, "align seed buffer"))) return rc;
+    uint8_t *d_reads = (uint8_t *)ctx->d_in;
+    int64_t *d_offs = (int64_t *)((char *)ctx->d_in + seq_b);
+    int64_t *d_seed_off = (int64_t *)((char *)d_offs + al(off_b));
+    bsb_intv_t *d_seeds = (bsb_intv_t *)ctx->d_out;
+    std::vector<int64_t> rel(n_reads + 1);
+    for (int r = 0; r <= n_reads; ++r) rel[r] = offs[r] - offs[0];
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_reads, seqs + offs[0], total, cudaMemcpyHostToDevice, ctx->stream), "H2D reads")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_offs, rel.data(), off_b, cudaMemcpyHostToDevice, ctx->stream), "H2D offsets")))
+        return rc;
+    bsb_seed_opt_t so;
+    so.min_seed_len = o->min_seed_len; so.split_factor = o->split_factor;
+    so.split_width = o->split_width; so.max_mem_intv = o->max_mem_intv;
+    if ((rc = bsb_seed_batch_device(ctx, &so, n_reads, d_reads, d_offs, total, max_len, d_seeds, d_seed_off))) return rc;
+    int64_t n_seeds = 0;
+    int ctrl[2] = {0, 0};
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&n_seeds, d_seed_off + n_reads, 8, cudaMemcpyDeviceToHost, ctx->stream), "seed total")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream), "seed ctrl")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seeding"))) return rc;
+    if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
+    bsb_reg_t *d_regs = nullptr;
+    int64_t *d_reg_off = nullptr, n_regs = 0;
+    if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, &d_regs, &d_reg_off,
+                                 &n_regs)))
+        return rc;
+    if (n_regs > max_regs)
+        return bsb_fail(ctx, BSB_EINVAL, "%lld regions do not fit max_regs %lld", (long long)n_regs, (long long)max_regs);
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(regs_off, d_reg_off, off_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H offsets")))
+        return rc;
+    if (n_regs > 0 &&
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(regs, d_regs, sizeof(bsb_reg_t) * n_regs, cudaMemcpyDeviceToHost, ctx->stream),
+                       "D2H regions")))
+        return rc;
+    return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "align batch");
+}

@@ -28,7 +28,7 @@
 #include <climits>
 #include <cstdio>
 
-#include "bsb_internal.cuh"
+#include "ksw_core.cuh"
 
 namespace {
 
@@ -51,226 +51,12 @@ __host__ __device__ inline int tile_bin(int qlen)
     return -1;
 }
 
-// Sign-extended byte of x chosen by a prmt selector (bit 3 of each selector
-// nibble replicates the sign of the chosen byte, PTX ISA prmt.b32 default mode).
-__device__ __forceinline__ int prmt_sext(uint32_t x, uint32_t sel)
-{
-    uint32_t r;
-    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "r"(sel));
-    return (int)r;
-}
-
-__device__ __forceinline__ uint32_t sext_selector(int byte)
-{
-    const uint32_t b = (uint32_t)byte, r = b | 8u;
-    return b | r << 4 | r << 8 | r << 12;
-}
-
-// Extends one job with the calling warp.  All control values are warp-uniform.
-//
-// Register state per lane, columns j = lane*C + s:
-//   Hs[s] = eh[j].h = H(i-1, j-1),  Es[s] = eh[j].e = E(i, j)   (ksw.c:376-378)
-// Invariant: every column left of the band (j < beg) holds H = E = 0.  The
-// reference never reads those cells again (beg only grows), and with them at
-// zero the F scan and the row maximum need no left-edge masks: a dead column
-// has M = 0, T = 0, V = e_ins*(j+1), F = 0 and H = 0.  The shrink step only
-// moves beg over cells that are already zero; when the band edge i-w moves
-// beg instead, the cells it passes are zeroed explicitly.
-template <int C>
-__device__ __forceinline__ void ksw_one(const KswParams &P, const bsb_ext_job_t &jb,
-                                        const uint8_t *__restrict__ seq, int lane,
-                                        bsb_ext_out_t *__restrict__ o, int64_t *__restrict__ cell_out)
-{
-    const int qlen = jb.qlen, tlen = jb.tlen, h0 = jb.h0;
-    const uint8_t *__restrict__ q = seq + jb.qoff;
-    const uint8_t *__restrict__ t = seq + jb.toff;
-    const int o_del = P.o_del, e_del = P.e_del, o_ins = P.o_ins, e_ins = P.e_ins;
-    const int oe_del = o_del + e_del, oe_ins = o_ins + e_ins;
-    const int base = lane * C;
-
-    // query profile: byte c of prof[s] = mat[c*5 + q[j]] for target bases 0..3;
-    // the N row (target base 4) is kept apart in profN, four slots per word.
-    uint32_t prof[C];
-    uint32_t profN[(C + 3) / 4];
-    int Hs[C], Es[C];
-#pragma unroll
-    for (int s = 0; s < (C + 3) / 4; ++s) profN[s] = 0;
-    const int h1run = max(h0 - oe_ins, 0);
-#pragma unroll
-    for (int s = 0; s < C; ++s) {
-        const int j = base + s;
-        const int qc = j < qlen ? q[j] : 0;
-        prof[s] = (uint32_t)(uint8_t)P.mat[qc] | (uint32_t)(uint8_t)P.mat[5 + qc] << 8 |
-                  (uint32_t)(uint8_t)P.mat[10 + qc] << 16 | (uint32_t)(uint8_t)P.mat[15 + qc] << 24;
-        profN[s >> 2] |= (uint32_t)(uint8_t)P.mat[20 + qc] << ((s & 3) * 8);
-        // first row: h0, then an insertion run clipped at zero (ksw.c:395-397)
-        Hs[s] = j == 0 ? h0 : (j <= qlen ? max(h1run - e_ins * (j - 1), 0) : 0);
-        Es[s] = 0;
-    }
-
-    // band clamp with the reference's double arithmetic (ksw.c:399-407)
-    int w = jb.w;
-    {
-        int max_ins = (int)((double)(qlen * P.mat_max + jb.end_bonus - o_ins) / e_ins + 1.);
-        max_ins = max_ins > 1 ? max_ins : 1;
-        w = w < max_ins ? w : max_ins;
-        int max_del = (int)((double)(qlen * P.mat_max + jb.end_bonus - o_del) / e_del + 1.);
-        max_del = max_del > 1 ? max_del : 1;
-        w = w < max_del ? w : max_del;
-    }
-
-    int best = h0, best_i = -1, best_j = -1, max_ie = -1, gscore = -1, max_off = 0;
-    int beg = 0, end = qlen;
-    long long ncell = 0;
-    const int q_lane = qlen / C, q_slot = qlen % C;   // owner of column qlen
-
-    // target bases arrive 32 rows at a time, one byte per lane, next chunk prefetched
-    uint32_t tch = lane < tlen ? t[lane] : 4u;
-    uint32_t tnext = 32 + lane < tlen ? t[32 + lane] : 4u;
-
-    for (int i = 0; i < tlen; ++i) {
-        const int tc = (int)__shfl_sync(BSB_FULL_MASK, tch, i & 31);
-        if ((i & 31) == 31) {
-            tch = tnext;
-            const int ti = i + 33 + lane;
-            tnext = ti < tlen ? t[ti] : 4u;
-        }
-        // band of this row (ksw.c:416-419)
-        if (beg < i - w) {
-            beg = i - w;
-#pragma unroll
-            for (int s = 0; s < C; ++s)
-                if (base + s < beg) Hs[s] = 0, Es[s] = 0;
-        }
-        if (end > i + w + 1) end = i + w + 1;
-        if (end > qlen) end = qlen;
-        // H(i,-1) (ksw.c:421-424)
-        const int h1_init = beg == 0 ? max(h0 - (o_del + e_del * (i + 1)), 0) : 0;
-
-        if (beg >= end) {
-            // empty band: the reference's loop does not run, eh[end] gets {h1,0},
-            // the query-end test sees j == beg, and the zero row max stops it.
-            if (beg == qlen) {
-                max_ie = gscore > h1_init ? max_ie : i;
-                gscore = gscore > h1_init ? gscore : h1_init;
-            }
-            break;
-        }
-
-        // ---- pass 1: M, next-row E, and the F-scan operand V = T(j) + e_ins*(j+1)
-        int Mv[C], En[C], Pf[C];
-        int run = 0;
-        if (tc < 4) {
-            const uint32_t sel = sext_selector(tc);
-#pragma unroll
-            for (int s = 0; s < C; ++s) {
-                const int j = base + s;
-                const int sc = prmt_sext(prof[s], sel);
-                const int Hp = Hs[s];
-                const int M = Hp ? Hp + sc : 0;
-                const int Ti = __viaddmax_s32(M, -oe_ins, 0);
-                En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
-                run = max(run, Ti + e_ins * (j + 1));
-                Pf[s] = run;
-                Mv[s] = M;
-            }
-        } else {
-#pragma unroll
-            for (int s = 0; s < C; ++s) {
-                const int j = base + s;
-                const int sc = prmt_sext(profN[s >> 2], sext_selector(s & 3));
-                const int Hp = Hs[s];
-                const int M = Hp ? Hp + sc : 0;
-                const int Ti = __viaddmax_s32(M, -oe_ins, 0);
-                En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
-                run = max(run, Ti + e_ins * (j + 1));
-                Pf[s] = run;
-                Mv[s] = M;
-            }
-        }
-
-        // ---- warp exclusive prefix max of the lane totals (lane 0 starts from 0 = F at column 0)
-        int incl = run;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) incl = max(incl, __shfl_up_sync(BSB_FULL_MASK, incl, d));
-        const int excl = __shfl_up_sync(BSB_FULL_MASK, incl, 1);
-        const int carry = lane == 0 ? 0 : excl;
-
-        // ---- pass 2: H, the row-max key (H << 10 | j), and the new eh[] (H shifted one column)
-        int kmax = -1, prevH = 0;
-        uint32_t nzb = 0;
-#pragma unroll
-        for (int s = 0; s < C; ++s) {
-            const int j = base + s;
-            const int G = s == 0 ? carry : max(carry, Pf[s - 1]);
-            const int F = G - e_ins * j;
-            const int H = __vimax3_s32(Mv[s], Es[s], F);
-            const bool lt = j < end;
-            if (lt) kmax = max(kmax, H * 1024 + j);     // ties keep the later column (ksw.c:437)
-            const int nE = lt ? En[s] : (j == end ? 0 : Es[s]);
-            Es[s] = nE;
-            if (s > 0) {
-                const int nH = j <= end ? prevH : Hs[s];
-                Hs[s] = nH;
-                if (j <= end && (nH | nE) != 0) nzb |= 1u << s;
-            }
-            prevH = H;
-        }
-        {
-            int Hleft = __shfl_up_sync(BSB_FULL_MASK, prevH, 1);
-            if (lane == 0) Hleft = h1_init;
-            const int nH = base <= end ? Hleft : Hs[0];
-            Hs[0] = nH;
-            if (base <= end && (nH | Es[0]) != 0) nzb |= 1u;
-        }
-
-        ncell += end - beg;
-        const int kw = __reduce_max_sync(BSB_FULL_MASK, kmax);
-        const int m = kw >> 10, mj = kw & 1023;
-
-        if (end == qlen) {          // reached the query end: eh[qlen].h == H(i,qlen-1) (ksw.c:450-453)
-            int hsel = 0;
-#pragma unroll
-            for (int s = 0; s < C; ++s) hsel = s == q_slot ? Hs[s] : hsel;
-            const int h1 = __shfl_sync(BSB_FULL_MASK, hsel, q_lane);
-            max_ie = gscore > h1 ? max_ie : i;
-            gscore = gscore > h1 ? gscore : h1;
-        }
-        if (m == 0) break;                             // ksw.c:454
-        if (m > best) {
-            best = m, best_i = i, best_j = mj;
-            const int d = mj > i ? mj - i : i - mj;
-            max_off = max_off > d ? max_off : d;
-        } else if (P.zdrop > 0) {                      // ksw.c:458-464
-            const int di = i - best_i, dj = mj - best_j;
-            if (di > dj) {
-                if (best - m - (di - dj) * e_del > P.zdrop) break;
-            } else {
-                if (best - m - (dj - di) * e_ins > P.zdrop) break;
-            }
-        }
-        // shrink to the non-zero cells (ksw.c:466-469); columns left of beg are zero
-        const int lfirst = nzb ? base + __ffs(nzb) - 1 : INT_MAX;
-        const int llast = nzb ? base + 31 - __clz(nzb) : -1;
-        const int fnz = __reduce_min_sync(BSB_FULL_MASK, lfirst);
-        const int lnz = __reduce_max_sync(BSB_FULL_MASK, llast);
-        if (fnz < end) {
-            beg = fnz;
-            end = lnz + 2 < qlen ? lnz + 2 : qlen;
-        } else {
-            const int jj = lnz == end ? end : end - 1;
-            beg = end;
-            end = jj + 2 < qlen ? jj + 2 : qlen;
-        }
-    }
-    if (lane == 0) {
-        bsb_ext_out_t r;
-        r.score = best; r.qle = best_j + 1; r.tle = best_i + 1;
-        r.gtle = max_ie + 1; r.gscore = gscore; r.max_off = max_off;
-        *o = r;
-        if (cell_out) *cell_out = ncell;
-    }
-}
+// Query and target bytes of a batched job, read from the shared sequence buffer.
+struct JobAcc {
+    const uint8_t *__restrict__ qp, *__restrict__ tp;
+    __device__ __forceinline__ int q(int j) const { return qp[j]; }
+    __device__ __forceinline__ int t(int i) const { return tp[i]; }
+};
 
 // Persistent per-bin kernel: warps pull job indices from counter[bin].
 template <int C>
@@ -288,7 +74,15 @@ ksw_bin_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8_
         if (idx >= hi) break;
         const int job = order[idx];
         const bsb_ext_job_t jb = jobs[job];
-        ksw_one<C>(P, jb, seq, lane, out + job, cells ? cells + job : nullptr);
+        const JobAcc acc{seq + jb.qoff, seq + jb.toff};
+        const KswResult r = ksw_warp<C>(P, jb.qlen, jb.tlen, jb.h0, jb.w, jb.end_bonus, acc, lane);
+        if (lane == 0) {
+            bsb_ext_out_t o;
+            o.score = r.score; o.qle = r.qle; o.tle = r.tle;
+            o.gtle = r.gtle; o.gscore = r.gscore; o.max_off = r.max_off;
+            out[job] = o;
+            if (cells) cells[job] = r.cells;
+        }
     }
 }
 

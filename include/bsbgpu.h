@@ -121,6 +121,10 @@ typedef struct {
     int32_t pad_;
     const uint8_t *pac;
     int64_t l_pac;
+    int32_t n_seqs;              /* contig table (bntseq_t anns, bntseq.h:41-65): */
+    int32_t pad2_;
+    const int64_t *ann_offset;   /*   offset of each converted contig in the pac  */
+    const int32_t *ann_len;      /*   and its length; needed by bsb_align_regs_batch */
 } bsb_index_view_t;
 
 /* Uploads an index the caller already holds (stands in for the host-side
@@ -170,6 +174,41 @@ int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_rea
 int bsb_sa_batch(bsb_ctx *ctx, const uint64_t *rows, int64_t n, uint64_t *pos);
 /* Device-buffer form; rows beyond seq_len give (uint64_t)-2. */
 int bsb_sa_batch_device(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos);
+
+/* ---- seeds -> chains -> regions: the pre-dedup part of mem_align1_core ---- */
+
+/* The mem_opt_t fields the path reads (bwamem.h:26-62; BWA defaults in
+ * mem_opt_init, bwamem.c:50-88). */
+typedef struct {
+    int32_t a, b, o_del, e_del, o_ins, e_ins, w, zdrop, pen_clip5, pen_clip3;
+    int32_t min_seed_len, max_occ, max_chain_gap, min_chain_weight, max_chain_extend;
+    float   mask_level, drop_ratio, split_factor;
+    int32_t split_width, max_mem_intv;
+    int8_t  mat[25];
+    int8_t  pad_[3];
+} bsb_align_opt_t;
+
+/* The fields of mem_alnreg_t (bwamem.h:64-82) that mem_chain2aln sets; every
+ * other field of the reference's struct is zero at that point. */
+typedef struct {
+    int64_t rb, re;
+    int32_t qb, qe, rid, score, truesc, w, seedcov, seedlen0;
+    float   frac_rep;
+    int32_t pad_;
+} bsb_reg_t;
+
+/* Replaces, for a batch of reads, the part of mem_align1_core
+ * (bwamem.c:1157-1180) before mem_sort_dedup_patch: mem_collect_intv,
+ * mem_chain (bwt_sa per sampled row, the chain tree), mem_chain_flt and
+ * mem_chain2aln with its ksw_extend2 calls.  Reads are nt4 codes (already
+ * converted, as mem_align1_core sees them); read r's regions, in the
+ * reference's order, are regs[regs_off[r] .. regs_off[r+1]).  Needs an index
+ * with pac and contig table.  Supports reads up to 512 bp whose length keeps
+ * mem_flt_chained_seeds a no-op (bwamem.c:606), indexes without ALT contigs
+ * (BSBolt writes none).  Host buffers; synchronous. */
+int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
+                         const uint8_t *seqs, const int64_t *offs,
+                         bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
 
 /* ---- extension without any device allocation ---------------------------- */
 

@@ -1,0 +1,90 @@
+"""Seeds -> chains -> chain filter -> mem_chain2aln on the GPU (bsb_align_regs_batch)
+against the reference's pre-dedup regions (tests/golden/reads*_L*.npz) and the
+oracle, through the C ABI.  Bit-exact, including frac_rep's float bits."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from bsbolt_gb300 import _lib, index, seed, synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
+import golden_data  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+REG_FIELDS = ["rb", "re", "qb", "qe", "rid", "score", "truesc", "w", "seedcov", "seedlen0"]
+
+
+def opt_from(o):
+    o = [int(x) for x in o]
+    return _lib.AlignOpt.bwa_defaults(a=o[0], b=o[1], o_del=o[2], e_del=o[3], o_ins=o[4], e_ins=o[5], w=o[6],
+                                      zdrop=o[7], pen_clip5=o[8], pen_clip3=o[9], min_seed_len=o[10],
+                                      max_occ=o[11], split_width=o[12], max_mem_intv=o[13], max_chain_gap=o[14])
+
+
+@pytest.fixture(scope="module")
+def indexes(tmp_path_factory):
+    out = {}
+    for tag, gen in (("plain", golden_data.golden_genome), ("rep", golden_data.golden_genome_rep)):
+        d = tmp_path_factory.mktemp("aidx" + tag)
+        synth.write_fasta(str(d / "ref.fa"), gen())
+        index.build_index(str(d / "ref.fa"), str(d / "ref"))
+        out[tag] = str(d / "ref")
+    return out
+
+
+@pytest.mark.parametrize("fn,tag", [("reads_L5.npz", "plain"), ("reads_L30.npz", "plain"),
+                                    ("reads_rep_L5.npz", "rep")])
+def test_regions_match_reference(gpu_ctx, indexes, fn, tag):
+    seed.load_index(gpu_ctx, indexes[tag])
+    g = np.load(os.path.join(GOLDEN, fn))
+    regs, off = seed.align_regs(gpu_ctx, g["reads"], g["read_off"], opt_from(g["opts"]))
+    assert np.array_equal(off, g["reg_off"]), "region counts per read differ"
+    gr = g["regs"]
+    for i, f in enumerate(REG_FIELDS):
+        bad = np.nonzero(regs[f] != gr[:, i])[0]
+        assert len(bad) == 0, f"{fn}: reg.{f} differs at {bad[:5]}"
+    assert np.array_equal(regs["frac_rep"].view(np.int32), gr[:, 10].astype(np.int32))
+
+
+def test_regions_random_reads_vs_oracle(gpu_ctx, indexes):
+    """Reads of every length 0..300 with errors and N runs, both strands, repeats."""
+    prefix = indexes["rep"]
+    seed.load_index(gpu_ctx, prefix)
+    bi = index.BwaIndex(prefix)
+    pac = bi.pac_codes()
+    rng = np.random.Generator(np.random.PCG64(17))
+    reads = []
+    for k in range(2500):
+        L = int(rng.integers(0, 301))
+        st = int(rng.integers(0, len(pac) - L - 1))
+        r = pac[st:st + L].copy()
+        if k % 2:
+            r = (3 - r[::-1]).astype(np.uint8)
+        e = rng.random(L) < 0.03
+        r[e] = rng.integers(0, 5, int(e.sum()))
+        reads.append(r.astype(np.uint8))
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    seqs = np.concatenate(reads)
+    opt = _lib.AlignOpt.bwa_defaults()
+    regs, off = seed.align_regs(gpu_ctx, seqs, offs, opt)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac,
+                            oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000]),
+                            seqs, offs, n_threads=8)
+    assert np.array_equal(off, ref["regs_off"])
+    for f in REG_FIELDS + ["frac_rep"]:
+        assert np.array_equal(regs[f], ref["regs"][f]), f"reg.{f}"
+
+
+def test_align_rejects_long_reads(gpu_ctx, indexes):
+    seed.load_index(gpu_ctx, indexes["plain"])
+    with pytest.raises(_lib.BsbError) as e:
+        seed.align_regs(gpu_ctx, np.zeros(600, np.uint8), np.array([0, 600]))
+    assert e.value.code == _lib.BSB_ETOOLONG
