@@ -132,6 +132,156 @@ def cpu_port_gcups(jobs, seq, n_sample, threads, mat):
     return float(cells.sum()) / dt / 1e9, dt, out, cells
 
 
+def cfg0_workload(n_pairs=20000):
+    """configs[0] shapes: 4 x 500 kb reference (GC 41 %, CpG 1 %), directional PE 2x100,
+    insert N(300,30), CpG meth 0.8, CH 0.01, 99.5 % conversion, 0.5 % errors; the reads
+    converted in silico as bsbolt does (read 1 C->T, read 2 G->A).  Cached on disk."""
+    from bsbolt_gb300 import index, synth
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"cfg0_{n_pairs}")
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "ref")
+    if not os.path.exists(prefix + ".sa"):
+        contigs = synth.bs_genome(4, 500_000, gc=0.41, cpg_frac=0.01, seed=20261203)
+        synth.write_fasta(prefix + ".fa", contigs)
+        index.build_index(prefix + ".fa", prefix)
+        r1, r2 = synth.bs_reads_pe(contigs, n_pairs, 100, 300, 30, seed=20261203)
+        reads = []
+        for a, b in zip(r1, r2):
+            reads.append(synth.bs_convert(a, g2a=False))
+            reads.append(synth.bs_convert(b, g2a=True))
+        offs = np.zeros(len(reads) + 1, np.int64)
+        offs[1:] = np.cumsum([len(r) for r in reads])
+        np.save(os.path.join(d, "reads.npy"), np.concatenate(reads))
+        np.save(os.path.join(d, "offs.npy"), offs)
+    return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
+
+
+def pipeline_secondary(ctx, steps, rank):
+    """Seeds -> chains -> regions for configs[0]-shaped reads, GPU vs the CPU oracle."""
+    import oracle
+    from bsbolt_gb300 import _lib, index, seed
+    prefix, reads, offs = cfg0_workload()
+    n_pairs = (len(offs) - 1) // 2
+    seed.load_index(ctx, prefix)
+    opt = _lib.AlignOpt.bwa_defaults()
+    regs, roff = seed.align_regs(ctx, reads, offs, opt)          # warm-up
+    t0 = time.perf_counter()
+    k = max(3, min(steps, 10))
+    for _ in range(k):
+        regs, roff = seed.align_regs(ctx, reads, offs, opt)
+    gpu_s = (time.perf_counter() - t0) / k
+    seed.seed_batch(ctx, reads, offs)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        sd, soff = seed.seed_batch(ctx, reads, offs)
+    seed_s = (time.perf_counter() - t0) / k
+    bi = index.BwaIndex(prefix)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac,
+                            oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000]),
+                            reads, offs, n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    exact = bool(np.array_equal(roff, ref["regs_off"]) and
+                 all(np.array_equal(regs[f], ref["regs"][f]) for f in ("rb", "re", "qb", "qe", "score", "truesc")))
+    return {
+        "workload": "configs[0] shapes: 2 Mb bisulfite reference (4x500 kb), 20k directional PE 2x100 pairs, "
+                    "BWA defaults, -L 5",
+        "stage": "seeds -> SA -> chains -> chain filter -> mem_chain2aln (pre-dedup regions, bsb_align_regs_batch, "
+                 "host buffers incl. H2D/D2H)",
+        "gpu_read_pairs_per_s": round(n_pairs / gpu_s, 1),
+        "gpu_ms_per_batch": round(gpu_s * 1e3, 3),
+        "gpu_seeding_reads_per_s": round(2 * n_pairs / seed_s, 1),
+        "seeds_per_batch": int(soff[-1]),
+        "cpu_oracle_read_pairs_per_s": round(n_pairs / cpu_s, 1),
+        "cpu_oracle_threads": threads,
+        "regions_bit_exact_vs_oracle": exact,
+        "regions": int(roff[-1]),
+        "ext_cells": int(ref["cells"]),
+    }
+
+
+def learned_schedule(ctx, L, param, d_jobs, n, d_seq, seq_bytes, d_out, cells_eval, jobs_eval, steps):
+    """Plain-bound vs learned cost keys for the same jobs: model quality and makespan."""
+    import torch
+    from bsbolt_gb300 import _lib, cost_model as cm, extend, synth
+    import ctypes
+    t0 = time.perf_counter()
+    tr_jobs, tr_seq = cached_jobs(1_000_000, 20261203 + 77)
+    mat = synth.fill_scmat(1, 4)
+    _, tr_cells = extend.ksw_extend2_batch(ctx, tr_jobs, tr_seq, mat, 6, 1, 6, 1, 100, want_cells=True)
+    model = cm.CostModel(ctx, seed=11)
+    dj = torch.from_numpy(tr_jobs.view(np.uint8).reshape(-1).copy()).cuda()
+    ds = torch.from_numpy(tr_seq).cuda()
+    feat = model.features(dj, len(tr_jobs), ds, len(tr_seq))
+    losses = model.train(feat, torch.from_numpy(np.log1p(tr_cells).astype(np.float32)).cuda(), epochs=6)
+    train_s = time.perf_counter() - t0
+    del dj, ds, feat
+    # inference on the benchmark jobs (timed on the device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    feat = model.features(d_jobs, n, d_seq, seq_bytes)
+    pred, key = model.forward(feat, want_key=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    infer_ms = ev0.elapsed_time(ev1)
+    pred_np = pred.cpu().numpy()
+    bound = synth.cells_upper_bound(jobs_eval).astype(np.float64)
+
+    jsz = synth.JOB_DTYPE.itemsize           # bsb_ext_job_t is 40 bytes
+
+    def run(keyp, lo=0, hi=n):
+        jb = ctypes.c_void_p(d_jobs.data_ptr() + lo * jsz)
+        rc = L.bsb_extend_batch_device(ctx.handle, ctypes.byref(param), jb, hi - lo, ctypes.c_void_p(d_seq.data_ptr()),
+                                       seq_bytes, ctypes.c_void_p(keyp + lo * 4) if keyp else None,
+                                       ctypes.c_void_p(d_out.data_ptr() + lo * 24), None)
+        _lib.check(ctx.handle, rc)
+
+    def timed(keyp, chunk):
+        s = torch.cuda.ExternalStream(ctx.stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(2):
+            for lo in range(0, n, chunk):
+                run(keyp, lo, min(n, lo + chunk))
+        L.bsb_sync(ctx.handle)
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(steps):
+            for lo in range(0, n, chunk):
+                run(keyp, lo, min(n, lo + chunk))
+        b.record(s)
+        torch.cuda.synchronize()
+        _lib.check(ctx.handle, L.bsb_sync(ctx.handle))     # no job may have been skipped
+        return a.elapsed_time(b) / steps
+
+    kp = key.data_ptr()
+    total_cells = float(cells_eval.sum())
+    ref_out = d_out.cpu().numpy().copy()
+    out = {}
+    for label, chunk in (("whole_batch", n), ("batches_of_65536", 65536)):
+        t_plain = timed(0, chunk)
+        t_learn = timed(kp, chunk)
+        same = bool(np.array_equal(d_out.cpu().numpy(), ref_out))
+        out[label] = {"plain_ms": round(t_plain, 3), "learned_ms": round(t_learn, 3), "tuples_identical": same,
+                      "plain_gcups": round(total_cells / t_plain / 1e6, 2),
+                      "learned_gcups": round(total_cells / t_learn / 1e6, 2),
+                      "speedup_learned_vs_plain": round(t_plain / t_learn, 4)}
+    out.update({
+        "model": "2x64 MLP, BF16 weights, FP32 accumulation, Adam, hand-written kernels (csrc/cost_mlp.cu)",
+        "trained_on": "1M jobs of another seed, target log1p(cells logged by the extension kernel)",
+        "train_s": round(train_s, 2), "train_loss_per_epoch": [round(x, 4) for x in losses],
+        "inference_ms_4M_jobs": round(infer_ms, 3),
+        "spearman_model": round(cm.spearman(pred_np, cells_eval), 4),
+        "spearman_plain_bound": round(cm.spearman(bound, cells_eval), 4),
+        "mape_model": round(cm.mape(np.expm1(pred_np), cells_eval), 4),
+        "mape_plain_bound_calibrated": round(cm.mape(cm.calibrated_bound(bound, cells_eval), cells_eval), 4),
+    })
+    return out
+
+
 def run_reference(args, ws, rank):
     from bsbolt_gb300 import synth
     if rank != 0:
@@ -280,6 +430,21 @@ def run_ours(args, ws, rank, local):
                          "CPU port of ksw.c:380-479, pthreads over all host cores",
                "tuples_bit_exact_on_sample": parity, "cells_match_on_sample": bool(cells_match)}
 
+    learned = None
+    if rank == 0 and not args.no_learned:
+        try:
+            learned = learned_schedule(ctx, L, param, d_jobs, n, d_seq, len(seq), d_out,
+                                       d_cells.cpu().numpy(), jobs, max(3, min(args.steps, 5)))
+        except Exception as e:   # reported, never hidden
+            learned = {"error": f"{type(e).__name__}: {e}"}
+
+    secondary = None
+    if rank == 0 and not args.no_pipeline:
+        try:
+            secondary = pipeline_secondary(ctx, args.steps, rank)
+        except Exception as e:   # reported, never hidden
+            secondary = {"error": f"{type(e).__name__}: {e}"}
+
     traffic = None
     prof = os.path.join(ROOT, "profiles", "ksw_extend_traffic.json")
     if os.path.exists(prof):
@@ -310,6 +475,8 @@ def run_ours(args, ws, rank, local):
                     "tuples_match_device_run": e2e_match, "s_per_step": round(e2e_s, 4)},
             "gpu_launches": KERNELS_PER_STEP * args.steps,
             "clocks": clocks,
+            "pipeline": secondary,
+            "learned_schedule": learned,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -326,6 +493,8 @@ def main():
     ap.add_argument("--jobs", type=int, default=4_000_000)
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--ref-sample", type=int, default=200_000)
+    ap.add_argument("--no-pipeline", action="store_true", help="skip the seeds->regions secondary block")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

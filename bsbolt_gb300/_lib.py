@@ -30,6 +30,7 @@ EXPORTS = (
     "bsb_probe_int_peak",
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
+    "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
 )
 
 
@@ -134,6 +135,14 @@ def load(path: str = LIB_PATH):
     L.bsb_extend_batch_noalloc.restype = I32
     L.bsb_align_regs_batch.argtypes = [P, P, ctypes.c_int32, P, P, P, I64, P]
     L.bsb_align_regs_batch.restype = I32
+    L.bsb_cost_features.argtypes = [P, P, I64, P, I64, P]
+    L.bsb_cost_features.restype = I32
+    L.bsb_mlp_forward.argtypes = [P, P, P, I64, P, P]
+    L.bsb_mlp_forward.restype = I32
+    L.bsb_mlp_backward.argtypes = [P, P, P, P, ctypes.c_int32, P]
+    L.bsb_mlp_backward.restype = I32
+    L.bsb_mlp_adam.argtypes = [P, P, P, P, P, P, ctypes.c_float, ctypes.c_int32]
+    L.bsb_mlp_adam.restype = I32
     L.bsb_last_kernel_ms.argtypes = [P]
     L.bsb_last_kernel_ms.restype = ctypes.c_float
     _lib = L

@@ -103,6 +103,7 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->seed_scratch) cudaFree(ctx->seed_scratch);
     if (ctx->arena0) cudaFree(ctx->arena0);
     if (ctx->arena1) cudaFree(ctx->arena1);
+    if (ctx->arena2) cudaFree(ctx->arena2);
     bsb_index_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

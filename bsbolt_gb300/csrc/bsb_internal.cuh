@@ -48,8 +48,8 @@ struct bsb_ctx {
     size_t seed_scratch_bytes = 0;
     int *seed_ctrl = nullptr;
     // chaining / chain-extension scratch
-    void *arena0 = nullptr, *arena1 = nullptr;
-    size_t arena0_bytes = 0, arena1_bytes = 0;
+    void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
+    size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;
 };
 
 // SA lookups of device rows with the context's index (bwt_sa, bwt.c:86-96).

@@ -210,6 +210,39 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_rea
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
 
+/* ---- learned cost model for the extension scheduler ---------------------- */
+
+/* No reference counterpart: BWA runs extensions in call order on CPU threads.
+ * A 2 x 64 MLP (BF16 weights, FP32 accumulation) predicts log(1 + cells) of
+ * an extension job; its prediction, as a cost key, only orders the issue of
+ * jobs (bsb_extend_batch_device's d_cost) and never changes a result.  All
+ * buffers are device memory; calls are asynchronous on the context stream. */
+#define BSB_MLP_FEATURES 8
+#define BSB_MLP_HIDDEN 64
+#define BSB_MLP_PARAMS (64 * 8 + 64 * 64 + 64 + 64 + 64 + 1)
+typedef struct {
+    uint16_t w1[64 * 8];         /* BF16 bit patterns, row-major [out][in] */
+    uint16_t w2[64 * 64];
+    uint16_t w3[64];
+    float b1[64], b2[64], b3;
+} bsb_mlp_weights_t;
+
+/* Eight features per job (see cost_mlp.cu): n x 8 floats. */
+int bsb_cost_features(bsb_ctx *ctx, const bsb_ext_job_t *d_jobs, int64_t n, const uint8_t *d_seq,
+                      int64_t seq_bytes, float *d_feat);
+/* Predictions (log1p cells) and/or int32 cost keys (predicted cells); either may be NULL. */
+int bsb_mlp_forward(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w, const float *d_feat, int64_t n,
+                    float *d_pred, int32_t *d_key);
+/* Gradient of mean((y - target)^2) over n samples into d_grad[BSB_MLP_PARAMS]
+ * (layout w1|w2|w3|b1|b2|b3), with the loss in d_grad[BSB_MLP_PARAMS].
+ * Deterministic: each parameter's gradient is summed in sample order. */
+int bsb_mlp_backward(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w, const float *d_feat,
+                     const float *d_target, int32_t n, float *d_grad);
+/* One Adam step (beta 0.9 / 0.999) on FP32 master weights (BSB_MLP_PARAMS
+ * floats, same layout) and moments; refreshes the BF16 weights. */
+int bsb_mlp_adam(bsb_ctx *ctx, bsb_mlp_weights_t *d_w, float *d_master, float *d_m, float *d_v,
+                 const float *d_grad, float lr, int32_t step);
+
 /* ---- extension without any device allocation ---------------------------- */
 
 /* No counterpart in the reference: BWA allocates freely on the host and has

@@ -10,7 +10,7 @@
  * Modes
  *   golden_dump ksw <in.bin> <out.bin>
  *       in:  int64 n, int64 seq_bytes, int8 mat[25], pad[7], int32 o_del,
- *            e_del, o_ins, e_ins, zdrop, pad, then n 32-byte jobs
+ *            e_del, o_ins, e_ins, zdrop, pad, then n 40-byte jobs
  *            (bsb_ext_job_t), then the sequence bytes.
  *       out: n x 6 int32 from the reference ksw_extend2 (ksw.c:380-479).
  *   golden_dump reads <index prefix> <reads.bin> <out prefix> <opt.bin>
