@@ -1,0 +1,105 @@
+/*
+ * glue_shim.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Lets the BWA glue (bsbolt_gb300/integration/bwamem_gpu.c) be tested on a
+ * machine without a GPU: bsb_align_regs_batch is answered by the CPU oracle
+ * (whose regions equal the GPU's, by the GPU tests), and the worker1 call of
+ * the reference's mem_process_seqs is redirected to mem_align_batch_gpu by a
+ * link-time wrap of kt_for (-Wl,--wrap=kt_for), so the reference sources stay
+ * untouched.  The resulting `bwa_glue mem` must write the same SAM as the
+ * reference `bwa mem`.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "bwamem.h"
+#include "bwamem_gpu.h"
+#include "bsb_oracle.h"
+#include "bsb_oracle_chain.h"
+
+struct bsb_ctx {
+    orc_bwt_t bwt;
+    orc_bns_t bns;
+    orc_ann_t *anns;
+    int ready;
+};
+static struct bsb_ctx g_ctx;
+
+const char *bsb_last_error(const bsb_ctx *ctx) { (void)ctx; return "oracle shim failure"; }
+
+int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                         const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    orc_opt_t oo;
+    orc_align_out_t out;
+    int rc, r;
+    memset(&oo, 0, sizeof oo);
+    oo.a = o->a; oo.b = o->b; oo.o_del = o->o_del; oo.e_del = o->e_del; oo.o_ins = o->o_ins; oo.e_ins = o->e_ins;
+    oo.w = o->w; oo.zdrop = o->zdrop; oo.pen_clip5 = o->pen_clip5; oo.pen_clip3 = o->pen_clip3;
+    oo.min_seed_len = o->min_seed_len; oo.max_occ = o->max_occ; oo.max_chain_gap = o->max_chain_gap;
+    oo.min_chain_weight = o->min_chain_weight; oo.max_chain_extend = o->max_chain_extend;
+    oo.mask_level = o->mask_level; oo.drop_ratio = o->drop_ratio; oo.split_factor = o->split_factor;
+    oo.split_width = o->split_width; oo.max_mem_intv = o->max_mem_intv;
+    memcpy(oo.mat, o->mat, 25);
+    rc = orc_align_regs_batch(&ctx->bwt, &ctx->bns, &oo, n_reads, seqs, offs, &out, 4);
+    if (rc == 0 && out.regs_off[n_reads] > max_regs) rc = BSB_EINVAL;
+    if (rc == 0) {
+        for (r = 0; r <= n_reads; ++r) regs_off[r] = out.regs_off[r];
+        for (r = 0; r < out.regs_off[n_reads]; ++r) {
+            const orc_reg_t *s = &out.regs[r];
+            bsb_reg_t *d = &regs[r];
+            memset(d, 0, sizeof(*d));
+            d->rb = s->rb; d->re = s->re; d->qb = s->qb; d->qe = s->qe; d->rid = s->rid; d->score = s->score;
+            d->truesc = s->truesc; d->w = s->w; d->seedcov = s->seedcov; d->seedlen0 = s->seedlen0;
+            d->frac_rep = s->frac_rep;
+        }
+        /* self-check of the test: with BSB_SHIM_PERTURB set, shift the first
+         * region by one base so the SAM must change if this path is live */
+        if (getenv("BSB_SHIM_PERTURB") && out.regs_off[n_reads] > 0) regs[0].rb += 1, regs[0].re += 1;
+    }
+    orc_align_out_free(&out);
+    return rc ? BSB_EINVAL : 0;
+}
+
+/* worker_t of bwamem.c:1274-1285 */
+typedef struct {
+    const mem_opt_t *opt;
+    const bwt_t *bwt;
+    const bntseq_t *bns;
+    const uint8_t *pac;
+    const uint8_t *opac;
+    const mem_pestat_t *pes;
+    void **aux;
+    bseq1_t *seqs;
+    mem_alnreg_v *regs;
+    int64_t n_processed;
+} worker_view_t;
+
+void __real_kt_for(int n_threads, void (*func)(void *, long, int), void *data, long n);
+
+void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, long n)
+{
+    static long calls = 0;
+    if ((calls++ & 1) == 0) {          /* mem_process_seqs: worker1 first, then worker2 */
+        worker_view_t *w = (worker_view_t *)data;
+        int n_reads = (w->opt->flag & MEM_F_PE) ? (int)(n << 1) : (int)n, i;
+        if (!g_ctx.ready) {
+            orc_bwt_init(&g_ctx.bwt, w->bwt->primary, w->bwt->L2 + 1, w->bwt->bwt, w->bwt->bwt_size, w->bwt->sa,
+                         w->bwt->n_sa, w->bwt->sa_intv);
+            g_ctx.anns = (orc_ann_t *)calloc(w->bns->n_seqs, sizeof(orc_ann_t));
+            for (i = 0; i < w->bns->n_seqs; ++i) {
+                g_ctx.anns[i].offset = w->bns->anns[i].offset;
+                g_ctx.anns[i].len = w->bns->anns[i].len;
+                g_ctx.anns[i].is_alt = w->bns->anns[i].is_alt;
+            }
+            g_ctx.bns.l_pac = w->bns->l_pac;
+            g_ctx.bns.n_seqs = w->bns->n_seqs;
+            g_ctx.bns.anns = g_ctx.anns;
+            g_ctx.bns.pac = w->pac;
+            g_ctx.ready = 1;
+        }
+        if (mem_align_batch_gpu(&g_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs) != 0) abort();
+        return;
+    }
+    __real_kt_for(n_threads, func, data, n);
+}
