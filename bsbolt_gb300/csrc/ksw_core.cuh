@@ -22,6 +22,25 @@ __device__ __forceinline__ int prmt_sext(uint32_t x, uint32_t sel)
     return (int)r;
 }
 
+// Scores of target bases 0..3 against query base qc, one per byte:
+// mat[c*5 + qc] for c = 0..3.  The matrix is only indexed with constants
+// (selecting on qc), which keeps the kernel parameters out of local memory.
+__device__ __forceinline__ uint32_t profile_word(const KswParams &P, int qc)
+{
+    uint32_t w[5];
+#pragma unroll
+    for (int b = 0; b < 5; ++b)
+        w[b] = (uint32_t)(uint8_t)P.mat[b] | (uint32_t)(uint8_t)P.mat[5 + b] << 8 |
+               (uint32_t)(uint8_t)P.mat[10 + b] << 16 | (uint32_t)(uint8_t)P.mat[15 + b] << 24;
+    return qc == 0 ? w[0] : qc == 1 ? w[1] : qc == 2 ? w[2] : qc == 3 ? w[3] : w[4];
+}
+
+// mat[20 + qc]: the score of an N in the target against query base qc.
+__device__ __forceinline__ int profile_n(const KswParams &P, int qc)
+{
+    return qc == 0 ? P.mat[20] : qc == 1 ? P.mat[21] : qc == 2 ? P.mat[22] : qc == 3 ? P.mat[23] : P.mat[24];
+}
+
 __device__ __forceinline__ uint32_t sext_selector(int byte)
 {
     const uint32_t b = (uint32_t)byte, r = b | 8u;
@@ -60,9 +79,8 @@ __device__ __forceinline__ KswResult ksw_warp(const KswParams &P, int qlen, int 
     for (int s = 0; s < C; ++s) {
         const int j = base + s;
         const int qc = j < qlen ? acc.q(j) : 0;
-        prof[s] = (uint32_t)(uint8_t)P.mat[qc] | (uint32_t)(uint8_t)P.mat[5 + qc] << 8 |
-                  (uint32_t)(uint8_t)P.mat[10 + qc] << 16 | (uint32_t)(uint8_t)P.mat[15 + qc] << 24;
-        profN[s >> 2] |= (uint32_t)(uint8_t)P.mat[20 + qc] << ((s & 3) * 8);
+        prof[s] = profile_word(P, qc);
+        profN[s >> 2] |= (uint32_t)(uint8_t)profile_n(P, qc) << ((s & 3) * 8);
         // first row: h0, then an insertion run clipped at zero (ksw.c:395-397)
         Hs[s] = j == 0 ? h0 : (j <= qlen ? max(h1run - e_ins * (j - 1), 0) : 0);
         Es[s] = 0;

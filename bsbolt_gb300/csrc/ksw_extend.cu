@@ -28,62 +28,49 @@
 #include <climits>
 #include <cstdio>
 
-#include "ksw_core.cuh"
+#include "ksw_group.cuh"
 
 namespace {
 
-// Tile widths (query columns per lane).  C covers qlen <= 32*C - 1.
-constexpr int kTiles[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 24, 32};
+// Tiles: G lanes per job (32/G jobs per warp) x C query columns per lane;
+// a tile holds queries of up to G*C - 1 bases (columns 0..qlen).
+struct Tile { int G, C; };
+constexpr Tile kTiles[] = {
+    {4, 1}, {4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {4, 7}, {4, 8},      // qlen <= 31
+    {8, 5}, {8, 6}, {8, 7}, {8, 8},                                      // <= 63
+    {16, 5}, {16, 6}, {16, 7}, {16, 8},                                  // <= 127
+    {32, 5}, {32, 6}, {32, 7}, {32, 8},                                  // <= 255
+    {32, 10}, {32, 12}, {32, 16}, {32, 24}, {32, 32}};                   // <= 1023
 constexpr int kNumBins = sizeof(kTiles) / sizeof(kTiles[0]);
 constexpr int kClasses = 128;           // cost classes within a bin
 constexpr int kBlock = 128;             // threads per block (4 warps)
 
-// Bin of the smallest tile in kTiles that holds columns 0..qlen.
+// Bin of the smallest tile that holds columns 0..qlen.
 __host__ __device__ inline int tile_bin(int qlen)
 {
-    const int need = (qlen + 32) >> 5;
-    if (need <= 8) return need - 1;
-    if (need <= 10) return 8;
-    if (need <= 12) return 9;
-    if (need <= 16) return 10;
-    if (need <= 24) return 11;
-    if (need <= 32) return 12;
+    const int need = qlen + 1;
+    if (need <= 32) return (need + 3) / 4 - 1;
+    if (need <= 64) return 8 + (need + 7) / 8 - 5;
+    if (need <= 128) return 12 + (need + 15) / 16 - 5;
+    if (need <= 256) return 16 + (need + 31) / 32 - 5;
+    if (need <= 320) return 20;
+    if (need <= 384) return 21;
+    if (need <= 512) return 22;
+    if (need <= 768) return 23;
+    if (need <= 1024) return 24;
     return -1;
 }
 
-// Query and target bytes of a batched job, read from the shared sequence buffer.
-struct JobAcc {
-    const uint8_t *__restrict__ qp, *__restrict__ tp;
-    __device__ __forceinline__ int q(int j) const { return qp[j]; }
-    __device__ __forceinline__ int t(int i) const { return tp[i]; }
-};
-
-// Persistent per-bin kernel: warps pull job indices from counter[bin].
-template <int C>
+// Persistent per-bin kernel.  Each group of G lanes pulls job indices from
+// counter[bin] and runs its jobs row by row; the warp leaves when the queue is
+// empty and every group is done.
+template <int C, int G>
 __global__ void __launch_bounds__(kBlock)
-ksw_bin_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8_t *__restrict__ seq,
-               const int32_t *__restrict__ order, const int32_t *__restrict__ bin_start, int bin,
-               int *__restrict__ counter, bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
+ksw_group_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8_t *__restrict__ seq,
+                 const int32_t *__restrict__ order, const int32_t *__restrict__ bin_start, int bin,
+                 int *__restrict__ counter, bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
 {
-    const int lane = threadIdx.x & 31;
-    const int lo = bin_start[bin], hi = bin_start[bin + 1];
-    for (;;) {
-        int idx = 0;
-        if (lane == 0) idx = atomicAdd(counter + bin, 1);
-        idx = __shfl_sync(BSB_FULL_MASK, idx, 0) + lo;
-        if (idx >= hi) break;
-        const int job = order[idx];
-        const bsb_ext_job_t jb = jobs[job];
-        const JobAcc acc{seq + jb.qoff, seq + jb.toff};
-        const KswResult r = ksw_warp<C>(P, jb.qlen, jb.tlen, jb.h0, jb.w, jb.end_bonus, acc, lane);
-        if (lane == 0) {
-            bsb_ext_out_t o;
-            o.score = r.score; o.qle = r.qle; o.tle = r.tle;
-            o.gtle = r.gtle; o.gscore = r.gscore; o.max_off = r.max_off;
-            out[job] = o;
-            if (cells) cells[job] = r.cells;
-        }
-    }
+    ksw_group_run<C, G>(P, jobs, seq, order, bin_start[bin], bin_start[bin + 1], counter + bin, out, cells);
 }
 
 __device__ __forceinline__ int cost_class(uint32_t key)
@@ -170,18 +157,19 @@ __global__ void ksw_sched_scatter(const int32_t *__restrict__ key, int n, int *_
     }
 }
 
-template <int C>
+template <int C, int G>
 cudaError_t launch_bin(const KswParams &P, const bsb_ext_job_t *jobs, const uint8_t *seq,
                        const int32_t *order, const int32_t *bin_start, int bin, int *counter,
                        bsb_ext_out_t *out, int64_t *cells, int n_sm, cudaStream_t st)
 {
     static int blocks_per_sm = 0;
     if (!blocks_per_sm) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, ksw_bin_kernel<C>, kBlock, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, ksw_group_kernel<C, G>, kBlock, 0);
         if (e != cudaSuccess) return e;
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
-    ksw_bin_kernel<C><<<n_sm * blocks_per_sm, kBlock, 0, st>>>(P, jobs, seq, order, bin_start, bin, counter, out, cells);
+    ksw_group_kernel<C, G><<<n_sm * blocks_per_sm, kBlock, 0, st>>>(P, jobs, seq, order, bin_start, bin, counter, out,
+                                                                      cells);
     return cudaGetLastError();
 }
 
@@ -193,7 +181,8 @@ cudaError_t launch_all_bins(const KswParams &P, const bsb_ext_job_t *jobs, const
     if constexpr (I == kNumBins) {
         return cudaSuccess;
     } else {
-        cudaError_t e = launch_bin<kTiles[I]>(P, jobs, seq, order, bin_start, I, counter, out, cells, n_sm, st);
+        cudaError_t e = launch_bin<kTiles[I].C, kTiles[I].G>(P, jobs, seq, order, bin_start, I, counter, out, cells,
+                                                             n_sm, st);
         if (e != cudaSuccess) return e;
         return launch_all_bins<I + 1>(P, jobs, seq, order, bin_start, counter, out, cells, n_sm, st);
     }
@@ -211,7 +200,7 @@ static size_t fixed_bytes()
 
 size_t ksw_scratch_bytes(int64_t n) { return fixed_bytes() + sizeof(int32_t) * 2 * (size_t)n + 256; }
 
-int ksw_max_qlen() { return 32 * kTiles[kNumBins - 1] - 1; }
+int ksw_max_qlen() { return kTiles[kNumBins - 1].G * kTiles[kNumBins - 1].C - 1; }
 
 int *ksw_rejected_counter(void *scratch) { return (int *)scratch + kNumBins; }
 
