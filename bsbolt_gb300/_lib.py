@@ -22,6 +22,8 @@ BSB_ETOOLONG = -6
 BSB_ENOINDEX = -7
 BSB_ECAPACITY = -8
 BSB_NOALLOC_MAX_JOBS = 1 << 18
+BSB_NUM_TILES = 57
+BSB_TILE_MAP_LEN = 1025
 
 # every extern "C" symbol include/bsbgpu.h declares
 EXPORTS = (
@@ -31,6 +33,7 @@ EXPORTS = (
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
+    "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map",
 )
 
 
@@ -145,6 +148,12 @@ def load(path: str = LIB_PATH):
     L.bsb_mlp_adam.restype = I32
     L.bsb_last_kernel_ms.argtypes = [P]
     L.bsb_last_kernel_ms.restype = ctypes.c_float
+    L.bsb_tile_shapes.argtypes = [P, P, I32]
+    L.bsb_tile_shapes.restype = I32
+    L.bsb_set_tile_map.argtypes = [P, P, I32]
+    L.bsb_set_tile_map.restype = I32
+    L.bsb_get_tile_map.argtypes = [P, P, I32]
+    L.bsb_get_tile_map.restype = I32
     _lib = L
     return L
 

@@ -79,6 +79,8 @@ int bsb_ctx_create(int device, bsb_ctx **out)
     bsb_ctx *ctx = new (std::nothrow) bsb_ctx();
     if (!ctx) return BSB_ENOMEM;
     ctx->device = device;
+    memcpy(ctx->tile_map, ksw_default_tile_map(), BSB_TILE_MAP_LEN);
+    ctx->map_tiles = ksw_map_tiles(ctx->tile_map);
     int rc;
     if ((rc = bsb_cuda(ctx, cudaSetDevice(device), "cudaSetDevice")) ||
         (rc = bsb_cuda(ctx, cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device), "sm count")) ||
@@ -104,6 +106,7 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->arena0) cudaFree(ctx->arena0);
     if (ctx->arena1) cudaFree(ctx->arena1);
     if (ctx->arena2) cudaFree(ctx->arena2);
+    if (ctx->d_tile_map) cudaFree(ctx->d_tile_map);
     bsb_index_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -166,10 +169,11 @@ static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_
     return 0;
 }
 
-extern "C" int bsb_extend_batch_device(bsb_ctx *ctx, const bsb_ext_param_t *param,
-                                       const bsb_ext_job_t *d_jobs, int64_t n_jobs,
-                                       const uint8_t *d_seq, int64_t seq_bytes,
-                                       const int32_t *d_cost, bsb_ext_out_t *d_out, int64_t *d_cells)
+// Device-buffer extension with the tile shapes `tiles` launched (every shape
+// the context's map uses when the caller cannot tell which are needed).
+static int extend_device(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_ext_job_t *d_jobs,
+                         int64_t n_jobs, const uint8_t *d_seq, int64_t seq_bytes, const int32_t *d_cost,
+                         bsb_ext_out_t *d_out, int64_t *d_cells, uint64_t tiles)
 {
     if (!ctx) return BSB_EINVAL;
     KswParams P;
@@ -181,10 +185,77 @@ extern "C" int bsb_extend_batch_device(bsb_ctx *ctx, const bsb_ext_param_t *para
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     if ((rc = bsb_ensure(ctx, &ctx->scratch, &ctx->scratch_bytes, ksw_scratch_bytes(n_jobs), "extension scratch")))
         return rc;
-    cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, d_cost, d_out, d_cells, ctx->scratch,
-                               ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1);
+    cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, d_cost, ctx->d_tile_map, tiles, d_out, d_cells,
+                               ctx->scratch, ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1);
     ctx->pending_ksw = 1;
     return bsb_cuda(ctx, e, "extension launch");
+}
+
+extern "C" int bsb_extend_batch_device(bsb_ctx *ctx, const bsb_ext_param_t *param,
+                                       const bsb_ext_job_t *d_jobs, int64_t n_jobs,
+                                       const uint8_t *d_seq, int64_t seq_bytes,
+                                       const int32_t *d_cost, bsb_ext_out_t *d_out, int64_t *d_cells)
+{
+    if (!ctx) return BSB_EINVAL;
+    return extend_device(ctx, param, d_jobs, n_jobs, d_seq, seq_bytes, d_cost, d_out, d_cells, ctx->map_tiles);
+}
+
+extern "C" int bsb_tile_shapes(int32_t *G, int32_t *C, int max)
+{
+    for (int t = 0; t < BSB_NUM_TILES && t < max; ++t) {
+        int g = 0, c = 0;
+        ksw_tile_shape(t, &g, &c);
+        if (G) G[t] = g;
+        if (C) C[t] = c;
+    }
+    return BSB_NUM_TILES;
+}
+
+extern "C" int bsb_set_tile_map(bsb_ctx *ctx, const uint8_t *map, int n)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!map) {
+        memcpy(ctx->tile_map, ksw_default_tile_map(), BSB_TILE_MAP_LEN);
+        ctx->map_tiles = ksw_map_tiles(ctx->tile_map);
+        if (ctx->d_tile_map) {
+            cudaSetDevice(ctx->device);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->d_tile_map);
+            ctx->d_tile_map = nullptr;
+        }
+        return 0;
+    }
+    if (n != BSB_TILE_MAP_LEN)
+        return bsb_fail(ctx, BSB_EINVAL, "tile map must have %d entries (got %d)", BSB_TILE_MAP_LEN, n);
+    for (int need = 1; need < BSB_TILE_MAP_LEN; ++need) {
+        int g = 0, c = 0;
+        if (ksw_tile_shape(map[need], &g, &c))
+            return bsb_fail(ctx, BSB_EINVAL, "tile map entry %d names shape %d (of %d)", need, map[need], BSB_NUM_TILES);
+        if (g * c < need)
+            return bsb_fail(ctx, BSB_EINVAL, "tile map entry %d: shape %d (%d x %d) holds %d columns", need, map[need],
+                            g, c, g * c);
+    }
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    if (!ctx->d_tile_map &&
+        (rc = bsb_cuda(ctx, cudaMalloc((void **)&ctx->d_tile_map, BSB_TILE_MAP_LEN), "tile map")))
+        return rc;
+    // batches already queued read the old map: the copy is ordered after them
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->d_tile_map, map, BSB_TILE_MAP_LEN, cudaMemcpyHostToDevice,
+                                            ctx->stream), "tile map upload")) ||
+        (rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "tile map upload")))
+        return rc;
+    memcpy(ctx->tile_map, map, BSB_TILE_MAP_LEN);
+    ctx->tile_map[0] = 0;
+    ctx->map_tiles = ksw_map_tiles(ctx->tile_map);
+    return 0;
+}
+
+extern "C" int bsb_get_tile_map(bsb_ctx *ctx, uint8_t *map, int n)
+{
+    if (!map || n < BSB_TILE_MAP_LEN) return ctx ? bsb_fail(ctx, BSB_EINVAL, "tile map buffer too small") : BSB_EINVAL;
+    memcpy(map, ctx ? ctx->tile_map : ksw_default_tile_map(), BSB_TILE_MAP_LEN);
+    return 0;
 }
 
 extern "C" int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_ext_job_t *jobs,
@@ -217,7 +288,9 @@ extern "C" int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, cons
         return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_jobs, jobs, jb, cudaMemcpyHostToDevice, ctx->stream), "H2D jobs")))
         return rc;
-    if ((rc = bsb_extend_batch_device(ctx, param, d_jobs, n_jobs, d_seq, seq_bytes, nullptr, d_out, d_cells)))
+    uint64_t tiles = 0;         // only the shapes these query lengths map to
+    for (int64_t i = 0; i < n_jobs; ++i) tiles |= 1ull << ctx->tile_map[jobs[i].qlen + 1];
+    if ((rc = extend_device(ctx, param, d_jobs, n_jobs, d_seq, seq_bytes, nullptr, d_out, d_cells, tiles)))
         return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream), "D2H out")))
         return rc;

@@ -47,6 +47,10 @@ struct bsb_ctx {
     void *seed_scratch = nullptr;
     size_t seed_scratch_bytes = 0;
     int *seed_ctrl = nullptr;
+    // tile map of the batched extension (host copy; device copy only when it is not the default)
+    uint8_t tile_map[BSB_TILE_MAP_LEN] = {};
+    uint8_t *d_tile_map = nullptr;
+    uint64_t map_tiles = 0;
     // chaining / chain-extension scratch
     void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
     size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;
@@ -78,7 +82,16 @@ size_t ksw_scratch_bytes(int64_t n);
 int ksw_max_qlen();
 // Device word counting the jobs the last launch rejected (precondition failures).
 int *ksw_rejected_counter(void *scratch);
+// d_map: the tile map in device memory (BSB_TILE_MAP_LEN bytes), or NULL for
+// the built-in default; tiles: bit t set = launch tile shape t (the shapes the
+// batch's query lengths map to; a shape left out leaves its jobs unrun).
 cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
-                       const uint8_t *d_seq, const int32_t *d_cost, bsb_ext_out_t *d_out,
-                       int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
+                       const uint8_t *d_seq, const int32_t *d_cost, const uint8_t *d_map, uint64_t tiles,
+                       bsb_ext_out_t *d_out, int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
                        cudaEvent_t ev0, cudaEvent_t ev1);
+// The built-in tile map (host copy, BSB_TILE_MAP_LEN entries).
+const uint8_t *ksw_default_tile_map();
+// Shape of tile t; -1 if t is out of range.
+int ksw_tile_shape(int t, int *G, int *C);
+// Set of tile shapes a map uses (bit t).
+uint64_t ksw_map_tiles(const uint8_t *map);

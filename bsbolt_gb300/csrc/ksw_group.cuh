@@ -152,7 +152,10 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
         const int h1_init = beg == 0 ? max(h0 - (P.o_del + e_del * (i + 1)), 0) : 0;   // ksw.c:421-424
         const bool empty = beg >= end;         // empty band: the zero row max stops the job
 
-        // pass 1: M, next-row E, and F from a zero carry-in, F(j+1) = max(F(j) - e_ins, T(j))
+        // pass 1: M, next-row E, and F from a zero carry-in, F(j+1) = max(F(j) - e_ins, T(j)).
+        // M = H(i-1,j-1) + score, or 0 when H(i-1,j-1) == 0 (ksw.c:431); min(Hp + sc, Hp << 8)
+        // is that value whenever Hp > 0 and at most 0 when Hp == 0, which every use of M
+        // (a maximum with a non-negative E, F or 0) cannot tell apart from 0.
         int Mv[C], En[C], Pf[C];
         int local = 0;
         if (!__any_sync(act, tc >= 4)) {
@@ -161,7 +164,7 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
             for (int s = 0; s < C; ++s) {
                 const int sc = prmt_sext(prof[s], sel);
                 const int Hp = Hs[s];
-                const int M = Hp ? Hp + sc : 0;
+                const int M = __viaddmin_s32(Hp, sc, Hp << 8);
                 En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
                 Pf[s] = local;
                 local = __viaddmax_s32(local, -e_ins, __viaddmax_s32(M, -oe_ins, 0));
@@ -173,7 +176,7 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
             for (int s = 0; s < C; ++s) {
                 const int sc = tc < 4 ? prmt_sext(prof[s], sel) : prmt_sext(profN[s >> 2], sext_selector(s & 3));
                 const int Hp = Hs[s];
-                const int M = Hp ? Hp + sc : 0;
+                const int M = __viaddmin_s32(Hp, sc, Hp << 8);
                 En[s] = __viaddmax_s32(Es[s], -e_del, __viaddmax_s32(M, -oe_del, 0));
                 Pf[s] = local;
                 local = __viaddmax_s32(local, -e_ins, __viaddmax_s32(M, -oe_ins, 0));
@@ -189,32 +192,35 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
         const int carry = gl == 0 ? 0 : excl;
 
         // pass 2: H, the row-max key (H << 10 | j), and the new eh[] (H shifted one column)
+        // (columns are tested lane-relative, s against end - base)
+        const int rend = end - base;
         int kmax = -1, prevH = 0;
         uint32_t nzb = 0;
 #pragma unroll
         for (int s = 0; s < C; ++s) {
-            const int j = base + s;
             const int F = __viaddmax_s32(carry, -e_ins * s, Pf[s]);
             const int H = __vimax3_s32(Mv[s], Es[s], F);
-            const bool lt = j < end;
-            if (lt) kmax = max(kmax, H * 1024 + j);     // ties keep the later column (ksw.c:437)
-            const int nE = lt ? En[s] : (j == end ? 0 : Es[s]);
+            const bool lt = s < rend;
+            if (lt) kmax = max(kmax, H * 1024 + s);     // ties keep the later column (ksw.c:437)
+            const int nE = lt ? En[s] : (s == rend ? 0 : Es[s]);
             Es[s] = nE;
             if (s > 0) {
-                const int nH = j <= end ? prevH : Hs[s];
+                const int nH = s <= rend ? prevH : Hs[s];
                 Hs[s] = nH;
-                if (j <= end && (nH | nE) != 0) nzb |= 1u << s;
+                if (s <= rend && (nH | nE) != 0) nzb |= 1u << s;
             }
             prevH = H;
         }
         {
             int Hleft = __shfl_up_sync(act, prevH, 1, G);
             if (gl == 0) Hleft = h1_init;
-            const int nH = base <= end ? Hleft : Hs[0];
+            const int nH = rend >= 0 ? Hleft : Hs[0];
             Hs[0] = nH;
-            if (base <= end && (nH | Es[0]) != 0) nzb |= 1u;
+            if (rend >= 0 && (nH | Es[0]) != 0) nzb |= 1u;
         }
-        const int kw = group_max<G>(act, kmax);
+        // A lane without a band column offers base - 1 < 1024: it can only win a row
+        // whose maximum is 0, which ends the job before the column is used.
+        const int kw = group_max<G>(act, kmax + base);
         const int m = kw >> 10, mj = kw & 1023;
         if (!empty) ncell += end - beg;
 

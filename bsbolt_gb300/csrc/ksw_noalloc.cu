@@ -80,7 +80,8 @@ extern "C" int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_
     int n_sm = 0;
     int rc = setup_device(dev, &scratch, &n_sm);
     if (rc) return rc;
-    cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, nullptr, d_out, d_cells, scratch, n_sm,
-                               (cudaStream_t)stream, nullptr, nullptr);
+    static const uint64_t tiles = ksw_map_tiles(ksw_default_tile_map());
+    cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, nullptr, nullptr, tiles, d_out, d_cells, scratch,
+                               n_sm, (cudaStream_t)stream, nullptr, nullptr);
     return e == cudaSuccess ? 0 : BSB_ECUDA;
 }

@@ -1,0 +1,91 @@
+// ksw_tiles.cuh -- the tile shapes of the batched extension and the map that
+// assigns one to every query length.
+//
+// A tile is G lanes per job (32/G jobs per warp) x C query columns per lane;
+// it holds queries of up to G*C - 1 bases (columns 0..qlen).  Every shape in
+// kTileList is compiled (ksw_tiles_g*.cu); a tile map picks, for each
+// need = qlen + 1, the shape its jobs run on.  The default map below was
+// chosen by timing every candidate shape per query-length band on a GB300;
+// bsb_set_tile_map installs another one (e.g. the autotuner's) per context.
+// The shape never changes a result, only the time.
+#pragma once
+
+#include "bsb_internal.cuh"
+
+struct KswTile {
+    int G, C;
+};
+
+constexpr KswTile kTileList[] = {
+    {4, 1},   {4, 2},   {4, 3},   {4, 4},   {4, 5},   {4, 6},   {4, 7},   {4, 8},      //  0..7
+    {4, 9},   {4, 10},  {4, 11},  {4, 12},  {4, 13},  {4, 14},  {4, 15},  {4, 16},     //  8..15
+    {8, 6},   {8, 7},   {8, 8},   {8, 9},   {8, 10},  {8, 11},  {8, 12},  {8, 13},     // 16..23
+    {8, 14},  {8, 15},  {8, 16},  {8, 17},  {8, 18},                                    // 24..28
+    {16, 5},  {16, 6},  {16, 7},  {16, 8},  {16, 9},  {16, 10}, {16, 11}, {16, 12},    // 29..36
+    {16, 13}, {16, 14}, {16, 15}, {16, 16},                                             // 37..40
+    {32, 5},  {32, 6},  {32, 7},  {32, 8},  {32, 9},  {32, 10}, {32, 11}, {32, 12},    // 41..48
+    {32, 13}, {32, 14}, {32, 15}, {32, 16},                                             // 49..52
+    {32, 20}, {32, 24}, {32, 28}, {32, 32}};                                            // 53..56
+constexpr int kNumTiles = sizeof(kTileList) / sizeof(kTileList[0]);
+constexpr int kMaxNeed = BSB_TILE_MAP_LEN - 1;    // columns 0..qlen with qlen <= 1023
+constexpr int kKswBlock = 128;                      // threads per block (4 warps)
+
+static_assert(kNumTiles == BSB_NUM_TILES, "tile list and public header disagree");
+static_assert(kNumTiles <= 64, "tile sets are 64-bit masks");
+
+constexpr int tile_index(int G, int C)
+{
+    for (int t = 0; t < kNumTiles; ++t)
+        if (kTileList[t].G == G && kTileList[t].C == C) return t;
+    return -1;
+}
+
+struct KswTileMap {
+    uint8_t tile[kMaxNeed + 1];    // [0] unused
+};
+
+// 4 lanes up to 64 columns, 8 lanes up to 144, 16 up to 256, then 32; the
+// narrowest C that holds the query within each group size.
+constexpr KswTileMap make_default_tile_map()
+{
+    KswTileMap m{};
+    for (int need = 1; need <= kMaxNeed; ++need) {
+        int t = 0;
+        if (need <= 64) t = tile_index(4, (need + 3) / 4);
+        else if (need <= 144) t = tile_index(8, (need + 7) / 8 < 9 ? 9 : (need + 7) / 8);
+        else if (need <= 256) t = tile_index(16, (need + 15) / 16 < 10 ? 10 : (need + 15) / 16);
+        else if (need <= 512) t = tile_index(32, (need + 31) / 32 < 9 ? 9 : (need + 31) / 32);
+        else if (need <= 640) t = tile_index(32, 20);
+        else if (need <= 768) t = tile_index(32, 24);
+        else if (need <= 896) t = tile_index(32, 28);
+        else t = tile_index(32, 32);
+        m.tile[need] = (uint8_t)t;
+    }
+    return m;
+}
+
+constexpr KswTileMap kDefaultTileMap = make_default_tile_map();
+
+// Launches the persistent kernel of one tile shape over bin `bin` of the
+// scheduled order (jobs order[bin_start[bin] .. bin_start[bin+1]) ).
+typedef cudaError_t (*KswTileLaunch)(const KswParams &P, const bsb_ext_job_t *jobs, const uint8_t *seq,
+                                     const int32_t *order, const int32_t *bin_start, int bin, int *counter,
+                                     bsb_ext_out_t *out, int64_t *cells, int n_sm, cudaStream_t st);
+
+KswTileLaunch ksw_tiles_g4(int C);
+KswTileLaunch ksw_tiles_g8(int C);
+KswTileLaunch ksw_tiles_g16(int C);
+KswTileLaunch ksw_tiles_g32(int C);
+
+inline KswTileLaunch ksw_tile_launcher(int t)
+{
+    if (t < 0 || t >= kNumTiles) return nullptr;
+    const KswTile s = kTileList[t];
+    switch (s.G) {
+    case 4: return ksw_tiles_g4(s.C);
+    case 8: return ksw_tiles_g8(s.C);
+    case 16: return ksw_tiles_g16(s.C);
+    case 32: return ksw_tiles_g32(s.C);
+    default: return nullptr;
+    }
+}

@@ -104,6 +104,29 @@ int bsb_sync(bsb_ctx *ctx);
  * kernels), in milliseconds; valid after bsb_sync. */
 float bsb_last_kernel_ms(const bsb_ctx *ctx);
 
+/* ---- Extension tile shapes (no counterpart in the reference) -------------
+ * A batched extension job runs on a tile of G lanes x C query columns per
+ * lane (32/G jobs per warp); the tile map assigns a compiled shape to every
+ * query length.  The shape changes the time, never a result.  The library
+ * ships a default map measured on GB300; an autotuner (bsbolt_gb300.autotune)
+ * can measure the shapes on the caller's own jobs and install its map. */
+#define BSB_NUM_TILES 57
+#define BSB_TILE_MAP_LEN 1025    /* entry [qlen + 1] for qlen = 0..1023; [0] unused */
+
+/* Fills G[t], C[t] for the compiled shapes t < min(max, BSB_NUM_TILES);
+ * returns BSB_NUM_TILES. */
+int bsb_tile_shapes(int32_t *G, int32_t *C, int max);
+
+/* Installs map (BSB_TILE_MAP_LEN entries, shape index per qlen + 1) for this
+ * context's later extension batches; NULL restores the default map.  Every
+ * entry [need], need = 1..1024, must name a shape with G*C >= need
+ * (BSB_EINVAL otherwise, and the current map stays). */
+int bsb_set_tile_map(bsb_ctx *ctx, const uint8_t *map, int n);
+
+/* Copies the context's current tile map into map (n >= BSB_TILE_MAP_LEN);
+ * ctx = NULL gives the built-in default map (no device needed). */
+int bsb_get_tile_map(bsb_ctx *ctx, uint8_t *map, int n);
+
 /* ---- FM-index (device resident) ----------------------------------------- */
 
 /* The index arrays as bwa_idx_load leaves them in memory (bwa.c:363-524,

@@ -39,3 +39,23 @@ def test_error_strings_and_no_device_behaviour():
     # NULL out-pointer is rejected before any CUDA call
     assert lib.bsb_ctx_create(0, None) == _lib.BSB_EINVAL
     assert lib.bsb_last_error(None) == b"no context"
+
+
+def test_tile_shapes_and_default_map():
+    """The compiled tile shapes and the built-in map (host-only calls)."""
+    lib = _lib.load()
+    G = (ctypes.c_int32 * 64)()
+    C = (ctypes.c_int32 * 64)()
+    n = lib.bsb_tile_shapes(G, C, 64)
+    assert n == _lib.BSB_NUM_TILES
+    shapes = [(G[t], C[t]) for t in range(n)]
+    assert len(set(shapes)) == n
+    assert all(g in (4, 8, 16, 32) and c >= 1 for g, c in shapes)
+    m = (ctypes.c_uint8 * _lib.BSB_TILE_MAP_LEN)()
+    assert lib.bsb_get_tile_map(None, m, _lib.BSB_TILE_MAP_LEN) == 0
+    for need in range(1, _lib.BSB_TILE_MAP_LEN):
+        g, c = shapes[m[need]]
+        assert g * c >= need, (need, g, c)
+    # the widest query (1023 bases = 1024 columns) fits the widest shape
+    assert max(g * c for g, c in shapes) == _lib.BSB_TILE_MAP_LEN - 1
+    assert lib.bsb_get_tile_map(None, m, 10) == _lib.BSB_EINVAL
