@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 METRIC = "extension GCUPS (batched ksw_extend2, plain schedule)"
 UNIT = "GCUPS"
 INT_OPS_PER_CELL = 14          # add+select, 2 max, select+max, 2x(sub, max0, sub, max): ksw.c:431-447
-KERNELS_PER_STEP = 3 + 13      # schedule (hist, scan, scatter) + one persistent kernel per tile bin
+SCHED_KERNELS = 3              # schedule: hist, scan, scatter (then one persistent kernel per tile shape)
 
 
 def dist_env():
@@ -282,6 +282,44 @@ def learned_schedule(ctx, L, param, d_jobs, n, d_seq, seq_bytes, d_out, cells_ev
     return out
 
 
+def autotune_block(ctx, L, param, d_jobs, n, d_seq, seq_bytes, d_out, out_ref, steps):
+    """Tile-shape autotuner: tune on a held-out job set of the same distribution, then time
+    the headline batch with the tuned map against the default map (same device entry)."""
+    import ctypes
+    import torch
+    from bsbolt_gb300 import _lib, autotune
+    tj, ts = cached_jobs(1_000_000, 20261203 + 99)
+    t0 = time.perf_counter()
+    tmap, report = autotune.tune(ctx, tj, ts, param, min_jobs=4096, max_jobs=100_000, reps=2)
+    tune_s = time.perf_counter() - t0
+
+    def run(k):
+        ms = []
+        for _ in range(k + 1):
+            rc = L.bsb_extend_batch_device(ctx.handle, ctypes.byref(param), ctypes.c_void_p(d_jobs.data_ptr()), n,
+                                           ctypes.c_void_p(d_seq.data_ptr()), seq_bytes, None,
+                                           ctypes.c_void_p(d_out.data_ptr()), None)
+            _lib.check(ctx.handle, rc)
+            _lib.check(ctx.handle, L.bsb_sync(ctx.handle))
+            ms.append(ctx.last_kernel_ms())
+        return float(np.median(ms[1:]))
+
+    default_ms = run(steps)
+    try:
+        autotune.set_map(ctx, tmap)
+        tuned_ms = run(steps)
+        same = bool(np.array_equal(d_out.cpu().numpy(), out_ref))
+    finally:
+        autotune.set_map(ctx, None)
+    changed = [r for r in report if r["best"] != r["current"]]
+    return {"tuned_on": "1M held-out jobs of the same distribution (another seed), bands of need = qlen+1",
+            "tune_s": round(tune_s, 2), "bands_tuned": len(report), "bands_changed": len(changed),
+            "changes": [{"need": r["need"], "from": r["current"], "to": r["best"],
+                         "ms": [r["current_ms"], r["best_ms"]]} for r in changed],
+            "default_map_ms": round(default_ms, 3), "tuned_map_ms": round(tuned_ms, 3),
+            "speedup_tuned_vs_default": round(default_ms / tuned_ms, 4), "tuples_identical": same}
+
+
 def run_reference(args, ws, rank):
     from bsbolt_gb300 import synth
     if rank != 0:
@@ -340,6 +378,12 @@ def run_ours(args, ws, rank, local):
     d_cells = torch.zeros(n, dtype=torch.int64, device=f"cuda:{local}")
     torch.cuda.synchronize()
 
+    from bsbolt_gb300 import autotune
+    shape_list = autotune.shapes(L)
+    tmap = autotune.get_map(ctx)
+    mapped = sorted(set(int(t) for t in tmap[1:]))          # shapes the device entry launches
+    job_tile = tmap[jobs["qlen"].astype(np.int64) + 1]
+
     def step(with_cells=False):
         rc = L.bsb_extend_batch_device(ctx.handle, ctypes.byref(param), ctypes.c_void_p(d_jobs.data_ptr()), n,
                                        ctypes.c_void_p(d_seq.data_ptr()), len(seq), None,
@@ -366,6 +410,8 @@ def run_ours(args, ws, rank, local):
     s = torch.cuda.ExternalStream(ctx.stream)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     kms = []
+    tile_ms = np.zeros(_lib.BSB_NUM_TILES)
+    tbuf = (ctypes.c_float * _lib.BSB_NUM_TILES)()
     with ClockSampler(local) as clk:
         if dist:
             dist.barrier()
@@ -375,6 +421,8 @@ def run_ours(args, ws, rank, local):
             step()
             L.bsb_sync(ctx.handle)
             kms.append(ctx.last_kernel_ms())
+            L.bsb_last_tile_ms(ctx.handle, tbuf, _lib.BSB_NUM_TILES)
+            tile_ms += np.frombuffer(tbuf, dtype=np.float32)
         ev1.record(s)
         torch.cuda.synchronize()
         if dist:
@@ -393,7 +441,24 @@ def run_ours(args, ws, rank, local):
     ms_step = elapsed_ms / args.steps
     value = all_cells / (ms_step * 1e-3) / 1e9
     kernel_ms = float(np.mean(kms))
-    achieved = total_cells * INT_OPS_PER_CELL / (kernel_ms * 1e-3) / 1e12
+    achieved_all = total_cells * INT_OPS_PER_CELL / (kernel_ms * 1e-3) / 1e12
+    # the dominant kernel: the tile shape with the most device time per step (CUDA events
+    # on the context stream around each shape's launch), and the cells its jobs hold
+    tile_ms /= args.steps
+    cells_host = d_cells.cpu().numpy()
+    tile_cells = np.bincount(job_tile, weights=cells_host.astype(np.float64), minlength=_lib.BSB_NUM_TILES)
+    tile_jobs = np.bincount(job_tile, minlength=_lib.BSB_NUM_TILES)
+    dom = int(np.argmax(tile_ms))
+    dom_ms = float(tile_ms[dom])
+    achieved = tile_cells[dom] * INT_OPS_PER_CELL / (dom_ms * 1e-3) / 1e12
+    dom_name = "ksw_tile_kernel<%d,%d>" % (shape_list[dom][1], shape_list[dom][0])
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "ksw_tile_kernel_traffic.txt")
+    if os.path.exists(prof):       # DRAM bytes per job of this shape from an ncu capture
+        for ln in open(prof):
+            f = ln.split()
+            if len(f) >= 3 and f[0] == "%dx%d" % shape_list[dom] and f[1] == "dram_bytes_per_job":
+                traffic = int(float(f[2]) * tile_jobs[dom])
 
     # end to end through the C ABI with pinned host buffers
     hj = torch.from_numpy(jobs_u8).pin_memory()
@@ -438,20 +503,20 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             learned = {"error": f"{type(e).__name__}: {e}"}
 
+    tuned = None
+    if rank == 0 and not args.no_autotune:
+        try:
+            tuned = autotune_block(ctx, L, param, d_jobs, n, d_seq, len(seq), d_out, out_host,
+                                   max(3, min(args.steps, 5)))
+        except Exception as e:   # reported, never hidden
+            tuned = {"error": f"{type(e).__name__}: {e}"}
+
     secondary = None
     if rank == 0 and not args.no_pipeline:
         try:
             secondary = pipeline_secondary(ctx, args.steps, rank)
         except Exception as e:   # reported, never hidden
             secondary = {"error": f"{type(e).__name__}: {e}"}
-
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "ksw_extend_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_step")
-        except Exception:
-            traffic = None
 
     if rank == 0:
         line = {
@@ -463,20 +528,26 @@ def run_ours(args, ws, rank, local):
                                    "(1% sub, 0.1% indel, 20% unrelated), h0 U[19,100], w=100, a1 b4 o6 e1 z100 L5",
                        "jobs": n, "cells_per_step": total_cells, "seq_bytes": int(len(seq)),
                        "l2": "inputs 1.0 GB > 129 MB L2 per step (no flush needed)",
-                       "schedule": "plain (tile bin, longest bound first)", "parallelism": f"replicas x{ws}"},
+                       "schedule": "plain (default tile map, longest bound first)", "parallelism": f"replicas x{ws}"},
             "roofline": {"bound": "int", "achieved": round(achieved, 3), "peak": round(int_peak, 3),
                          "unit": "Tops/s", "frac": round(achieved / int_peak, 4), "traffic": traffic,
+                         "kernel": dom_name, "kernel_ms_per_launch": round(dom_ms, 4),
+                         "kernel_cells_per_launch": int(tile_cells[dom]),
+                         "kernel_share_of_step": round(dom_ms / kernel_ms, 4),
                          "peak_source": "measured add+max int32 throughput (bsb_probe_int_peak) on this GPU; "
                                         "MEASURED_PEAKS.json has no integer figure",
-                         "ops_per_cell": INT_OPS_PER_CELL, "kernel_ms_per_step": round(kernel_ms, 4)},
+                         "ops_per_cell": INT_OPS_PER_CELL,
+                         "all_kernels": {"achieved": round(achieved_all, 3), "frac": round(achieved_all / int_peak, 4),
+                                         "ms_per_step": round(kernel_ms, 4)}},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
                     "h2d_bytes_per_step": int(jobs_u8.nbytes + len(seq)), "d2h_bytes_per_step": int(n * 24),
                     "tuples_match_device_run": e2e_match, "s_per_step": round(e2e_s, 4)},
-            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "gpu_launches": (SCHED_KERNELS + len(mapped)) * args.steps,
             "clocks": clocks,
             "pipeline": secondary,
             "learned_schedule": learned,
+            "autotune": tuned,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -495,6 +566,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=200_000)
     ap.add_argument("--no-pipeline", action="store_true", help="skip the seeds->regions secondary block")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

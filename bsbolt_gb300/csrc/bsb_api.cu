@@ -90,6 +90,11 @@ int bsb_ctx_create(int device, bsb_ctx **out)
         bsb_ctx_destroy(ctx);
         return rc;
     }
+    for (int t = 0; t <= BSB_NUM_TILES; ++t)
+        if ((rc = bsb_cuda(ctx, cudaEventCreate(&ctx->tile_ev[t]), "event"))) {
+        bsb_ctx_destroy(ctx);
+        return rc;
+    }
     *out = ctx;
     return BSB_OK;
 }
@@ -108,6 +113,8 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->arena2) cudaFree(ctx->arena2);
     if (ctx->d_tile_map) cudaFree(ctx->d_tile_map);
     bsb_index_release(ctx);
+    for (int t = 0; t <= BSB_NUM_TILES; ++t)
+        if (ctx->tile_ev[t]) cudaEventDestroy(ctx->tile_ev[t]);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -186,8 +193,9 @@ static int extend_device(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_e
     if ((rc = bsb_ensure(ctx, &ctx->scratch, &ctx->scratch_bytes, ksw_scratch_bytes(n_jobs), "extension scratch")))
         return rc;
     cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, d_cost, ctx->d_tile_map, tiles, d_out, d_cells,
-                               ctx->scratch, ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1);
+                               ctx->scratch, ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1, ctx->tile_ev);
     ctx->pending_ksw = 1;
+    ctx->last_tiles = tiles;
     return bsb_cuda(ctx, e, "extension launch");
 }
 
@@ -251,6 +259,13 @@ extern "C" int bsb_set_tile_map(bsb_ctx *ctx, const uint8_t *map, int n)
     return 0;
 }
 
+extern "C" int bsb_last_tile_ms(const bsb_ctx *ctx, float *ms, int n)
+{
+    if (!ctx || !ms) return BSB_EINVAL;
+    for (int t = 0; t < BSB_NUM_TILES && t < n; ++t) ms[t] = ctx->tile_ms[t];
+    return 0;
+}
+
 extern "C" int bsb_get_tile_map(bsb_ctx *ctx, uint8_t *map, int n)
 {
     if (!map || n < BSB_TILE_MAP_LEN) return ctx ? bsb_fail(ctx, BSB_EINVAL, "tile map buffer too small") : BSB_EINVAL;
@@ -308,6 +323,13 @@ extern "C" int bsb_sync(bsb_ctx *ctx)
     if (ctx->pending_ksw) {
         ctx->pending_ksw = 0;
         cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1);
+        for (int t = 0; t < BSB_NUM_TILES; ++t) {       // each shape until the next launched one
+            ctx->tile_ms[t] = 0.f;
+            if (!(ctx->last_tiles >> t & 1)) continue;
+            int u = t + 1;
+            while (u < BSB_NUM_TILES && !(ctx->last_tiles >> u & 1)) ++u;
+            cudaEventElapsedTime(&ctx->tile_ms[t], ctx->tile_ev[t], ctx->tile_ev[u]);
+        }
         int rej = 0;
         if ((rc = bsb_cuda(ctx, cudaMemcpy(&rej, ksw_rejected_counter(ctx->scratch), sizeof(int),
                                            cudaMemcpyDeviceToHost), "rejected-job counter")))

@@ -51,6 +51,11 @@ struct bsb_ctx {
     uint8_t tile_map[BSB_TILE_MAP_LEN] = {};
     uint8_t *d_tile_map = nullptr;
     uint64_t map_tiles = 0;
+    // per-shape device time of the last extension batch: tile_ev[t] is recorded before
+    // shape t's kernel, tile_ev[BSB_NUM_TILES] after the last one
+    cudaEvent_t tile_ev[BSB_NUM_TILES + 1] = {};
+    uint64_t last_tiles = 0;
+    float tile_ms[BSB_NUM_TILES] = {};
     // chaining / chain-extension scratch
     void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
     size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;
@@ -85,10 +90,11 @@ int *ksw_rejected_counter(void *scratch);
 // d_map: the tile map in device memory (BSB_TILE_MAP_LEN bytes), or NULL for
 // the built-in default; tiles: bit t set = launch tile shape t (the shapes the
 // batch's query lengths map to; a shape left out leaves its jobs unrun).
+// tile_ev (optional, BSB_NUM_TILES + 1 events): per-shape timing marks as in bsb_ctx.
 cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
                        const uint8_t *d_seq, const int32_t *d_cost, const uint8_t *d_map, uint64_t tiles,
                        bsb_ext_out_t *d_out, int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
-                       cudaEvent_t ev0, cudaEvent_t ev1);
+                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev = nullptr);
 // The built-in tile map (host copy, BSB_TILE_MAP_LEN entries).
 const uint8_t *ksw_default_tile_map();
 // Shape of tile t; -1 if t is out of range.

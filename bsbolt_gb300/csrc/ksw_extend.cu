@@ -177,7 +177,7 @@ uint64_t ksw_map_tiles(const uint8_t *map)
 cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
                        const uint8_t *d_seq, const int32_t *d_cost, const uint8_t *d_map, uint64_t tiles,
                        bsb_ext_out_t *d_out, int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
-                       cudaEvent_t ev0, cudaEvent_t ev1)
+                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev)
 {
     char *p = (char *)scratch;
     int *counter = (int *)p;
@@ -202,9 +202,11 @@ cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t 
             if (!(tiles >> t & 1)) continue;
             KswTileLaunch f = ksw_tile_launcher(t);
             if (!f) return cudaErrorInvalidValue;
+            if (tile_ev) cudaEventRecord(tile_ev[t], st);
             e = f(P, d_jobs, d_seq, order, bin_start, t, counter, d_out, d_cells, n_sm, st);
             if (e != cudaSuccess) return e;
         }
+        if (tile_ev) cudaEventRecord(tile_ev[kNumTiles], st);
     }
     if (ev1) cudaEventRecord(ev1, st);
     return cudaSuccess;

@@ -123,6 +123,12 @@ int bsb_tile_shapes(int32_t *G, int32_t *C, int max);
  * (BSB_EINVAL otherwise, and the current map stays). */
 int bsb_set_tile_map(bsb_ctx *ctx, const uint8_t *map, int n);
 
+/* Device time of each shape's kernel in the context's most recent extension
+ * batch (CUDA events on the context stream between consecutive shape
+ * launches), ms[t] for t < min(n, BSB_NUM_TILES); 0 for shapes not launched.
+ * Valid after bsb_sync. */
+int bsb_last_tile_ms(const bsb_ctx *ctx, float *ms, int n);
+
 /* Copies the context's current tile map into map (n >= BSB_TILE_MAP_LEN);
  * ctx = NULL gives the built-in default map (no device needed). */
 int bsb_get_tile_map(bsb_ctx *ctx, uint8_t *map, int n);
