@@ -7,7 +7,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "bsb_internal.cuh"
 
@@ -90,10 +93,21 @@ int bsb_ctx_create(int device, bsb_ctx **out)
         bsb_ctx_destroy(ctx);
         return rc;
     }
-    for (int t = 0; t <= BSB_NUM_TILES; ++t)
-        if ((rc = bsb_cuda(ctx, cudaEventCreate(&ctx->tile_ev[t]), "event"))) {
+    bool ok = true;
+    for (int t = 0; t < 2 * BSB_NUM_TILES && ok; ++t) ok = cudaEventCreate(&ctx->tile_ev[t]) == cudaSuccess;
+    for (int t = 0; t < 4 * BSB_MAX_CHUNKS && ok; ++t)
+        ok = cudaEventCreateWithFlags(&ctx->chunk_ev[t], (t & 3) < 2 ? cudaEventDisableTiming : cudaEventDefault) ==
+             cudaSuccess;
+    for (int a = 0; a < BSB_AUX_STREAMS && ok; ++a)
+        ok = cudaStreamCreateWithFlags(&ctx->ms.aux[a], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->ms.join[a], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->ms.fork, cudaEventDisableTiming) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+        rc = bsb_cuda(ctx, cudaGetLastError(), "streams and events");
         bsb_ctx_destroy(ctx);
-        return rc;
+        return rc ? rc : BSB_ECUDA;
     }
     *out = ctx;
     return BSB_OK;
@@ -113,8 +127,19 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->arena2) cudaFree(ctx->arena2);
     if (ctx->d_tile_map) cudaFree(ctx->d_tile_map);
     bsb_index_release(ctx);
-    for (int t = 0; t <= BSB_NUM_TILES; ++t)
+    for (cudaStream_t s : {ctx->h2d, ctx->d2h, ctx->ms.aux[0], ctx->ms.aux[1], ctx->ms.aux[2]})
+        if (s) cudaStreamSynchronize(s);
+    for (int t = 0; t < 2 * BSB_NUM_TILES; ++t)
         if (ctx->tile_ev[t]) cudaEventDestroy(ctx->tile_ev[t]);
+    for (int t = 0; t < 4 * BSB_MAX_CHUNKS; ++t)
+        if (ctx->chunk_ev[t]) cudaEventDestroy(ctx->chunk_ev[t]);
+    for (int a = 0; a < BSB_AUX_STREAMS; ++a) {
+        if (ctx->ms.aux[a]) cudaStreamDestroy(ctx->ms.aux[a]);
+        if (ctx->ms.join[a]) cudaEventDestroy(ctx->ms.join[a]);
+    }
+    if (ctx->ms.fork) cudaEventDestroy(ctx->ms.fork);
+    if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
+    if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -131,6 +156,9 @@ void *bsb_ctx_stream(bsb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr;
 float bsb_last_kernel_ms(const bsb_ctx *ctx) { return ctx ? ctx->last_kernel_ms : 0.f; }
 
 }  // extern "C"
+
+// Host batches of at least this many jobs are extended in BSB_MAX_CHUNKS pieces.
+static const int64_t kChunkFrom = (int64_t)1 << 20;
 
 static int check_param(bsb_ctx *ctx, const bsb_ext_param_t *param, KswParams *P)
 {
@@ -156,11 +184,13 @@ static int check_param(bsb_ctx *ctx, const bsb_ext_param_t *param, KswParams *P)
 }
 
 // Host-side validation of a job table (the kernel trusts what passes here).
-static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_t seq_bytes)
+// The precondition message for the first failing job of jobs[0..n) (numbered from first).
+static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_t seq_bytes, int64_t first = 0)
 {
     const int qmax = ksw_max_qlen();
-    for (int64_t i = 0; i < n; ++i) {
-        const bsb_ext_job_t &j = jobs[i];
+    for (int64_t k = 0; k < n; ++k) {
+        const bsb_ext_job_t &j = jobs[k];
+        const int64_t i = first + k;
         if (j.qlen < 0 || j.tlen < 0 || j.w < 0 || j.flags != 0)
             return bsb_fail(ctx, BSB_EINVAL, "job %lld: negative length/band or nonzero flags", (long long)i);
         if (j.h0 <= 0 || j.h0 > (1 << 20))
@@ -176,11 +206,90 @@ static int check_jobs(bsb_ctx *ctx, const bsb_ext_job_t *jobs, int64_t n, int64_
     return 0;
 }
 
+// What the host entry needs from one stretch of jobs: the first job failing the
+// preconditions (n if none), the shapes its query lengths map to, and the end of the
+// sequence bytes it references.
+struct JobScan {
+    int64_t first_bad;
+    uint64_t tiles;
+    int64_t need;
+};
+
+static bool job_ok(const bsb_ext_job_t &j, int64_t seq_bytes, int qmax)
+{
+    return j.qlen >= 0 && j.tlen >= 0 && j.w >= 0 && j.flags == 0 && j.h0 > 0 && j.h0 <= (1 << 20) &&
+           j.qlen <= qmax && j.qoff >= 0 && j.toff >= 0 && j.qoff + j.qlen <= seq_bytes &&
+           j.toff + j.tlen <= seq_bytes && (int64_t)j.qlen + j.tlen <= (1 << 30);
+}
+
+static JobScan scan_jobs(const bsb_ext_job_t *jobs, int64_t lo, int64_t hi, int64_t seq_bytes,
+                         const uint8_t *tile_map)
+{
+    const int qmax = ksw_max_qlen();
+    JobScan r{hi, 0, 0};
+    for (int64_t i = lo; i < hi; ++i) {
+        const bsb_ext_job_t &j = jobs[i];
+        if (!job_ok(j, seq_bytes, qmax)) {
+            r.first_bad = i;
+            break;
+        }
+        r.tiles |= 1ull << tile_map[j.qlen + 1];
+        r.need = r.need > j.qoff + j.qlen ? r.need : j.qoff + j.qlen;
+        r.need = r.need > j.toff + j.tlen ? r.need : j.toff + j.tlen;
+    }
+    return r;
+}
+
+// scan_jobs over pieces [k*per, (k+1)*per), host threads sharing the work for large
+// batches (the scan is on the host entry's critical path before any device work).
+static void scan_pieces(const bsb_ext_job_t *jobs, int64_t n, int64_t per, int nck, int64_t seq_bytes,
+                        const uint8_t *tile_map, JobScan *piece)
+{
+    const int64_t kSlice = 1 << 16;
+    const int64_t n_slices = (n + kSlice - 1) / kSlice;
+    std::vector<JobScan> sl((size_t)n_slices);
+    auto run = [&](int64_t a, int64_t b) {
+        for (int64_t k = a; k < b; ++k)
+            sl[(size_t)k] = scan_jobs(jobs, k * kSlice, std::min(n, (k + 1) * kSlice), seq_bytes, tile_map);
+    };
+    unsigned hw = std::thread::hardware_concurrency();
+    int T = (int)std::min<int64_t>(n_slices, hw ? (int64_t)hw : 4);
+    if (T > 16) T = 16;
+    if (T <= 1) {
+        run(0, n_slices);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < T; ++t) th.emplace_back(run, n_slices * t / T, n_slices * (t + 1) / T);
+        for (auto &x : th) x.join();
+    }
+    for (int k = 0; k < nck; ++k) piece[k] = JobScan{n, 0, 0};
+    for (int64_t k = 0; k < n_slices; ++k) {        // a slice may straddle two pieces: split it
+        const int64_t lo = k * kSlice, hi = std::min(n, lo + kSlice);
+        const int a = (int)(lo / per), b = (int)((hi - 1) / per);
+        if (a == b) {
+            JobScan &p = piece[a];
+            p.first_bad = std::min(p.first_bad, sl[(size_t)k].first_bad < hi ? sl[(size_t)k].first_bad : n);
+            p.tiles |= sl[(size_t)k].tiles;
+            p.need = std::max(p.need, sl[(size_t)k].need);
+        } else {
+            for (int c = a; c <= b; ++c) {
+                const JobScan q = scan_jobs(jobs, std::max(lo, c * per), std::min(hi, (c + 1) * per), seq_bytes,
+                                            tile_map);
+                JobScan &p = piece[c];
+                p.first_bad = std::min(p.first_bad, q.first_bad < std::min(hi, (c + 1) * per) ? q.first_bad : n);
+                p.tiles |= q.tiles;
+                p.need = std::max(p.need, q.need);
+            }
+        }
+    }
+}
+
 // Device-buffer extension with the tile shapes `tiles` launched (every shape
 // the context's map uses when the caller cannot tell which are needed).
 static int extend_device(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_ext_job_t *d_jobs,
                          int64_t n_jobs, const uint8_t *d_seq, int64_t seq_bytes, const int32_t *d_cost,
-                         bsb_ext_out_t *d_out, int64_t *d_cells, uint64_t tiles)
+                         bsb_ext_out_t *d_out, int64_t *d_cells, uint64_t tiles, cudaEvent_t e0 = nullptr,
+                         cudaEvent_t e1 = nullptr)
 {
     if (!ctx) return BSB_EINVAL;
     KswParams P;
@@ -193,7 +302,8 @@ static int extend_device(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_e
     if ((rc = bsb_ensure(ctx, &ctx->scratch, &ctx->scratch_bytes, ksw_scratch_bytes(n_jobs), "extension scratch")))
         return rc;
     cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, d_cost, ctx->d_tile_map, tiles, d_out, d_cells,
-                               ctx->scratch, ctx->n_sm, ctx->stream, ctx->ev0, ctx->ev1, ctx->tile_ev);
+                               ctx->scratch, ctx->n_sm, ctx->stream, e0 ? e0 : ctx->ev0, e1 ? e1 : ctx->ev1,
+                               ctx->tile_ev, &ctx->ms);
     ctx->pending_ksw = 1;
     ctx->last_tiles = tiles;
     return bsb_cuda(ctx, e, "extension launch");
@@ -284,7 +394,18 @@ extern "C" int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, cons
     KswParams P;
     int rc = check_param(ctx, param, &P);
     if (rc) return rc;
-    if ((rc = check_jobs(ctx, jobs, n_jobs, seq_bytes))) return rc;
+    // Large batches are extended in pieces of consecutive jobs: piece k starts once the
+    // sequence prefix its jobs reference and its job records are on the device (h2d
+    // stream), and its tuples return (d2h stream) while piece k+1 runs.  Jobs laid out in
+    // buffer order make that prefix grow piece by piece; any other layout is still
+    // correct, it just overlaps less.
+    const int64_t per = n_jobs >= kChunkFrom ? (n_jobs + BSB_MAX_CHUNKS - 1) / BSB_MAX_CHUNKS : n_jobs;
+    const int nck = (int)((n_jobs + per - 1) / per);
+    JobScan piece[BSB_MAX_CHUNKS];
+    scan_pieces(jobs, n_jobs, per, nck, seq_bytes, ctx->tile_map, piece);
+    for (int k = 0; k < nck; ++k)          // every job is checked before any device work
+        if (piece[k].first_bad < n_jobs) return check_jobs(ctx, jobs + piece[k].first_bad, 1, seq_bytes,
+                                                           piece[k].first_bad);
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
 
     const size_t jb = sizeof(bsb_ext_job_t) * (size_t)n_jobs;
@@ -299,19 +420,40 @@ extern "C" int bsb_extend_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, cons
     bsb_ext_out_t *d_out = (bsb_ext_out_t *)ctx->d_out;
     int64_t *d_cells = cells_out ? (int64_t *)((char *)ctx->d_out + ((ob + 255) & ~(size_t)255)) : nullptr;
 
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seq, seq, seq_bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D seq")))
+    if ((rc = bsb_ensure(ctx, &ctx->scratch, &ctx->scratch_bytes, ksw_scratch_bytes(per), "extension scratch")))
         return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_jobs, jobs, jb, cudaMemcpyHostToDevice, ctx->stream), "H2D jobs")))
-        return rc;
-    uint64_t tiles = 0;         // only the shapes these query lengths map to
-    for (int64_t i = 0; i < n_jobs; ++i) tiles |= 1ull << ctx->tile_map[jobs[i].qlen + 1];
-    if ((rc = extend_device(ctx, param, d_jobs, n_jobs, d_seq, seq_bytes, nullptr, d_out, d_cells, tiles)))
-        return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream), "D2H out")))
-        return rc;
-    if (cells_out &&
-        (rc = bsb_cuda(ctx, cudaMemcpyAsync(cells_out, d_cells, cb, cudaMemcpyDeviceToHost, ctx->stream), "D2H cells")))
-        return rc;
+    // the stream must not still read the staging buffers from an earlier call when h2d overwrites them
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize"))) return rc;
+    int64_t done = 0;
+    for (int k = 0; k < nck; ++k) {
+        const int64_t lo = k * per, cnt = n_jobs - lo < per ? n_jobs - lo : per;
+        const int64_t need = piece[k].need;
+        const uint64_t tiles = piece[k].tiles;     // only the shapes these query lengths map to
+        cudaEvent_t *ev = ctx->chunk_ev + 4 * k;      // in, out, start, end
+        if (need > done &&
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seq + done, seq + done, need - done, cudaMemcpyHostToDevice, ctx->h2d),
+                           "H2D seq")))
+            return rc;
+        done = need > done ? need : done;
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_jobs + lo, jobs + lo, sizeof(bsb_ext_job_t) * cnt,
+                                                cudaMemcpyHostToDevice, ctx->h2d), "H2D jobs")) ||
+            (rc = bsb_cuda(ctx, cudaEventRecord(ev[0], ctx->h2d), "event")) ||
+            (rc = bsb_cuda(ctx, cudaStreamWaitEvent(ctx->stream, ev[0], 0), "event")))
+            return rc;
+        if ((rc = extend_device(ctx, param, d_jobs + lo, cnt, d_seq, seq_bytes, nullptr, d_out + lo,
+                                d_cells ? d_cells + lo : nullptr, tiles, ev[2], ev[3])))
+            return rc;
+        if ((rc = bsb_cuda(ctx, cudaEventRecord(ev[1], ctx->stream), "event")) ||
+            (rc = bsb_cuda(ctx, cudaStreamWaitEvent(ctx->d2h, ev[1], 0), "event")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(out + lo, d_out + lo, sizeof(bsb_ext_out_t) * cnt,
+                                                cudaMemcpyDeviceToHost, ctx->d2h), "D2H out")))
+            return rc;
+        if (cells_out && (rc = bsb_cuda(ctx, cudaMemcpyAsync(cells_out + lo, d_cells + lo, sizeof(int64_t) * cnt,
+                                                             cudaMemcpyDeviceToHost, ctx->d2h), "D2H cells")))
+            return rc;
+    }
+    ctx->n_chunks = nck;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->d2h), "D2H synchronize"))) return rc;
     return bsb_sync(ctx);
 }
 
@@ -322,13 +464,20 @@ extern "C" int bsb_sync(bsb_ctx *ctx)
     if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize"))) return rc;
     if (ctx->pending_ksw) {
         ctx->pending_ksw = 0;
-        cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1);
-        for (int t = 0; t < BSB_NUM_TILES; ++t) {       // each shape until the next launched one
+        if (ctx->n_chunks) {        // a host batch in pieces: the sum of the pieces' extension times
+            ctx->last_kernel_ms = 0.f;
+            for (int k = 0; k < ctx->n_chunks; ++k) {
+                float m = 0.f;
+                cudaEventElapsedTime(&m, ctx->chunk_ev[4 * k + 2], ctx->chunk_ev[4 * k + 3]);
+                ctx->last_kernel_ms += m;
+            }
+            ctx->n_chunks = 0;
+        } else {
+            cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1);
+        }
+        for (int t = 0; t < BSB_NUM_TILES; ++t) {
             ctx->tile_ms[t] = 0.f;
-            if (!(ctx->last_tiles >> t & 1)) continue;
-            int u = t + 1;
-            while (u < BSB_NUM_TILES && !(ctx->last_tiles >> u & 1)) ++u;
-            cudaEventElapsedTime(&ctx->tile_ms[t], ctx->tile_ev[t], ctx->tile_ev[u]);
+            if (ctx->last_tiles >> t & 1) cudaEventElapsedTime(&ctx->tile_ms[t], ctx->tile_ev[2 * t], ctx->tile_ev[2 * t + 1]);
         }
         int rej = 0;
         if ((rc = bsb_cuda(ctx, cudaMemcpy(&rej, ksw_rejected_counter(ctx->scratch), sizeof(int),

@@ -14,6 +14,16 @@
 #define BSB_SEED_MAX_LEN 1024
 // Longest read the full seed-chain-extend batch accepts (extension tiles up to 16 columns per lane).
 #define BSB_ALIGN_MAX_LEN 512
+// Most pieces the host extension entry splits a batch into (copies overlap the extension).
+#define BSB_MAX_CHUNKS 8
+#define BSB_AUX_STREAMS 3
+
+// Fork/join streams for the per-shape extension kernels of one batch.
+struct KswStreams {
+    cudaStream_t aux[BSB_AUX_STREAMS] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[BSB_AUX_STREAMS] = {};
+};
 
 struct bsb_ctx {
     int device = 0;
@@ -51,11 +61,18 @@ struct bsb_ctx {
     uint8_t tile_map[BSB_TILE_MAP_LEN] = {};
     uint8_t *d_tile_map = nullptr;
     uint64_t map_tiles = 0;
-    // per-shape device time of the last extension batch: tile_ev[t] is recorded before
-    // shape t's kernel, tile_ev[BSB_NUM_TILES] after the last one
-    cudaEvent_t tile_ev[BSB_NUM_TILES + 1] = {};
+    // per-shape device time of the last extension batch: tile_ev[2t], tile_ev[2t+1] are
+    // recorded around shape t's kernel on the stream it runs on
+    cudaEvent_t tile_ev[2 * BSB_NUM_TILES] = {};
     uint64_t last_tiles = 0;
     float tile_ms[BSB_NUM_TILES] = {};
+    // extra streams: shape kernels of one batch run on `stream` and aux[] so that one
+    // shape's tail overlaps the next; h2d/d2h carry the host entry's chunked copies
+    KswStreams ms;
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    // host entry chunks: copy-in done, extension done, extension start/end marks
+    cudaEvent_t chunk_ev[4 * BSB_MAX_CHUNKS] = {};
+    int n_chunks = 0;
     // chaining / chain-extension scratch
     void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
     size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;
@@ -90,11 +107,15 @@ int *ksw_rejected_counter(void *scratch);
 // d_map: the tile map in device memory (BSB_TILE_MAP_LEN bytes), or NULL for
 // the built-in default; tiles: bit t set = launch tile shape t (the shapes the
 // batch's query lengths map to; a shape left out leaves its jobs unrun).
-// tile_ev (optional, BSB_NUM_TILES + 1 events): per-shape timing marks as in bsb_ctx.
+// tile_ev (optional, 2 * BSB_NUM_TILES events): per-shape timing marks as in bsb_ctx.
+// ms (optional): run the shape kernels of batches below ksw_concurrent_below() jobs
+// on st and ms->aux (joined back into st before ev1).
 cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
                        const uint8_t *d_seq, const int32_t *d_cost, const uint8_t *d_map, uint64_t tiles,
                        bsb_ext_out_t *d_out, int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
-                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev = nullptr);
+                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev = nullptr,
+                       const KswStreams *ms = nullptr);
+int64_t ksw_concurrent_below();
 // The built-in tile map (host copy, BSB_TILE_MAP_LEN entries).
 const uint8_t *ksw_default_tile_map();
 // Shape of tile t; -1 if t is out of range.

@@ -155,6 +155,8 @@ size_t ksw_scratch_bytes(int64_t n) { return fixed_bytes() + sizeof(int32_t) * 2
 
 int ksw_max_qlen() { return kMaxNeed - 1; }
 
+int64_t ksw_concurrent_below() { return (int64_t)1 << 20; }
+
 int *ksw_rejected_counter(void *scratch) { return (int *)scratch + kNumTiles; }
 
 const uint8_t *ksw_default_tile_map() { return kDefaultTileMap.tile; }
@@ -177,7 +179,7 @@ uint64_t ksw_map_tiles(const uint8_t *map)
 cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t n, int64_t seq_bytes,
                        const uint8_t *d_seq, const int32_t *d_cost, const uint8_t *d_map, uint64_t tiles,
                        bsb_ext_out_t *d_out, int64_t *d_cells, void *scratch, int n_sm, cudaStream_t st,
-                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev)
+                       cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev, const KswStreams *ms)
 {
     char *p = (char *)scratch;
     int *counter = (int *)p;
@@ -198,15 +200,32 @@ cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t 
         ksw_sched_scatter<<<nb, 256, 0, st>>>(key, (int)n, cursor, order);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        // Small batches: the shapes run on four streams, so the next shape's blocks fill
+        // the SMs a finishing shape leaves during its tail.  Large batches keep one stream
+        // (the tails are a small part of them, and each shape is timed alone).
+        const bool conc = ms && n < ksw_concurrent_below();
+        if (conc) {
+            cudaEventRecord(ms->fork, st);
+            for (int a = 0; a < BSB_AUX_STREAMS; ++a) cudaStreamWaitEvent(ms->aux[a], ms->fork, 0);
+        }
+        int k = 0;
         for (int t = 0; t < kNumTiles; ++t) {
             if (!(tiles >> t & 1)) continue;
             KswTileLaunch f = ksw_tile_launcher(t);
             if (!f) return cudaErrorInvalidValue;
-            if (tile_ev) cudaEventRecord(tile_ev[t], st);
-            e = f(P, d_jobs, d_seq, order, bin_start, t, counter, d_out, d_cells, n_sm, st);
+            const int lane = k++ % (BSB_AUX_STREAMS + 1);
+            cudaStream_t s = conc && lane ? ms->aux[lane - 1] : st;
+            if (tile_ev) cudaEventRecord(tile_ev[2 * t], s);
+            e = f(P, d_jobs, d_seq, order, bin_start, t, counter, d_out, d_cells, n_sm, s);
             if (e != cudaSuccess) return e;
+            if (tile_ev) cudaEventRecord(tile_ev[2 * t + 1], s);
         }
-        if (tile_ev) cudaEventRecord(tile_ev[kNumTiles], st);
+        if (conc) {
+            for (int a = 0; a < BSB_AUX_STREAMS; ++a) {
+                cudaEventRecord(ms->join[a], ms->aux[a]);
+                cudaStreamWaitEvent(st, ms->join[a], 0);
+            }
+        }
     }
     if (ev1) cudaEventRecord(ev1, st);
     return cudaSuccess;

@@ -70,7 +70,10 @@ typedef struct {
 } bsb_ext_out_t;
 
 /* Replaces a loop of ksw_extend2 calls (bsbolt/External/BWA/ksw.c:380-479,
- * declared ksw.h:98-99) with one batch.  Host buffers; synchronous.
+ * declared ksw.h:98-99) with one batch.  Host buffers; synchronous.  A batch
+ * of 2^20 jobs or more runs in pieces whose host<->device copies overlap the
+ * extension of the neighbouring pieces (best when the jobs' bytes are laid
+ * out in job order in seq; the result never depends on it).
  * cells_out (optional, may be NULL) receives per job the number of DP cells
  * the reference visits (sum over rows of end-beg).  Requires qlen <= 1023,
  * 1 <= e_del, e_ins <= 65535, 0 <= o_del, o_ins <= 65535, matrix entries in
@@ -124,9 +127,11 @@ int bsb_tile_shapes(int32_t *G, int32_t *C, int max);
 int bsb_set_tile_map(bsb_ctx *ctx, const uint8_t *map, int n);
 
 /* Device time of each shape's kernel in the context's most recent extension
- * batch (CUDA events on the context stream between consecutive shape
- * launches), ms[t] for t < min(n, BSB_NUM_TILES); 0 for shapes not launched.
- * Valid after bsb_sync. */
+ * batch (CUDA events around its launch on the stream it ran on), ms[t] for
+ * t < min(n, BSB_NUM_TILES); 0 for shapes not launched.  Batches below 2^20
+ * jobs run their shapes on four streams at once, so a shape's time there
+ * includes sharing the GPU; a host batch extended in pieces reports its last
+ * piece.  Valid after bsb_sync. */
 int bsb_last_tile_ms(const bsb_ctx *ctx, float *ms, int n);
 
 /* Copies the context's current tile map into map (n >= BSB_TILE_MAP_LEN);

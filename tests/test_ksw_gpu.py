@@ -117,3 +117,18 @@ def test_ksw_errors(gpu_ctx):
     out = extend.ksw_extend2_batch(gpu_ctx, jobs, seq, mat, 6, 1, 6, 1, 100)
     ref, _ = oracle.ksw_batch(jobs, seq, mat, 6, 1, 6, 1, 100)
     assert_same(out, ref, "after errors")
+
+
+@pytest.mark.parametrize("reverse", [False, True], ids=["buffer-order", "reversed"])
+def test_ksw_host_batch_in_pieces(gpu_ctx, reverse):
+    """A host batch of >= 2^20 jobs is extended in pieces whose copies overlap the
+    extension; tuples and cell counts still equal the oracle's, whatever the layout."""
+    jobs, seq = synth.ksw_jobs((1 << 20) + 12345, seed=4242)
+    if reverse:
+        jobs = jobs[::-1].copy()
+    mat = synth.fill_scmat(1, 4)
+    out, cells = extend.ksw_extend2_batch(gpu_ctx, jobs, seq, mat, 6, 1, 6, 1, 100, want_cells=True)
+    ref, rcells = oracle.ksw_batch(jobs, seq, mat, 6, 1, 6, 1, 100, n_threads=os.cpu_count() or 4)
+    assert_same(out, ref, "pieces")
+    assert np.array_equal(cells, rcells)
+    assert gpu_ctx.last_kernel_ms() > 0
