@@ -95,51 +95,33 @@ __device__ __forceinline__ Occ4 occ4(const DevFM &F, uint64_t k)
     return occ_in_block(load_block(F, kk), kk);
 }
 
-// bwt_2occ4 (bwt.c:189-220): one block fetch when k and l share a 128-symbol bucket.
+// bwt_2occ4 (bwt.c:189-220) without branches: both blocks are always loaded (the same
+// 64 bytes twice when k and l share a 128-symbol bucket, the second from L1), so the
+// threads of a warp never split over which case they are in.
 __device__ __forceinline__ void occ4_pair(const DevFM &F, uint64_t k, uint64_t l, Occ4 &ok, Occ4 &ol)
 {
-    const uint64_t kk = k - (k >= F.primary), ll = l - (l >= F.primary);
-    if (k != (uint64_t)-1 && l != (uint64_t)-1 && (kk >> 7) == (ll >> 7)) {
-        const Block b = load_block(F, kk);
-        ok = occ_in_block(b, kk);
-        ol = occ_in_block(b, ll);
-    } else {
-        ok = occ4(F, k);
-        ol = occ4(F, l);
-    }
+    const bool kz = k == (uint64_t)-1, lz = l == (uint64_t)-1;
+    const uint64_t kk = kz ? 0 : k - (k >= F.primary), ll = lz ? 0 : l - (l >= F.primary);
+    const Block bk = load_block(F, kk), bl = load_block(F, ll);
+    ok = occ_in_block(bk, kk);
+    ol = occ_in_block(bl, ll);
+    if (kz) ok.c[0] = ok.c[1] = ok.c[2] = ok.c[3] = 0;
+    if (lz) ol.c[0] = ol.c[1] = ol.c[2] = ol.c[3] = 0;
 }
 
-// bwt_extend (bwt.c:262-275): extension of ik by every base; is_back selects the direction.
-__device__ __forceinline__ void bwt_extend_dev(const DevFM &F, const DevIntv &ik, DevIntv ok[4], bool is_back)
+// F.L2[i] for i = 0..4, indexed with constants only (a dynamic index would copy the
+// kernel parameter to local memory).
+__device__ __forceinline__ uint64_t l2_at(const DevFM &F, int i)
 {
-    const uint64_t xf = is_back ? ik.x0 : ik.x1;     // x[!is_back]
-    const uint64_t xb = is_back ? ik.x1 : ik.x0;     // x[is_back]
-    Occ4 tk, tl;
-    occ4_pair(F, xf - 1, xf - 1 + ik.x2, tk, tl);
-    uint64_t sz[4], fw[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        fw[i] = F.L2[i] + 1 + tk.c[i];
-        sz[i] = tl.c[i] - tk.c[i];
-    }
-    uint64_t bk3 = xb + (xf <= F.primary && xf + ik.x2 - 1 >= F.primary);
-    uint64_t bk2 = bk3 + sz[3], bk1 = bk2 + sz[2], bk0 = bk1 + sz[1];
-    const uint64_t bk[4] = {bk0, bk1, bk2, bk3};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        if (is_back) { ok[i].x0 = fw[i]; ok[i].x1 = bk[i]; }
-        else { ok[i].x1 = fw[i]; ok[i].x0 = bk[i]; }
-        ok[i].x2 = sz[i];
-        ok[i].info = 0;
-    }
+    return i == 0 ? F.L2[0] : i == 1 ? F.L2[1] : i == 2 ? F.L2[2] : i == 3 ? F.L2[3] : F.L2[4];
 }
 
 __device__ __forceinline__ DevIntv set_intv(const DevFM &F, int c)   // bwt.h:80
 {
     DevIntv r;
-    r.x0 = F.L2[c] + 1;
-    r.x2 = F.L2[c + 1] - F.L2[c];
-    r.x1 = F.L2[3 - c] + 1;
+    r.x0 = l2_at(F, c) + 1;
+    r.x2 = l2_at(F, c + 1) - l2_at(F, c);
+    r.x1 = l2_at(F, 3 - c) + 1;
     r.info = 0;
     return r;
 }

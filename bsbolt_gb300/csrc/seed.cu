@@ -25,187 +25,306 @@ struct SeedOpt {
     int min_seed_len, split_len, split_width, max_mem_intv;
 };
 
-// bwt_smem1 == bwt_smem1a(max_intv = 0).  mem receives the SMEMs covering x, sorted
-// by start; returns the end of the longest match from x.  lists: 2*(len+2) entries.
-__device__ int smem1(const DevFM &F, int len, const uint8_t *__restrict__ q, int x, int min_intv,
-                     DevIntv *__restrict__ mem, int &n_mem, DevIntv *__restrict__ lists, int cap)
-{
-    DevIntv ik, ok[4];
-    DevIntv *curr = lists, *prev = lists + cap;
-    int i, n_curr = 0, n_prev, ret;
-    n_mem = 0;
-    if (q[x] > 3) return x + 1;
-    if (min_intv < 1) min_intv = 1;
-    ik = set_intv(F, q[x]);
-    ik.info = (uint64_t)(x + 1);
-    // forward: remember the interval whenever its size is about to change
-    for (i = x + 1; i < len; ++i) {
-        const int b = q[i];
-        if (b < 4) {
-            const int c = 3 - b;
-            bwt_extend_dev(F, ik, ok, false);
-            if (ok[c].x2 != ik.x2) {
-                curr[n_curr++] = ik;
-                if (ok[c].x2 < (uint64_t)min_intv) break;
-            }
-            ik = ok[c];
-            ik.info = (uint64_t)(i + 1);
-        } else {
-            curr[n_curr++] = ik;
-            break;
-        }
-    }
-    if (i == len) curr[n_curr++] = ik;
-    for (int j = 0; j < n_curr / 2; ++j) {
-        DevIntv t = curr[j];
-        curr[j] = curr[n_curr - 1 - j];
-        curr[n_curr - 1 - j] = t;
-    }
-    ret = (int)(uint32_t)curr[0].info;
-    { DevIntv *s = curr; curr = prev; prev = s; }
-    n_prev = n_curr;
-    // backward: grow every remembered interval to the left
-    for (i = x - 1; i >= -1; --i) {
-        const int c = i < 0 ? -1 : (q[i] < 4 ? q[i] : -1);
-        n_curr = 0;
-        for (int j = 0; j < n_prev; ++j) {
-            const DevIntv p = prev[j];
-            if (c >= 0) bwt_extend_dev(F, p, ok, true);
-            if (c < 0 || ok[c].x2 < (uint64_t)min_intv) {
-                if (n_curr == 0) {
-                    if (n_mem == 0 || (uint64_t)(i + 1) < (mem[n_mem - 1].info >> 32)) {
-                        DevIntv m = p;
-                        m.info |= (uint64_t)(i + 1) << 32;
-                        mem[n_mem++] = m;
-                    }
-                }
-            } else if (n_curr == 0 || ok[c].x2 != curr[n_curr - 1].x2) {
-                DevIntv m = ok[c];
-                m.info = p.info;
-                curr[n_curr++] = m;
-            }
-        }
-        if (n_curr == 0) break;
-        { DevIntv *s = curr; curr = prev; prev = s; }
-        n_prev = n_curr;
-    }
-    for (int j = 0; j < n_mem / 2; ++j) {
-        DevIntv t = mem[j];
-        mem[j] = mem[n_mem - 1 - j];
-        mem[n_mem - 1 - j] = t;
-    }
-    return ret;
-}
-
-__device__ int seed_strategy1(const DevFM &F, int len, const uint8_t *__restrict__ q, int x, int min_len,
-                              int max_intv, DevIntv &mem)
-{
-    DevIntv ik, ok[4];
-    mem.x0 = mem.x1 = mem.x2 = mem.info = 0;
-    if (q[x] > 3) return x + 1;
-    ik = set_intv(F, q[x]);
-    for (int i = x + 1; i < len; ++i) {
-        if (q[i] < 4) {
-            const int c = 3 - q[i];
-            bwt_extend_dev(F, ik, ok, false);
-            if (ok[c].x2 < (uint64_t)max_intv && i - x >= min_len) {
-                mem = ok[c];
-                mem.info = (uint64_t)x << 32 | (uint64_t)(i + 1);
-                return i + 1;
-            }
-            ik = ok[c];
-        } else return i + 1;
-    }
-    return len;
-}
-
 __device__ __forceinline__ int seed_len(const DevIntv &p)
 {
     return (int)((uint32_t)p.info - (uint32_t)(p.info >> 32));
 }
 
-// Persistent: each thread takes reads from a counter.  out holds, per read r,
-// cap(r) = 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r.
-__global__ void __launch_bounds__(kSeedBlock)
+// bwt_extend (bwt.c:262-275) of ik by the single base c: the reference computes all
+// four extensions and its callers keep ok[c] only, so only that one is formed here.
+__device__ __forceinline__ DevIntv extend_one(const DevFM &F, const DevIntv &ik, bool is_back, int c)
+{
+    const uint64_t xf = is_back ? ik.x0 : ik.x1;     // x[!is_back]
+    const uint64_t xb = is_back ? ik.x1 : ik.x0;     // x[is_back]
+    Occ4 tk, tl;
+    occ4_pair(F, xf - 1, xf - 1 + ik.x2, tk, tl);
+    const uint64_t s0 = tl.c[0] - tk.c[0], s1 = tl.c[1] - tk.c[1], s2 = tl.c[2] - tk.c[2], s3 = tl.c[3] - tk.c[3];
+    const uint64_t tkc = c == 0 ? tk.c[0] : c == 1 ? tk.c[1] : c == 2 ? tk.c[2] : tk.c[3];
+    const uint64_t szc = c == 0 ? s0 : c == 1 ? s1 : c == 2 ? s2 : s3;
+    const uint64_t above = c == 0 ? s1 + s2 + s3 : c == 1 ? s2 + s3 : c == 2 ? s3 : 0;   // bases > c
+    const uint64_t l2c = l2_at(F, c);
+    const uint64_t fw = l2c + 1 + tkc;
+    const uint64_t bk = xb + (xf <= F.primary && xf + ik.x2 - 1 >= F.primary) + above;
+    DevIntv o;
+    o.x0 = is_back ? fw : bk;
+    o.x1 = is_back ? bk : fw;
+    o.x2 = szc;
+    o.info = 0;
+    return o;
+}
+
+// Seeding state machine.  Each loop iteration, every thread first runs its read's
+// bookkeeping up to the next bwt_extend it needs (divergent, cheap), then all
+// threads perform that extend together (converged, the expensive part), then apply
+// its result.  The bookkeeping is mem_collect_intv (bwamem.c:118-166):
+//   pass 1  bwt_smem1 from every x (bwt.c:289-356), keep SMEMs >= min_seed_len;
+//   pass 2  re-seed from the middle of SMEMs >= split_len with <= split_width hits;
+//   pass 3  bwt_seed_strategy1 (bwt.c:358-379) from every x;
+// then the read's seeds are sorted by info (equal info = the same substring and so
+// the same interval: no tie rule is needed, and the order seeds are found in does
+// not matter).  bwt_smem1 runs as:
+//   FWD  extend ik forward from x, pushing ik whenever its size is about to change;
+//        the pushes go down from the top of list A, so read upwards they are the
+//        reference's reversed curr list;
+//   BWD  one round per position i = x-1 .. -1: extend every prev entry backward by
+//        q[i]; entries that fail may emit an SMEM (only while nothing has survived
+//        this round), survivors are deduplicated by size into curr.
+enum SeedState : int {
+    kNeedRead, kP1X, kFwd, kFwdEnd, kBwdRound, kBwdEntry, kSmemDone, kP2K, kP3X, kP3Fwd, kFinish, kExit
+};
+
+// Persistent: each thread takes work items from a counter, two per read: item 2r
+// runs passes 1 and 2 of read r, item 2r+1 its pass 3 (independent of the other two).
+// out holds, per read r, 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r:
+// the first part_cap0(len) for passes 1-2, the rest (at least len/2 + 8: pass 3 finds
+// at most one seed per min_seed_len + 1 >= 2 bases) for pass 3.  Each part is sorted
+// by info on its own and counted in count[2r + part]; compact_seeds merges the two.
+__device__ __host__ __forceinline__ int part_cap1(int len) { return len / 2 + 8; }
+__device__ __host__ __forceinline__ int part_cap0(int len) { return 2 * len + 32 - part_cap1(len); }
+
+__global__ void __launch_bounds__(kSeedBlock, 4)
 seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs, const int64_t *__restrict__ offs,
             DevIntv *__restrict__ out, int *__restrict__ count, DevIntv *__restrict__ scratch, int list_cap,
             int *__restrict__ next_read, int *__restrict__ overflow)
 {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    DevIntv *lists = scratch + (size_t)tid * 3 * list_cap;   // curr/prev lists, then mem
-    DevIntv *mem = lists + 2 * list_cap;
+    DevIntv *const listA = scratch + (size_t)tid * 3 * list_cap;     // forward pushes / curr and prev rounds
+    DevIntv *const listB = listA + list_cap;
+    DevIntv *const mem = listB + list_cap;                           // SMEMs of one bwt_smem1 call
     const int64_t base_off = offs[0];
+
+    int st = kNeedRead;
+    // read
+    int r = 0, part = 0, len = 0, cap = 0, n = 0, old_n = 0;
+    const uint8_t *q = nullptr;
+    DevIntv *dst = nullptr;
+    // bwt_smem1
+    int pass = 1, x = 0, i = 0, min_intv = 1, n_curr = 0, n_prev = 0, n_mem = 0, j = 0, c = 0, ret = 0, k = 0;
+    uint64_t last_mem_start = 0, last_x2 = 0;
+    DevIntv ik, p;
+    DevIntv *prev = listA, *curr = listB;
+    // bwt_seed_strategy1
+    int x0 = 0;
+    ik.x0 = ik.x1 = ik.x2 = ik.info = 0;
+    p = ik;
+
     for (;;) {
-        const int r = atomicAdd(next_read, 1);
-        if (r >= n_reads) break;
-        const int64_t o = offs[r];
-        const int64_t len64 = offs[r + 1] - o;
-        if (len64 < 0 || len64 > list_cap - 2) {    // outside the scratch the launch sized: refuse, never overrun
-            count[r] = 0;
-            atomicMax(overflow, r + 1);
-            continue;
-        }
-        const int len = (int)len64;
-        const uint8_t *q = seqs + o;
-        DevIntv *dst = out + 2 * (o - base_off) + 32 * (int64_t)r;
-        const int cap = 2 * len + 32;
-        int n = 0, nm;
-        if (len < opt.min_seed_len) {     // mem_chain returns before seeding (bwamem.c:266)
-            count[r] = 0;
-            continue;
-        }
-        // pass 1
-        for (int x = 0; x < len;) {
-            if (q[x] < 4) {
-                x = smem1(F, len, q, x, 1, mem, nm, lists, list_cap);
-                for (int i = 0; i < nm; ++i)
-                    if (seed_len(mem[i]) >= opt.min_seed_len) {
-                        if (n < cap) dst[n] = mem[i];
-                        ++n;
-                    }
-            } else ++x;
-        }
-        // pass 2
-        const int old_n = n < cap ? n : cap;
-        for (int k = 0; k < old_n; ++k) {
-            const DevIntv p = dst[k];
-            const int start = (int)(p.info >> 32), end = (int)(uint32_t)p.info;
-            if (end - start < opt.split_len || p.x2 > (uint64_t)opt.split_width) continue;
-            smem1(F, len, q, (start + end) >> 1, (int)p.x2 + 1, mem, nm, lists, list_cap);
-            for (int i = 0; i < nm; ++i)
-                if (seed_len(mem[i]) >= opt.min_seed_len) {
-                    if (n < cap) dst[n] = mem[i];
-                    ++n;
+        // ---- bookkeeping up to the next extension (or the end of the work)
+        DevIntv e_ik;
+        bool e_back = false;
+        int e_c = 0;
+        bool need = false;
+        while (!need && st != kExit) {
+            switch (st) {
+            case kNeedRead: {
+                const int w = atomicAdd(next_read, 1);
+                if (w >= 2 * n_reads) { st = kExit; break; }
+                r = w >> 1;
+                part = w & 1;
+                const int64_t o = offs[r];
+                const int64_t len64 = offs[r + 1] - o;
+                if (len64 < 0 || len64 > list_cap - 2) {    // outside the scratch the launch sized: refuse
+                    count[w] = 0;
+                    atomicMax(overflow, r + 1);
+                    break;
                 }
-        }
-        // pass 3
-        if (opt.max_mem_intv > 0) {
-            for (int x = 0; x < len;) {
-                if (q[x] < 4) {
-                    DevIntv m;
-                    x = seed_strategy1(F, len, q, x, opt.min_seed_len, opt.max_mem_intv, m);
-                    if (m.x2 > 0) {
+                len = (int)len64;
+                q = seqs + o;
+                dst = out + 2 * (o - base_off) + 32 * (int64_t)r + (part ? part_cap0(len) : 0);
+                cap = part ? part_cap1(len) : part_cap0(len);
+                n = 0;
+                if (len < opt.min_seed_len || (part && opt.max_mem_intv <= 0)) {
+                    count[w] = 0;                            // mem_chain returns before seeding (bwamem.c:266)
+                    break;
+                }
+                x = 0;
+                st = part ? kP3X : kP1X;
+                break;
+            }
+            case kP1X:
+                if (x >= len) {                             // pass 1 done
+                    old_n = n < cap ? n : cap;
+                    k = 0;
+                    st = kP2K;
+                    break;
+                }
+                if (q[x] > 3) { ++x; break; }
+                pass = 1;
+                min_intv = 1;
+                goto smem_start;
+            case kP2K: {
+                if (k >= old_n) { st = kFinish; break; }
+                const DevIntv s = dst[k];
+                const int start = (int)(s.info >> 32), end = (int)(uint32_t)s.info;
+                if (end - start < opt.split_len || s.x2 > (uint64_t)opt.split_width) { ++k; break; }
+                pass = 2;
+                x = (start + end) >> 1;
+                min_intv = (int)s.x2 + 1;
+                if (q[x] > 3) { ++k; break; }               // bwt_smem1 returns at once: no SMEM
+                goto smem_start;
+            }
+            smem_start:
+                if (min_intv < 1) min_intv = 1;
+                ik = set_intv(F, q[x]);
+                ik.info = (uint64_t)(x + 1);
+                n_curr = 0;
+                i = x + 1;
+                st = kFwd;
+                break;
+            case kFwd:
+                if (i < len && q[i] < 4) {
+                    e_ik = ik; e_back = false; e_c = 3 - q[i];
+                    need = true;
+                    break;
+                }
+                listA[list_cap - 1 - n_curr++] = ik;        // an N or the read end stops the match
+                st = kFwdEnd;
+                break;
+            case kFwdEnd:
+                prev = listA + list_cap - n_curr;            // reversed forward list
+                curr = listB;
+                n_prev = n_curr;
+                ret = (int)(uint32_t)prev[0].info;
+                n_mem = 0;
+                i = x - 1;
+                st = kBwdRound;
+                break;
+            case kBwdRound:
+                c = i < 0 ? -1 : (q[i] < 4 ? q[i] : -1);
+                n_curr = 0;
+                j = 0;
+                st = kBwdEntry;
+                break;
+            case kBwdEntry:
+                if (j >= n_prev) {
+                    if (n_curr == 0) { st = kSmemDone; break; }
+                    // this round's curr becomes the next prev; the list the old prev lived in
+                    // (the forward pushes sit at the top of A) takes the next curr
+                    DevIntv *const was_prev = prev;
+                    prev = curr;
+                    curr = was_prev < listB ? listA : listB;
+                    n_prev = n_curr;
+                    --i;
+                    st = kBwdRound;
+                    break;
+                }
+                p = prev[j];
+                if (c >= 0) {
+                    e_ik = p; e_back = true; e_c = c;
+                    need = true;
+                    break;
+                }
+                // no base to extend by: p cannot grow, and is maximal if nothing survived yet
+                if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
+                    DevIntv m = p;
+                    m.info |= (uint64_t)(i + 1) << 32;
+                    mem[n_mem++] = m;
+                    last_mem_start = (uint64_t)(i + 1);
+                }
+                ++j;
+                break;
+            case kSmemDone:
+                for (int t = 0; t < n_mem; ++t) {
+                    const DevIntv m = mem[t];
+                    if (seed_len(m) >= opt.min_seed_len) {
                         if (n < cap) dst[n] = m;
                         ++n;
                     }
-                } else ++x;
+                }
+                if (pass == 1) { x = ret; st = kP1X; }
+                else { ++k; st = kP2K; }
+                break;
+            case kP3X:
+                if (x >= len) { st = kFinish; break; }
+                if (q[x] > 3) { ++x; break; }
+                ik = set_intv(F, q[x]);
+                x0 = x;
+                i = x + 1;
+                st = kP3Fwd;
+                break;
+            case kP3Fwd:
+                if (i >= len) { x = len; st = kP3X; break; }
+                if (q[i] > 3) { x = i + 1; st = kP3X; break; }
+                e_ik = ik; e_back = false; e_c = 3 - q[i];
+                need = true;
+                break;
+            case kFinish:
+                if (n > cap) {
+                    atomicMax(overflow, r + 1);
+                    n = cap;
+                }
+                // insertion sort by info (ks_introsort with intv_lt, bwamem.c:92-93; equal keys are equal values)
+                for (int a = 1; a < n; ++a) {
+                    const DevIntv v = dst[a];
+                    int b = a - 1;
+                    while (b >= 0 && dst[b].info > v.info) {
+                        dst[b + 1] = dst[b];
+                        --b;
+                    }
+                    dst[b + 1] = v;
+                }
+                count[2 * r + part] = n;
+                st = kNeedRead;
+                break;
+            default:
+                st = kExit;
+                break;
             }
         }
-        if (n > cap) {
-            atomicMax(overflow, r + 1);
-            n = cap;
+        if (!__any_sync(BSB_FULL_MASK, need)) {
+            if (st == kExit) break;
+            continue;
         }
-        // insertion sort by info (ks_introsort with intv_lt, bwamem.c:92-93; equal keys are equal values)
-        for (int i = 1; i < n; ++i) {
-            const DevIntv v = dst[i];
-            int j = i - 1;
-            while (j >= 0 && dst[j].info > v.info) {
-                dst[j + 1] = dst[j];
-                --j;
+
+        // ---- the extension, converged across the warp
+        DevIntv ok;
+        if (need) ok = extend_one(F, e_ik, e_back, e_c);
+
+        // ---- apply it
+        if (!need) continue;
+        switch (st) {
+        case kFwd:
+            if (ok.x2 != ik.x2) {
+                listA[list_cap - 1 - n_curr++] = ik;
+                if (ok.x2 < (uint64_t)min_intv) { st = kFwdEnd; break; }
             }
-            dst[j + 1] = v;
+            ik = ok;
+            ik.info = (uint64_t)(i + 1);
+            ++i;
+            break;
+        case kBwdEntry:
+            if (ok.x2 < (uint64_t)min_intv) {
+                if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
+                    DevIntv m = p;
+                    m.info |= (uint64_t)(i + 1) << 32;
+                    mem[n_mem++] = m;
+                    last_mem_start = (uint64_t)(i + 1);
+                }
+            } else if (n_curr == 0 || ok.x2 != last_x2) {
+                ok.info = p.info;
+                curr[n_curr++] = ok;
+                last_x2 = ok.x2;
+            }
+            ++j;
+            break;
+        case kP3Fwd:
+            if (ok.x2 < (uint64_t)opt.max_mem_intv && i - x0 >= opt.min_seed_len) {
+                if (ok.x2 > 0) {                            // an empty interval is not kept (bwamem.c:160)
+                    DevIntv m = ok;
+                    m.info = (uint64_t)x0 << 32 | (uint64_t)(i + 1);
+                    if (n < cap) dst[n] = m;
+                    ++n;
+                }
+                x = i + 1;
+                st = kP3X;
+                break;
+            }
+            ik = ok;
+            ++i;
+            break;
+        default:
+            break;
         }
-        count[r] = n;
     }
 }
 
@@ -217,7 +336,7 @@ __global__ void scan_counts(const int *__restrict__ count, int n, int64_t *__res
     const int per = (n + T - 1) / T;
     const int lo = t * per, hi = min(n, lo + per);
     int64_t s = 0;
-    for (int i = lo; i < hi; ++i) s += count[i];
+    for (int i = lo; i < hi; ++i) s += count[2 * i] + count[2 * i + 1];
     part[t] = s;
     __syncthreads();
     if (t == 0) {
@@ -233,19 +352,38 @@ __global__ void scan_counts(const int *__restrict__ count, int n, int64_t *__res
     int64_t acc = part[t];
     for (int i = lo; i < hi; ++i) {
         out_off[i] = acc;
-        acc += count[i];
+        acc += count[2 * i] + count[2 * i + 1];
     }
 }
 
+// Merges the two sorted parts of each read into the compact output (one block per
+// read): an element's place is its index in its own part plus the number of elements
+// of the other part before it (elements with equal info are equal, so ties may go
+// either way; part 0 goes first).
 __global__ void compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads,
                               const int *__restrict__ count, const int64_t *__restrict__ out_off,
                               DevIntv *__restrict__ out)
 {
     const int64_t base_off = offs[0];
     for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
-        const DevIntv *src = padded + 2 * (offs[r] - base_off) + 32 * (int64_t)r;
+        const int len = (int)(offs[r + 1] - offs[r]);
+        const DevIntv *a = padded + 2 * (offs[r] - base_off) + 32 * (int64_t)r;
+        const DevIntv *b = a + part_cap0(len);
+        const int na = count[2 * r], nb = count[2 * r + 1];
         DevIntv *dst = out + out_off[r];
-        for (int i = threadIdx.x; i < count[r]; i += blockDim.x) dst[i] = src[i];
+        for (int i = threadIdx.x; i < na + nb; i += blockDim.x) {
+            const bool in_a = i < na;
+            const DevIntv v = in_a ? a[i] : b[i - na];
+            const DevIntv *o = in_a ? b : a;
+            int lo = 0, hi = in_a ? nb : na;     // first element of the other part after v
+            while (lo < hi) {
+                const int m = (lo + hi) >> 1;
+                const bool before = in_a ? o[m].info < v.info : o[m].info <= v.info;
+                if (before) lo = m + 1;
+                else hi = m;
+            }
+            dst[(in_a ? i : i - na) + lo] = v;
+        }
     }
 }
 
@@ -272,7 +410,7 @@ __global__ void sa_kernel(DevFM F, const uint64_t *__restrict__ rows, int64_t n,
             const int c = (int)(block_word(b, (int)((xs & 127) >> 4)) >> ((~xs & 15) << 1) & 3);
             // xs and kk differ only when k == primary, handled above, so one block serves both
             const Occ4 o = occ_in_block(b, kk);
-            k = F.L2[c] + o.c[c];
+            k = l2_at(F, c) + (c == 0 ? o.c[0] : c == 1 ? o.c[1] : c == 2 ? o.c[2] : o.c[3]);
         }
         pos[i] = steps + __ldg(F.sa + (k >> F.sa_shift));
     }
@@ -285,15 +423,24 @@ size_t seed_scratch_bytes(int n_threads, int max_len)
     return (size_t)n_threads * 3 * (size_t)(max_len + 2) * sizeof(DevIntv);
 }
 
-// Persistent seeding threads: 4 blocks per SM, fewer when long reads would make
-// the per-thread interval lists exceed ~1 GB of scratch.
-int seed_threads(int n_sm, int max_len)
+// Persistent seeding threads: as many as fit on the GPU at once, no more than the
+// reads need, and fewer when long reads would make the per-thread interval lists
+// exceed ~1 GB of scratch.
+int seed_threads(int n_sm, int max_len, int n_reads)
 {
+    static int resident = 0;
+    if (!resident) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, seed_kernel, kSeedBlock, 0) != cudaSuccess || b < 1) b = 4;
+        resident = b;
+    }
     const size_t per_block = (size_t)kSeedBlock * 3 * (size_t)(max_len + 2) * sizeof(DevIntv);
-    size_t blocks = (size_t)n_sm * 4;
+    size_t blocks = (size_t)n_sm * resident;
+    const size_t want = ((size_t)2 * (n_reads > 0 ? n_reads : 1) + kSeedBlock - 1) / kSeedBlock;   // two items per read
+    if (blocks > want) blocks = want;
     const size_t budget = (size_t)1 << 30;
     if (blocks * per_block > budget) blocks = budget / per_block;
-    if (blocks < (size_t)n_sm) blocks = n_sm;
+    if (blocks < 1) blocks = 1;
     return (int)blocks * kSeedBlock;
 }
 
@@ -314,7 +461,7 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
     o.max_mem_intv = max_mem_intv;
     cudaError_t e = cudaMemsetAsync(d_ctrl, 0, 2 * sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const int blocks = seed_threads(n_sm, max_len) / kSeedBlock;
+    const int blocks = seed_threads(n_sm, max_len, n_reads) / kSeedBlock;
     seed_kernel<<<blocks, kSeedBlock, 0, st>>>(F, o, n_reads, d_seqs, d_offs, (DevIntv *)d_padded, d_count,
                                                (DevIntv *)d_lists, max_len + 2, d_ctrl, d_ctrl + 1);
     scan_counts<<<1, 1024, 0, st>>>(d_count, n_reads, d_out_off);
