@@ -73,8 +73,8 @@ enum SeedState : int {
     kNeedRead, kP1X, kFwd, kFwdEnd, kBwdRound, kBwdEntry, kSmemDone, kP2K, kP3X, kP3Fwd, kFinish, kExit
 };
 
-// Persistent: each thread takes work items from a counter, two per read: item 2r
-// runs passes 1 and 2 of read r, item 2r+1 its pass 3 (independent of the other two).
+// Persistent: each thread takes work items from a counter, two per read: item r
+// runs passes 1 and 2 of read r, item n_reads + r its pass 3 (independent of the other two).
 // out holds, per read r, 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r:
 // the first part_cap0(len) for passes 1-2, the rest (at least len/2 + 8: pass 3 finds
 // at most one seed per min_seed_len + 1 >= 2 bases) for pass 3.  Each part is sorted
@@ -105,8 +105,13 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
     DevIntv *prev = listA, *curr = listB;
     // bwt_seed_strategy1
     int x0 = 0;
+    // values loaded one step ahead, so their latency overlaps the extension in flight:
+    // qi = q[i] (forward phases), qb = q[i] of the next backward round, pn = prev[j]
+    int qi = 4, qb = 4;
+    DevIntv pn;
     ik.x0 = ik.x1 = ik.x2 = ik.info = 0;
     p = ik;
+    pn = ik;
 
     for (;;) {
         // ---- bookkeeping up to the next extension (or the end of the work)
@@ -117,14 +122,16 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
         while (!need && st != kExit) {
             switch (st) {
             case kNeedRead: {
+                // all passes-1-2 items first, then all pass-3 items: the warps that take
+                // them hold items of similar length, so fewer lanes idle behind a long one
                 const int w = atomicAdd(next_read, 1);
                 if (w >= 2 * n_reads) { st = kExit; break; }
-                r = w >> 1;
-                part = w & 1;
+                part = w >= n_reads;
+                r = part ? w - n_reads : w;
                 const int64_t o = offs[r];
                 const int64_t len64 = offs[r + 1] - o;
                 if (len64 < 0 || len64 > list_cap - 2) {    // outside the scratch the launch sized: refuse
-                    count[w] = 0;
+                    count[2 * r + part] = 0;
                     atomicMax(overflow, r + 1);
                     break;
                 }
@@ -134,7 +141,7 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 cap = part ? part_cap1(len) : part_cap0(len);
                 n = 0;
                 if (len < opt.min_seed_len || (part && opt.max_mem_intv <= 0)) {
-                    count[w] = 0;                            // mem_chain returns before seeding (bwamem.c:266)
+                    count[2 * r + part] = 0;                 // mem_chain returns before seeding (bwamem.c:266)
                     break;
                 }
                 x = 0;
@@ -169,11 +176,13 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 ik.info = (uint64_t)(x + 1);
                 n_curr = 0;
                 i = x + 1;
+                qi = i < len ? q[i] : 4;
                 st = kFwd;
                 break;
             case kFwd:
-                if (i < len && q[i] < 4) {
-                    e_ik = ik; e_back = false; e_c = 3 - q[i];
+                if (i < len && qi < 4) {
+                    e_ik = ik; e_back = false; e_c = 3 - qi;
+                    qi = i + 1 < len ? q[i + 1] : 4;         // for the next step
                     need = true;
                     break;
                 }
@@ -187,12 +196,15 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 ret = (int)(uint32_t)prev[0].info;
                 n_mem = 0;
                 i = x - 1;
+                qb = i >= 0 ? q[i] : 4;
                 st = kBwdRound;
                 break;
             case kBwdRound:
-                c = i < 0 ? -1 : (q[i] < 4 ? q[i] : -1);
+                c = i < 0 ? -1 : (qb < 4 ? qb : -1);
+                qb = i - 1 >= 0 ? q[i - 1] : 4;              // for the next round
                 n_curr = 0;
                 j = 0;
+                pn = prev[0];
                 st = kBwdEntry;
                 break;
             case kBwdEntry:
@@ -208,7 +220,8 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                     st = kBwdRound;
                     break;
                 }
-                p = prev[j];
+                p = pn;
+                if (j + 1 < n_prev) pn = prev[j + 1];       // for the next entry
                 if (c >= 0) {
                     e_ik = p; e_back = true; e_c = c;
                     need = true;
@@ -240,12 +253,14 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 ik = set_intv(F, q[x]);
                 x0 = x;
                 i = x + 1;
+                qi = i < len ? q[i] : 4;
                 st = kP3Fwd;
                 break;
             case kP3Fwd:
                 if (i >= len) { x = len; st = kP3X; break; }
-                if (q[i] > 3) { x = i + 1; st = kP3X; break; }
-                e_ik = ik; e_back = false; e_c = 3 - q[i];
+                if (qi > 3) { x = i + 1; st = kP3X; break; }
+                e_ik = ik; e_back = false; e_c = 3 - qi;
+                qi = i + 1 < len ? q[i + 1] : 4;             // for the next step
                 need = true;
                 break;
             case kFinish:
