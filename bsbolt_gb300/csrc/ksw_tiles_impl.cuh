@@ -5,8 +5,14 @@
 #include "ksw_group.cuh"
 #include "ksw_tiles.cuh"
 
+// Shapes up to 18 columns per lane are held to 128 registers (4 blocks = 16 warps per
+// SM): measured on GB300, the extra warps hide the ALU dependency latency better than
+// the registers they cost (a few bytes of spill at C >= 15), 3-18 % faster.  Wider
+// shapes keep their registers.
+constexpr int ksw_min_blocks(int C) { return C <= 18 ? 4 : 1; }
+
 template <int C, int G>
-__global__ void __launch_bounds__(kKswBlock)
+__global__ void __launch_bounds__(kKswBlock, ksw_min_blocks(C))
 ksw_tile_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8_t *__restrict__ seq,
                 const int32_t *__restrict__ order, const int32_t *__restrict__ bin_start, int bin,
                 int *__restrict__ counter, bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
