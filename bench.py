@@ -156,6 +156,87 @@ def cfg0_workload(n_pairs=20000):
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
 
 
+def cfg2_workload(n_pairs=100_000):
+    """configs[2] shapes: 100 Mb reference (4 x 25 Mb, GC 41 %, CpG 1 %, 15 % interspersed
+    repeats of 300 bp - 6 kb families at 2-15 % divergence), directional PE 2x150, insert
+    N(400,50), the configs[0] methylation/conversion/error model.  Cached on disk."""
+    from bsbolt_gb300 import index, synth
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"cfg2_{n_pairs}")
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "ref")
+    if not os.path.exists(prefix + ".sa"):
+        contigs = synth.bs_genome(4, 25_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 2)
+        synth.add_repeats(contigs, 0.15, seed=20261203 + 2)
+        synth.write_fasta(prefix + ".fa", contigs)
+        index.build_index(prefix + ".fa", prefix)
+        r1, r2 = synth.bs_reads_pe(contigs, n_pairs, 150, 400, 50, seed=20261203 + 2)
+        reads = []
+        for a, b in zip(r1, r2):
+            reads.append(synth.bs_convert(a, g2a=False))
+            reads.append(synth.bs_convert(b, g2a=True))
+        offs = np.zeros(len(reads) + 1, np.int64)
+        offs[1:] = np.cumsum([len(r) for r in reads])
+        np.save(os.path.join(d, "reads.npy"), np.concatenate(reads))
+        np.save(os.path.join(d, "offs.npy"), offs)
+    return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
+
+
+def pipeline_cfg2(ctx, batch_pairs=33_333, cpu_pairs=2_000):
+    """Seeds -> regions at configs[2] scale (200 MB BWT, larger than L2) in -K 10M-base
+    batches, against the CPU oracle on a sample."""
+    import oracle
+    from bsbolt_gb300 import _lib, index, seed
+    t0 = time.perf_counter()
+    prefix, reads, offs = cfg2_workload()
+    prep_s = time.perf_counter() - t0
+    n_reads = len(offs) - 1
+    seed.load_index(ctx, prefix)
+    opt = _lib.AlignOpt.bwa_defaults()
+    b = 2 * batch_pairs
+    batches = [(lo, min(n_reads, lo + b)) for lo in range(0, n_reads, b)]
+
+    def sub(lo, hi):
+        return reads[offs[lo]:offs[hi]], offs[lo:hi + 1] - offs[lo]
+    seed.align_regs(ctx, *sub(*batches[0]))                      # warm-up
+    t0 = time.perf_counter()
+    first = None
+    for lo, hi in batches:
+        regs, roff = seed.align_regs(ctx, *sub(lo, hi))
+        if first is None:
+            first = (regs, roff)
+    gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for lo, hi in batches:
+        seed.seed_batch(ctx, *sub(lo, hi))
+    seed_s = time.perf_counter() - t0
+    bi = index.BwaIndex(prefix)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    threads = os.cpu_count() or 1
+    cr, co = sub(0, 2 * cpu_pairs)
+    t0 = time.perf_counter()
+    ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac,
+                            oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000]),
+                            cr, co, n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    regs, roff = first
+    k = int(roff[2 * cpu_pairs])
+    exact = bool(np.array_equal(roff[:2 * cpu_pairs + 1], ref["regs_off"]) and
+                 all(np.array_equal(regs[f][:k], ref["regs"][f]) for f in ("rb", "re", "qb", "qe", "score", "truesc")))
+    n_pairs = n_reads // 2
+    return {
+        "workload": "configs[2] shapes: 100 Mb bisulfite reference (4x25 Mb, 15% interspersed repeats, BWT 200 MB > L2), "
+                    f"{n_pairs} directional PE 2x150 pairs in -K 10M-base batches of {batch_pairs} pairs, BWA defaults",
+        "gpu_read_pairs_per_s": round(n_pairs / gpu_s, 1),
+        "gpu_ms_per_batch": round(gpu_s / len(batches) * 1e3, 3),
+        "gpu_seeding_reads_per_s": round(n_reads / seed_s, 1),
+        "cpu_oracle_read_pairs_per_s": round(cpu_pairs / cpu_s, 1),
+        "cpu_oracle_threads": threads, "cpu_sample_pairs": cpu_pairs,
+        "regions_bit_exact_vs_oracle_on_sample": exact,
+        "workload_prep_s": round(prep_s, 1),
+    }
+
+
 def pipeline_secondary(ctx, steps, rank):
     """Seeds -> chains -> regions for configs[0]-shaped reads, GPU vs the CPU oracle."""
     import oracle
@@ -503,6 +584,13 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             learned = {"error": f"{type(e).__name__}: {e}"}
 
+    cfg2 = None
+    if rank == 0 and args.cfg2:
+        try:
+            cfg2 = pipeline_cfg2(ctx)
+        except Exception as e:   # reported, never hidden
+            cfg2 = {"error": f"{type(e).__name__}: {e}"}
+
     tuned = None
     if rank == 0 and not args.no_autotune:
         try:
@@ -548,6 +636,7 @@ def run_ours(args, ws, rank, local):
             "pipeline": secondary,
             "learned_schedule": learned,
             "autotune": tuned,
+            "pipeline_cfg2": cfg2,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -567,6 +656,8 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true", help="skip the seeds->regions secondary block")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
     ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
+    ap.add_argument("--cfg2", action="store_true",
+                    help="add the configs[2]-scale seed->region block (builds a 100 Mb index: ~2 min the first time)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -180,6 +180,32 @@ def bs_genome(n_contigs: int = 4, contig_len: int = 500_000, gc: float = 0.41,
     return contigs
 
 
+def add_repeats(contigs, frac: float = 0.15, fam_len=(300, 6000), div=(0.02, 0.15), n_families: int = 200,
+                seed: int = 20261203):
+    """Interspersed repeats: copies of `n_families` random families (lengths uniform in
+    fam_len), each copy with its own substitution rate uniform in `div`, written over
+    random positions until about `frac` of every contig is repeat.  In place; returns
+    contigs."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    fams = [rng.integers(0, 4, int(rng.integers(fam_len[0], fam_len[1] + 1))).astype(np.uint8)
+            for _ in range(n_families)]
+    for _, g in contigs:
+        covered, target = 0, int(frac * len(g))
+        while covered < target:
+            f = fams[int(rng.integers(0, n_families))]
+            if len(f) >= len(g):
+                break
+            cp = f.copy()
+            if rng.random() < 0.5:
+                cp = COMP[cp[::-1]]
+            mut = rng.random(len(cp)) < rng.uniform(div[0], div[1])
+            cp[mut] = (cp[mut] + rng.integers(1, 4, int(mut.sum()))) % 4
+            at = int(rng.integers(0, len(g) - len(cp)))
+            g[at:at + len(cp)] = cp
+            covered += len(cp)
+    return contigs
+
+
 def write_fasta(path: str, contigs, width: int = 60) -> None:
     letters = np.frombuffer(b"ACGTN", np.uint8)
     with open(path, "w") as f:
