@@ -15,11 +15,12 @@
 
 size_t seed_scratch_bytes(int n_threads, int max_len);
 size_t seed_padded_entries(int64_t total_bases, int n_reads);
+size_t seed_queue_entries(int64_t total_bases, int n_reads);
 int seed_threads(int n_sm, int max_len, int n_reads);
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
-                        void *d_lists, int *d_ctrl, int n_sm, cudaStream_t st);
+                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int n_sm, cudaStream_t st);
 cudaError_t sa_launch(const DevFM &F, const uint64_t *d_rows, int64_t n, uint64_t *d_pos, int n_sm, cudaStream_t st);
 
 void bsb_index_release(bsb_ctx *ctx)
@@ -202,17 +203,19 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     const size_t padded = seed_padded_entries(total_bases, n_reads) * sizeof(DevIntv);
     if (max_len > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "max_len %d > %d", max_len, BSB_SEED_MAX_LEN);
     const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len, n_reads), max_len);
-    const size_t need = padded + lists + 256 * 4 + sizeof(int) * (2 * (size_t)n_reads + 64);
+    const size_t qn = seed_queue_entries(total_bases, n_reads);
+    const size_t need = padded + lists + 256 * 5 + sizeof(int) * (2 * (size_t)n_reads + 64) + 8 * qn;
     if ((rc = bsb_ensure(ctx, &ctx->seed_scratch, &ctx->seed_scratch_bytes, need, "seed scratch"))) return rc;
     char *s = (char *)ctx->seed_scratch;
     void *d_padded = s;
     void *d_lists = s + ((padded + 255) & ~(size_t)255);
     int *d_count = (int *)((char *)d_lists + ((lists + 255) & ~(size_t)255));
     int *d_ctrl = d_count + ((2 * n_reads + 63) & ~63);     // two counts per read (seed_kernel's two parts)
+    void *d_queue = d_ctrl + 64;                              // pass-2 work items (int2)
     const DevFM F = dev_fm(ctx);
     cudaError_t e = seed_launch(F, opt->min_seed_len, opt->split_factor, opt->split_width, opt->max_mem_intv, n_reads,
                                 d_seqs, d_offs, max_len, d_padded, d_count, d_out_off, d_out, d_lists, d_ctrl,
-                                ctx->n_sm, ctx->stream);
+                                d_queue, (int64_t)qn, ctx->n_sm, ctx->stream);
     ctx->seed_ctrl = d_ctrl;
     return bsb_cuda(ctx, e, "seed launch");
 }

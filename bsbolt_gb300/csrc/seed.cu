@@ -62,7 +62,9 @@ __device__ __forceinline__ DevIntv extend_one(const DevFM &F, const DevIntv &ik,
 //   pass 3  bwt_seed_strategy1 (bwt.c:358-379) from every x;
 // then the read's seeds are sorted by info (equal info = the same substring and so
 // the same interval: no tie rule is needed, and the order seeds are found in does
-// not matter).  bwt_smem1 runs as:
+// not matter -- compact_seeds sorts them).  Pass 2 depends only on pass 1's SMEMs,
+// so it runs as a second launch with one work item per SMEM it re-seeds, in parallel
+// with the other re-seeds instead of after them.  bwt_smem1 runs as:
 //   FWD  extend ik forward from x, pushing ik whenever its size is about to change;
 //        the pushes go down from the top of list A, so read upwards they are the
 //        reference's reversed curr list;
@@ -70,23 +72,33 @@ __device__ __forceinline__ DevIntv extend_one(const DevFM &F, const DevIntv &ik,
 //        q[i]; entries that fail may emit an SMEM (only while nothing has survived
 //        this round), survivors are deduplicated by size into curr.
 enum SeedState : int {
-    kNeedRead, kP1X, kFwd, kFwdEnd, kBwdRound, kBwdEntry, kSmemDone, kP2K, kP3X, kP3Fwd, kFinish, kExit
+    kNeedRead, kP1X, kFwd, kFwdEnd, kBwdRound, kBwdEntry, kSmemDone, kP3X, kP3Fwd, kExit
 };
 
-// Persistent: each thread takes work items from a counter, two per read: item r
-// runs passes 1 and 2 of read r, item n_reads + r its pass 3 (independent of the other two).
+// Launch control words: [0] next item of the first launch, [1] overflow (read + 1),
+// [2] pass-2 items queued, [3] next item of the second launch.
+enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrlWords = 4 };
+
+// Persistent: each thread takes work items from a counter.
+//   mode 0: item r < n_reads runs pass 1 of read r and queues its pass-2 re-seeds;
+//           item n_reads + r runs pass 3 of read r (independent of passes 1-2);
+//   mode 1: item w runs the pass-2 re-seed queue[w] = (read, index of the SMEM).
 // out holds, per read r, 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r:
-// the first part_cap0(len) for passes 1-2, the rest (at least len/2 + 8: pass 3 finds
-// at most one seed per min_seed_len + 1 >= 2 bases) for pass 3.  Each part is sorted
-// by info on its own and counted in count[2r + part]; compact_seeds merges the two.
+// the first part_cap0(len) for passes 1-2 (pass 2 appends with an atomic counter),
+// the rest (at least len/2 + 8: pass 3 finds at most one seed per min_seed_len + 1 >= 2
+// bases) for pass 3; count[2r + part] counts each part.
 __device__ __host__ __forceinline__ int part_cap1(int len) { return len / 2 + 8; }
 __device__ __host__ __forceinline__ int part_cap0(int len) { return 2 * len + 32 - part_cap1(len); }
 
 __global__ void __launch_bounds__(kSeedBlock, 4)
-seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs, const int64_t *__restrict__ offs,
-            DevIntv *__restrict__ out, int *__restrict__ count, DevIntv *__restrict__ scratch, int list_cap,
-            int *__restrict__ next_read, int *__restrict__ overflow)
+seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restrict__ seqs,
+            const int64_t *__restrict__ offs, DevIntv *__restrict__ out, int *__restrict__ count,
+            DevIntv *__restrict__ scratch, int list_cap, int *__restrict__ ctrl, int2 *__restrict__ queue,
+            int queue_cap)
 {
+    int *const next_item = ctrl + (mode ? kCtrlNext2 : kCtrlNext1);
+    int *const overflow = ctrl + kCtrlOverflow;
+    const int n_items = mode ? min(*(volatile int *)(ctrl + kCtrlQueued), queue_cap) : 2 * n_reads;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     DevIntv *const listA = scratch + (size_t)tid * 3 * list_cap;     // forward pushes / curr and prev rounds
     DevIntv *const listB = listA + list_cap;
@@ -95,11 +107,11 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
 
     int st = kNeedRead;
     // read
-    int r = 0, part = 0, len = 0, cap = 0, n = 0, old_n = 0;
+    int r = 0, part = 0, len = 0, cap = 0, n = 0;
     const uint8_t *q = nullptr;
     DevIntv *dst = nullptr;
     // bwt_smem1
-    int pass = 1, x = 0, i = 0, min_intv = 1, n_curr = 0, n_prev = 0, n_mem = 0, j = 0, c = 0, ret = 0, k = 0;
+    int pass = 1, x = 0, i = 0, min_intv = 1, n_curr = 0, n_prev = 0, n_mem = 0, j = 0, c = 0, ret = 0;
     uint64_t last_mem_start = 0, last_x2 = 0;
     DevIntv ik, p;
     DevIntv *prev = listA, *curr = listB;
@@ -122,12 +134,20 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
         while (!need && st != kExit) {
             switch (st) {
             case kNeedRead: {
-                // all passes-1-2 items first, then all pass-3 items: the warps that take
+                // all pass-1 items first, then all pass-3 items: the warps that take
                 // them hold items of similar length, so fewer lanes idle behind a long one
-                const int w = atomicAdd(next_read, 1);
-                if (w >= 2 * n_reads) { st = kExit; break; }
-                part = w >= n_reads;
-                r = part ? w - n_reads : w;
+                const int w = atomicAdd(next_item, 1);
+                if (w >= n_items) { st = kExit; break; }
+                int k = 0;
+                if (mode) {
+                    const int2 it = queue[w];
+                    r = it.x;
+                    k = it.y;
+                    part = 0;
+                } else {
+                    part = w >= n_reads;
+                    r = part ? w - n_reads : w;
+                }
                 const int64_t o = offs[r];
                 const int64_t len64 = offs[r + 1] - o;
                 if (len64 < 0 || len64 > list_cap - 2) {    // outside the scratch the launch sized: refuse
@@ -140,6 +160,14 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 dst = out + 2 * (o - base_off) + 32 * (int64_t)r + (part ? part_cap0(len) : 0);
                 cap = part ? part_cap1(len) : part_cap0(len);
                 n = 0;
+                if (mode) {                                  // re-seed in the middle of a long, rare SMEM
+                    const DevIntv sm = dst[k];
+                    pass = 2;
+                    x = (int)(((sm.info >> 32) + (uint32_t)sm.info) >> 1);
+                    min_intv = (int)sm.x2 + 1;
+                    if (q[x] > 3) break;                     // bwt_smem1 returns at once: no SMEM
+                    goto smem_start;
+                }
                 if (len < opt.min_seed_len || (part && opt.max_mem_intv <= 0)) {
                     count[2 * r + part] = 0;                 // mem_chain returns before seeding (bwamem.c:266)
                     break;
@@ -149,27 +177,27 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 break;
             }
             case kP1X:
-                if (x >= len) {                             // pass 1 done
-                    old_n = n < cap ? n : cap;
-                    k = 0;
-                    st = kP2K;
+                if (x >= len) {                             // pass 1 done: queue the pass-2 re-seeds
+                    if (n > cap) {
+                        atomicMax(overflow, r + 1);
+                        n = cap;
+                    }
+                    for (int t = 0; t < n; ++t) {
+                        const DevIntv sm = dst[t];
+                        const int start = (int)(sm.info >> 32), end = (int)(uint32_t)sm.info;
+                        if (end - start < opt.split_len || sm.x2 > (uint64_t)opt.split_width) continue;
+                        const int slot = atomicAdd(ctrl + kCtrlQueued, 1);
+                        if (slot < queue_cap) queue[slot] = make_int2(r, t);
+                        else atomicMax(overflow, r + 1);
+                    }
+                    count[2 * r] = n;
+                    st = kNeedRead;
                     break;
                 }
                 if (q[x] > 3) { ++x; break; }
                 pass = 1;
                 min_intv = 1;
                 goto smem_start;
-            case kP2K: {
-                if (k >= old_n) { st = kFinish; break; }
-                const DevIntv s = dst[k];
-                const int start = (int)(s.info >> 32), end = (int)(uint32_t)s.info;
-                if (end - start < opt.split_len || s.x2 > (uint64_t)opt.split_width) { ++k; break; }
-                pass = 2;
-                x = (start + end) >> 1;
-                min_intv = (int)s.x2 + 1;
-                if (q[x] > 3) { ++k; break; }               // bwt_smem1 returns at once: no SMEM
-                goto smem_start;
-            }
             smem_start:
                 if (min_intv < 1) min_intv = 1;
                 ik = set_intv(F, q[x]);
@@ -240,15 +268,29 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 for (int t = 0; t < n_mem; ++t) {
                     const DevIntv m = mem[t];
                     if (seed_len(m) >= opt.min_seed_len) {
-                        if (n < cap) dst[n] = m;
-                        ++n;
+                        if (pass == 1) {
+                            if (n < cap) dst[n] = m;
+                            ++n;
+                        } else {                            // re-seeds of one read arrive from many threads
+                            const int slot = atomicAdd(&count[2 * r], 1);
+                            if (slot < cap) dst[slot] = m;
+                            else atomicMax(overflow, r + 1);
+                        }
                     }
                 }
                 if (pass == 1) { x = ret; st = kP1X; }
-                else { ++k; st = kP2K; }
+                else st = kNeedRead;
                 break;
             case kP3X:
-                if (x >= len) { st = kFinish; break; }
+                if (x >= len) {                             // pass 3 done
+                    if (n > cap) {
+                        atomicMax(overflow, r + 1);
+                        n = cap;
+                    }
+                    count[2 * r + 1] = n;
+                    st = kNeedRead;
+                    break;
+                }
                 if (q[x] > 3) { ++x; break; }
                 ik = set_intv(F, q[x]);
                 x0 = x;
@@ -262,24 +304,6 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
                 e_ik = ik; e_back = false; e_c = 3 - qi;
                 qi = i + 1 < len ? q[i + 1] : 4;             // for the next step
                 need = true;
-                break;
-            case kFinish:
-                if (n > cap) {
-                    atomicMax(overflow, r + 1);
-                    n = cap;
-                }
-                // insertion sort by info (ks_introsort with intv_lt, bwamem.c:92-93; equal keys are equal values)
-                for (int a = 1; a < n; ++a) {
-                    const DevIntv v = dst[a];
-                    int b = a - 1;
-                    while (b >= 0 && dst[b].info > v.info) {
-                        dst[b + 1] = dst[b];
-                        --b;
-                    }
-                    dst[b + 1] = v;
-                }
-                count[2 * r + part] = n;
-                st = kNeedRead;
                 break;
             default:
                 st = kExit;
@@ -343,15 +367,30 @@ seed_kernel(DevFM F, SeedOpt opt, int n_reads, const uint8_t *__restrict__ seqs,
     }
 }
 
+// Seeds of read r in the two parts of its padded region (a part that overflowed holds
+// its capacity; the launch reports the overflow).
+__device__ __forceinline__ void part_counts(const int *__restrict__ count, const int64_t *__restrict__ offs, int r,
+                                            int &na, int &nb)
+{
+    const int len = (int)(offs[r + 1] - offs[r]);
+    na = min(count[2 * r], part_cap0(len));
+    nb = min(count[2 * r + 1], part_cap1(len));
+}
+
 // Exclusive scan of per-read counts into out_off[0..n] (single block, chunked).
-__global__ void scan_counts(const int *__restrict__ count, int n, int64_t *__restrict__ out_off)
+__global__ void scan_counts(const int *__restrict__ count, const int64_t *__restrict__ offs, int n,
+                            int64_t *__restrict__ out_off)
 {
     __shared__ int64_t part[1024];
     const int t = threadIdx.x, T = blockDim.x;
     const int per = (n + T - 1) / T;
     const int lo = t * per, hi = min(n, lo + per);
     int64_t s = 0;
-    for (int i = lo; i < hi; ++i) s += count[2 * i] + count[2 * i + 1];
+    for (int i = lo; i < hi; ++i) {
+        int na, nb;
+        part_counts(count, offs, i, na, nb);
+        s += na + nb;
+    }
     part[t] = s;
     __syncthreads();
     if (t == 0) {
@@ -367,37 +406,44 @@ __global__ void scan_counts(const int *__restrict__ count, int n, int64_t *__res
     int64_t acc = part[t];
     for (int i = lo; i < hi; ++i) {
         out_off[i] = acc;
-        acc += count[2 * i] + count[2 * i + 1];
+        int na, nb;
+        part_counts(count, offs, i, na, nb);
+        acc += na + nb;
     }
 }
 
-// Merges the two sorted parts of each read into the compact output (one block per
-// read): an element's place is its index in its own part plus the number of elements
-// of the other part before it (elements with equal info are equal, so ties may go
-// either way; part 0 goes first).
+// Each read's seeds, sorted by info into the compact output (one block per read): an
+// element's place is the number of elements with a smaller info, plus the number of
+// equal ones before it (ks_introsort with intv_lt, bwamem.c:92-93; elements with equal
+// info are equal, so the tie rule cannot show).
+constexpr int kSortStage = 1024;
 __global__ void compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads,
                               const int *__restrict__ count, const int64_t *__restrict__ out_off,
                               DevIntv *__restrict__ out)
 {
+    __shared__ uint64_t key[kSortStage];
     const int64_t base_off = offs[0];
     for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
         const int len = (int)(offs[r + 1] - offs[r]);
         const DevIntv *a = padded + 2 * (offs[r] - base_off) + 32 * (int64_t)r;
         const DevIntv *b = a + part_cap0(len);
-        const int na = count[2 * r], nb = count[2 * r + 1];
+        int na, nb;
+        part_counts(count, offs, r, na, nb);
+        const int m = na + nb;
         DevIntv *dst = out + out_off[r];
-        for (int i = threadIdx.x; i < na + nb; i += blockDim.x) {
-            const bool in_a = i < na;
-            const DevIntv v = in_a ? a[i] : b[i - na];
-            const DevIntv *o = in_a ? b : a;
-            int lo = 0, hi = in_a ? nb : na;     // first element of the other part after v
-            while (lo < hi) {
-                const int m = (lo + hi) >> 1;
-                const bool before = in_a ? o[m].info < v.info : o[m].info <= v.info;
-                if (before) lo = m + 1;
-                else hi = m;
+        const bool staged = m <= kSortStage;
+        __syncthreads();
+        if (staged)
+            for (int i = threadIdx.x; i < m; i += blockDim.x) key[i] = (i < na ? a[i] : b[i - na]).info;
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const DevIntv v = i < na ? a[i] : b[i - na];
+            int rank = 0;
+            for (int j = 0; j < m; ++j) {
+                const uint64_t w = staged ? key[j] : (j < na ? a[j] : b[j - na]).info;
+                rank += w < v.info || (w == v.info && j < i);
             }
-            dst[(in_a ? i : i - na) + lo] = v;
+            dst[rank] = v;
         }
     }
 }
@@ -459,6 +505,10 @@ int seed_threads(int n_sm, int max_len, int n_reads)
     return (int)blocks * kSeedBlock;
 }
 
+// Pass-2 work items a batch can queue: at most one per SMEM of pass 1, i.e. per read
+// position.
+size_t seed_queue_entries(int64_t total_bases, int n_reads) { return (size_t)total_bases + (size_t)n_reads + 64; }
+
 size_t seed_padded_entries(int64_t total_bases, int n_reads)
 {
     return 2 * (size_t)total_bases + 32 * (size_t)n_reads;
@@ -467,19 +517,21 @@ size_t seed_padded_entries(int64_t total_bases, int n_reads)
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
-                        void *d_lists, int *d_ctrl, int n_sm, cudaStream_t st)
+                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int n_sm, cudaStream_t st)
 {
     SeedOpt o;
     o.min_seed_len = min_seed_len;
     o.split_len = (int)(min_seed_len * split_factor + .499);    // bwamem.c:122
     o.split_width = split_width;
     o.max_mem_intv = max_mem_intv;
-    cudaError_t e = cudaMemsetAsync(d_ctrl, 0, 2 * sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(d_ctrl, 0, kCtrlWords * sizeof(int), st);
     if (e != cudaSuccess) return e;
     const int blocks = seed_threads(n_sm, max_len, n_reads) / kSeedBlock;
-    seed_kernel<<<blocks, kSeedBlock, 0, st>>>(F, o, n_reads, d_seqs, d_offs, (DevIntv *)d_padded, d_count,
-                                               (DevIntv *)d_lists, max_len + 2, d_ctrl, d_ctrl + 1);
-    scan_counts<<<1, 1024, 0, st>>>(d_count, n_reads, d_out_off);
+    const int qcap = (int)(queue_cap < 0x7fffffff ? queue_cap : 0x7fffffff);
+    for (int mode = 0; mode < 2; ++mode)        // passes 1 and 3, then the pass-2 re-seeds
+        seed_kernel<<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs, (DevIntv *)d_padded, d_count,
+                                                   (DevIntv *)d_lists, max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+    scan_counts<<<1, 1024, 0, st>>>(d_count, d_offs, n_reads, d_out_off);
     compact_seeds<<<n_sm * 4, 128, 0, st>>>((const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off,
                                             (DevIntv *)d_out);
     return cudaGetLastError();
