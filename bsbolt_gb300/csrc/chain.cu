@@ -579,6 +579,10 @@ __device__ KswResult run_ext(const KswParams &P, int qlen, int tlen, int h0, int
     return ksw_warp<C>(P, qlen, tlen, h0, w, eb, acc, lane);
 }
 
+// The narrowest warp tile (C columns per lane) that holds qlen + 1 columns; a kernel
+// compiled for reads of at most 32 * MaxC - 1 bases only instantiates C <= MaxC, which
+// keeps its register count (and so its occupancy) that of its widest tile.
+template <int MaxC>
 __device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, int w, int eb, const ReadRefAcc &acc,
                                 int lane)
 {
@@ -591,14 +595,23 @@ __device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, 
     case 5: return run_ext<5>(P, qlen, tlen, h0, w, eb, acc, lane);
     case 6: return run_ext<6>(P, qlen, tlen, h0, w, eb, acc, lane);
     case 7: return run_ext<7>(P, qlen, tlen, h0, w, eb, acc, lane);
-    case 8: return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
-    case 9: case 10: case 11: case 12: return run_ext<12>(P, qlen, tlen, h0, w, eb, acc, lane);
-    default: return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
+    default:
+        if constexpr (MaxC <= 8) {
+            return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
+        } else {
+            if (need == 8) return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
+            if (need <= 12) return run_ext<12>(P, qlen, tlen, h0, w, eb, acc, lane);
+            return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
+        }
     }
 }
 
 // One warp per read.  regs: the read's region slots start at its row offset.
-__global__ void __launch_bounds__(128)
+// MaxC = 8 serves reads of up to 255 bases, 16 every read the batch accepts; the
+// narrow variant is held to 3 blocks (12 warps) per SM, which costs it 16 bytes of
+// spill.
+template <int MaxC>
+__global__ void __launch_bounds__(128, MaxC <= 8 ? 3 : 1)
 chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *__restrict__ reads,
                  const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
                  const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
@@ -728,7 +741,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                     for (int i = 0; i < 2; ++i) {
                         const int prev = a.score;
                         aw0 = opt.w << i;
-                        x = extend_any(P, s.qbeg, tlen, s.len * opt.a, aw0, opt.pen_clip5, acc, lane);
+                        x = extend_any<MaxC>(P, s.qbeg, tlen, s.len * opt.a, aw0, opt.pen_clip5, acc, lane);
                         a.score = x.score;
                         if (a.score == prev || x.max_off < (aw0 >> 1) + (aw0 >> 2)) break;
                     }
@@ -749,7 +762,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                     for (int i = 0; i < 2; ++i) {
                         const int prev = a.score;
                         aw1 = opt.w << i;
-                        x = extend_any(P, l_query - qe, tlen, sc0, aw1, opt.pen_clip3, acc, lane);
+                        x = extend_any<MaxC>(P, l_query - qe, tlen, sc0, aw1, opt.pen_clip3, acc, lane);
                         a.score = x.score;
                         if (a.score == prev || x.max_off < (aw1 >> 1) + (aw1 >> 2)) break;
                     }
@@ -812,7 +825,8 @@ static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_reads, const uint8_t *d_reads,
                        const int64_t *d_read_off, const bsb_intv_t *d_seeds, const int64_t *d_seed_off,
-                       int64_t n_seeds, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out, int64_t *n_regs_total)
+                       int64_t n_seeds, int max_len, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out,
+                       int64_t *n_regs_total)
 {
     int rc;
     cudaStream_t st = ctx->stream;
@@ -885,8 +899,12 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     P.mat_max = mx;
     chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
                                                  pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
-    chain2aln_kernel<<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff, cseeds,
-                                                     cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+    if (max_len <= 255)       // every extension of these reads fits 8 columns per lane
+        chain2aln_kernel<8><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+    else
+        chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
+                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
     scan_i32<<<1, 1024, 0, st>>>(n_regs, n_reads, reg_off);
     compact_regs<<<ctx->n_sm * 4, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
     cudaError_t e = cudaGetLastError();
@@ -959,7 +977,7 @@ extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
     if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
     bsb_reg_t *d_regs = nullptr;
     int64_t *d_reg_off = nullptr, n_regs = 0;
-    if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, &d_regs, &d_reg_off,
+    if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, &d_regs, &d_reg_off,
                                  &n_regs)))
         return rc;
     if (n_regs > max_regs)
