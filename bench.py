@@ -132,12 +132,12 @@ def cpu_port_gcups(jobs, seq, n_sample, threads, mat):
     return float(cells.sum()) / dt / 1e9, dt, out, cells
 
 
-def cfg0_workload(n_pairs=20000):
-    """configs[0] shapes: 4 x 500 kb reference (GC 41 %, CpG 1 %), directional PE 2x100,
+def ref2mb_workload(n_pairs=20000):
+    """The 2 Mb-reference workload: 4 x 500 kb reference (GC 41 %, CpG 1 %), directional PE 2x100,
     insert N(300,30), CpG meth 0.8, CH 0.01, 99.5 % conversion, 0.5 % errors; the reads
     converted in silico as bsbolt does (read 1 C->T, read 2 G->A).  Cached on disk."""
     from bsbolt_gb300 import index, synth
-    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"cfg0_{n_pairs}")
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"ref2mb_{n_pairs}")
     os.makedirs(d, exist_ok=True)
     prefix = os.path.join(d, "ref")
     if not os.path.exists(prefix + ".sa"):
@@ -156,12 +156,12 @@ def cfg0_workload(n_pairs=20000):
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
 
 
-def cfg2_workload(n_pairs=100_000):
-    """configs[2] shapes: 100 Mb reference (4 x 25 Mb, GC 41 %, CpG 1 %, 15 % interspersed
+def ref100mb_workload(n_pairs=100_000):
+    """The 100 Mb-reference workload: 4 x 25 Mb reference (GC 41 %, CpG 1 %, 15 % interspersed
     repeats of 300 bp - 6 kb families at 2-15 % divergence), directional PE 2x150, insert
-    N(400,50), the configs[0] methylation/conversion/error model.  Cached on disk."""
+    N(400,50), the 2 Mb workload's methylation/conversion/error model.  Cached on disk."""
     from bsbolt_gb300 import index, synth
-    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"cfg2_{n_pairs}")
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"ref100mb_{n_pairs}")
     os.makedirs(d, exist_ok=True)
     prefix = os.path.join(d, "ref")
     if not os.path.exists(prefix + ".sa"):
@@ -181,13 +181,13 @@ def cfg2_workload(n_pairs=100_000):
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
 
 
-def pipeline_cfg2(ctx, batch_pairs=33_333, cpu_pairs=2_000):
-    """Seeds -> regions at configs[2] scale (200 MB BWT, larger than L2) in -K 10M-base
+def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
+    """Seeds -> regions on the 100 Mb reference (200 MB BWT, larger than L2) in -K 10M-base
     batches, against the CPU oracle on a sample."""
     import oracle
     from bsbolt_gb300 import _lib, index, seed
     t0 = time.perf_counter()
-    prefix, reads, offs = cfg2_workload()
+    prefix, reads, offs = ref100mb_workload()
     prep_s = time.perf_counter() - t0
     n_reads = len(offs) - 1
     seed.load_index(ctx, prefix)
@@ -225,7 +225,7 @@ def pipeline_cfg2(ctx, batch_pairs=33_333, cpu_pairs=2_000):
                  all(np.array_equal(regs[f][:k], ref["regs"][f]) for f in ("rb", "re", "qb", "qe", "score", "truesc")))
     n_pairs = n_reads // 2
     return {
-        "workload": "configs[2] shapes: 100 Mb bisulfite reference (4x25 Mb, 15% interspersed repeats, BWT 200 MB > L2), "
+        "workload": "100 Mb bisulfite reference (4x25 Mb, 15% interspersed repeats, BWT 200 MB > L2), "
                     f"{n_pairs} directional PE 2x150 pairs in -K 10M-base batches of {batch_pairs} pairs, BWA defaults",
         "gpu_read_pairs_per_s": round(n_pairs / gpu_s, 1),
         "gpu_ms_per_batch": round(gpu_s / len(batches) * 1e3, 3),
@@ -238,10 +238,10 @@ def pipeline_cfg2(ctx, batch_pairs=33_333, cpu_pairs=2_000):
 
 
 def pipeline_secondary(ctx, steps, rank):
-    """Seeds -> chains -> regions for configs[0]-shaped reads, GPU vs the CPU oracle."""
+    """Seeds -> chains -> regions on the 2 Mb-reference workload, GPU vs the CPU oracle."""
     import oracle
     from bsbolt_gb300 import _lib, index, seed
-    prefix, reads, offs = cfg0_workload()
+    prefix, reads, offs = ref2mb_workload()
     n_pairs = (len(offs) - 1) // 2
     seed.load_index(ctx, prefix)
     opt = _lib.AlignOpt.bwa_defaults()
@@ -268,7 +268,7 @@ def pipeline_secondary(ctx, steps, rank):
     exact = bool(np.array_equal(roff, ref["regs_off"]) and
                  all(np.array_equal(regs[f], ref["regs"][f]) for f in ("rb", "re", "qb", "qe", "score", "truesc")))
     return {
-        "workload": "configs[0] shapes: 2 Mb bisulfite reference (4x500 kb), 20k directional PE 2x100 pairs, "
+        "workload": "2 Mb bisulfite reference (4x500 kb), 20k directional PE 2x100 pairs, "
                     "BWA defaults, -L 5",
         "stage": "seeds -> SA -> chains -> chain filter -> mem_chain2aln (pre-dedup regions, bsb_align_regs_batch, "
                  "host buffers incl. H2D/D2H)",
@@ -420,7 +420,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(tms)), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded PCG64), BASELINE configs[1] shapes",
+        "data": "synthetic (seeded PCG64): the 4M-job extension workload's shapes",
         "config": {"workload": "batched ksw_extend2, 4M jobs, qlen U[10,140], w=100, BWA default scoring",
                    "sample_jobs_per_step": args.ref_sample, "parallelism": "host threads"},
         "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
@@ -584,12 +584,12 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             learned = {"error": f"{type(e).__name__}: {e}"}
 
-    cfg2 = None
-    if rank == 0 and args.cfg2:
+    big = None
+    if rank == 0 and args.ref100mb:
         try:
-            cfg2 = pipeline_cfg2(ctx)
+            big = pipeline_ref100mb(ctx)
         except Exception as e:   # reported, never hidden
-            cfg2 = {"error": f"{type(e).__name__}: {e}"}
+            big = {"error": f"{type(e).__name__}: {e}"}
 
     tuned = None
     if rank == 0 and not args.no_autotune:
@@ -611,7 +611,7 @@ def run_ours(args, ws, rank, local):
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded PCG64), BASELINE configs[1] shapes",
+            "data": "synthetic (seeded PCG64): the 4M-job extension workload's shapes",
             "config": {"workload": "batched ksw_extend2, 4M jobs, qlen U[10,140], target=query+100nt "
                                    "(1% sub, 0.1% indel, 20% unrelated), h0 U[19,100], w=100, a1 b4 o6 e1 z100 L5",
                        "jobs": n, "cells_per_step": total_cells, "seq_bytes": int(len(seq)),
@@ -636,7 +636,7 @@ def run_ours(args, ws, rank, local):
             "pipeline": secondary,
             "learned_schedule": learned,
             "autotune": tuned,
-            "pipeline_cfg2": cfg2,
+            "pipeline_100mb_ref": big,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -656,8 +656,8 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true", help="skip the seeds->regions secondary block")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
     ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
-    ap.add_argument("--cfg2", action="store_true",
-                    help="add the configs[2]-scale seed->region block (builds a 100 Mb index: ~2 min the first time)")
+    ap.add_argument("--ref100mb", action="store_true",
+                    help="add the 100 Mb-reference seed->region block (builds a 100 Mb index: ~2 min the first time)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
