@@ -1,15 +1,16 @@
 // seed.cu -- SMEM seeding (mem_collect_intv) and suffix-array lookups on sm_103a.
 //
-// One thread carries one read through the three passes of mem_collect_intv
-// (bsbolt/External/BWA/bwamem.c:118-166):
+// mem_collect_intv (bsbolt/External/BWA/bwamem.c:118-166) runs its three passes as
+// independent work items of one persistent kernel (seed_kernel, state machine below):
 //   pass 1  bwt_smem1 from every x (bwt.c:289-356), keep SMEMs >= min_seed_len;
-//   pass 2  re-seed from the middle of SMEMs >= split_len with <= split_width hits;
-//   pass 3  bwt_seed_strategy1 (bwt.c:358-379) from every x.
-// then sorts the read's seeds by info.  Equal info means the same substring
-// and so the same interval, so the sort needs no tie rule.  The interval
-// lists of bwt_smem1 live in a per-thread slice of device scratch (they are
-// short in practice, but a repeat can make them as long as the read).
-// Every occurrence query reads one or two 64-byte BWT blocks (fm_index.cuh).
+//   pass 2  re-seed from the middle of SMEMs >= split_len with <= split_width hits
+//           (a second launch: one item per such SMEM);
+//   pass 3  bwt_seed_strategy1 (bwt.c:358-379) from every x;
+// compact_seeds then sorts each read's seeds by info.  Equal info means the same
+// substring and so the same interval, so the sort needs no tie rule.  The interval
+// lists of bwt_smem1 live in a per-thread slice of device scratch (they are short in
+// practice, but a repeat can make them as long as the read).  Every occurrence query
+// reads one or two 64-byte BWT blocks (fm_index.cuh).
 //
 // bwt_sa (bwt.c:86-96) is one thread per suffix-array row: LF steps until a
 // sampled row, each step one 64-byte block.
