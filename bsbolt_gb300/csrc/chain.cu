@@ -21,6 +21,7 @@
 #include "bsb_internal.cuh"
 #include "fm_index.cuh"
 #include "ksw_core.cuh"
+#include "scan.cuh"
 
 namespace {
 
@@ -131,34 +132,6 @@ __global__ void rows_fill(const DevIntv *__restrict__ seeds, int64_t n, int max_
         const int m = rows_of(seeds[i].x2, max_occ, step);
         uint64_t *dst = rows + roff[i];
         for (int c = 0; c < m; ++c) dst[c] = seeds[i].x0 + (uint64_t)c * step;
-    }
-}
-
-// Exclusive scan of int counts into int64 offsets (one block, chunked per thread).
-__global__ void scan_i32(const int *__restrict__ cnt, int64_t n, int64_t *__restrict__ off)
-{
-    __shared__ int64_t part[1024];
-    const int t = threadIdx.x, T = blockDim.x;
-    const int64_t per = (n + T - 1) / T;
-    const int64_t lo = t * per, hi = min(n, lo + per);
-    int64_t s = 0;
-    for (int64_t i = lo; i < hi; ++i) s += cnt[i];
-    part[t] = s;
-    __syncthreads();
-    if (t == 0) {
-        int64_t acc = 0;
-        for (int i = 0; i < T; ++i) {
-            const int64_t v = part[i];
-            part[i] = acc;
-            acc += v;
-        }
-        off[n] = acc;
-    }
-    __syncthreads();
-    int64_t acc = part[t];
-    for (int64_t i = lo; i < hi; ++i) {
-        off[i] = acc;
-        acc += cnt[i];
     }
 }
 
@@ -825,14 +798,17 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     cudaStream_t st = ctx->stream;
     const int nb = ctx->n_sm * 4;
     // rows per seed interval and their offsets
-    size_t need = al(sizeof(int) * (n_seeds + 1)) + al(sizeof(int64_t) * (n_seeds + 1));
+    const int64_t scan_n = n_seeds > n_reads ? n_seeds : n_reads;
+    size_t need = al(sizeof(int) * (n_seeds + 1)) + al(sizeof(int64_t) * (n_seeds + 1)) +
+                  al(sizeof(int64_t) * scan_tmp_words(scan_n));
     if ((rc = bsb_ensure(ctx, &ctx->arena0, &ctx->arena0_bytes, need, "chain scratch (rows)"))) return rc;
     int *rcnt = (int *)ctx->arena0;
     int64_t *roff = (int64_t *)((char *)ctx->arena0 + al(sizeof(int) * (n_seeds + 1)));
+    int64_t *scan_tmp = (int64_t *)((char *)roff + al(sizeof(int64_t) * (n_seeds + 1)));
     if (n_seeds > 0) {
         rows_count<<<nb, 256, 0, st>>>((const DevIntv *)d_seeds, n_seeds, o->max_occ, rcnt);
     }
-    scan_i32<<<1, 1024, 0, st>>>(rcnt, n_seeds, roff);
+    if ((rc = bsb_cuda(ctx, scan_i32_i64(rcnt, n_seeds, roff, scan_tmp, st), "row offsets"))) return rc;
     int64_t R = 0;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&R, roff + n_seeds, 8, cudaMemcpyDeviceToHost, st), "row total"))) return rc;
     if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "row count"))) return rc;
@@ -898,7 +874,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     else
         chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                              cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
-    scan_i32<<<1, 1024, 0, st>>>(n_regs, n_reads, reg_off);
+    if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
     compact_regs<<<ctx->n_sm * 4, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return bsb_cuda(ctx, e, "chain/extension launch");
