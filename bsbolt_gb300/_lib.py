@@ -33,7 +33,7 @@ EXPORTS = (
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
-    "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms",
+    "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
 )
 
 
@@ -156,6 +156,8 @@ def load(path: str = LIB_PATH):
     L.bsb_get_tile_map.restype = I32
     L.bsb_last_tile_ms.argtypes = [P, P, I32]
     L.bsb_last_tile_ms.restype = I32
+    L.bsb_index_full_sa.argtypes = [P, I32]
+    L.bsb_index_full_sa.restype = I32
     _lib = L
     return L
 

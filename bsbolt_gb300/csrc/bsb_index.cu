@@ -22,12 +22,15 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
                         void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int n_sm, cudaStream_t st);
 cudaError_t sa_launch(const DevFM &F, const uint64_t *d_rows, int64_t n, uint64_t *d_pos, int n_sm, cudaStream_t st);
+cudaError_t sa_full_build(const DevFM &F, int64_t n_sa, uint64_t *full, int *failed, int n_sm, cudaStream_t st);
 
 void bsb_index_release(bsb_ctx *ctx)
 {
     if (ctx->idx_bwt) cudaFree(ctx->idx_bwt);
     if (ctx->idx_sa) cudaFree(ctx->idx_sa);
     if (ctx->idx_pac) cudaFree(ctx->idx_pac);
+    if (ctx->idx_sa_full) cudaFree(ctx->idx_sa_full);
+    ctx->idx_sa_full = nullptr;
     if (ctx->idx_ann_off) cudaFree(ctx->idx_ann_off);
     if (ctx->idx_ann_len) cudaFree(ctx->idx_ann_len);
     ctx->idx_bwt = ctx->idx_sa = ctx->idx_pac = ctx->idx_ann_off = ctx->idx_ann_len = nullptr;
@@ -40,6 +43,7 @@ static DevFM dev_fm(const bsb_ctx *ctx)
     DevFM F;
     F.blk = (const uint4 *)ctx->idx_bwt;
     F.sa = (const uint64_t *)ctx->idx_sa;
+    F.sa_full = (const uint64_t *)ctx->idx_sa_full;
     F.primary = ctx->primary;
     F.seq_len = ctx->seq_len;
     for (int i = 0; i < 5; ++i) F.L2[i] = ctx->L2[i];
@@ -47,6 +51,47 @@ static DevFM dev_fm(const bsb_ctx *ctx)
     while ((1 << sh) < ctx->sa_intv) ++sh;
     F.sa_shift = sh;
     return F;
+}
+
+// The full suffix array, resident in HBM (8 bytes per row: 3.2 GB for a 100 Mb
+// bisulfite reference), turns every bwt_sa into one load.  Built from the sampled one
+// on the device; when it does not fit, bwt_sa keeps its LF walk.
+static int build_sa_full(bsb_ctx *ctx)
+{
+    if (ctx->idx_sa_full) return 0;
+    void *full = nullptr;
+    int *failed = nullptr;
+    if (cudaMalloc(&full, 8 * (ctx->seq_len + 1)) == cudaSuccess && cudaMalloc((void **)&failed, sizeof(int)) == cudaSuccess) {
+        int h_failed = 1;
+        if (cudaMemsetAsync(failed, 0, sizeof(int), ctx->stream) == cudaSuccess &&
+            sa_full_build(dev_fm(ctx), (int64_t)ctx->n_sa, (uint64_t *)full, failed, ctx->n_sm, ctx->stream) == cudaSuccess &&
+            cudaMemcpyAsync(&h_failed, failed, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+            cudaStreamSynchronize(ctx->stream) == cudaSuccess && !h_failed) {
+            ctx->idx_sa_full = full;
+            full = nullptr;
+        }
+    }
+    if (full) cudaFree(full);
+    if (failed) cudaFree(failed);
+    cudaGetLastError();           // an allocation that did not fit is not an error
+    return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "full suffix array");
+}
+
+extern "C" int bsb_index_full_sa(bsb_ctx *ctx, int enable)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice")) ||
+        (rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize")))
+        return rc;
+    if (!enable) {
+        if (ctx->idx_sa_full) cudaFree(ctx->idx_sa_full);
+        ctx->idx_sa_full = nullptr;
+        return 0;
+    }
+    if ((rc = build_sa_full(ctx))) return rc;
+    return ctx->idx_sa_full ? 0 : bsb_fail(ctx, BSB_ENOMEM, "the full suffix array does not fit in device memory");
 }
 
 extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
@@ -101,6 +146,7 @@ extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
     ctx->n_sa = v->n_sa;
     ctx->l_pac = v->l_pac;
     if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "index upload"))) return rc;
+    if ((rc = build_sa_full(ctx))) return rc;
     ctx->has_index = 1;
     return 0;
 }

@@ -46,6 +46,7 @@ struct bsb_ctx {
     // device-resident FM-index (reference layout) and its scalars
     int has_index = 0;
     void *idx_bwt = nullptr, *idx_sa = nullptr, *idx_pac = nullptr;
+    void *idx_sa_full = nullptr;  // every row's SA value (built at upload when it fits), or NULL
     uint64_t primary = 0, seq_len = 0, n_sa = 0;
     uint64_t L2[5] = {0, 0, 0, 0, 0};
     int sa_intv = 0;

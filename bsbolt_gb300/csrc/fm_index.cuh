@@ -12,6 +12,7 @@
 struct DevFM {
     const uint4 *blk;        // 64-byte occurrence blocks
     const uint64_t *sa;      // sampled suffix array, sa[0] = (uint64_t)-1
+    const uint64_t *sa_full; // every row's bwt_sa value (seq_len + 1 entries), or NULL
     uint64_t primary;
     uint64_t seq_len;
     uint64_t L2[5];
@@ -30,6 +31,10 @@ struct Occ4 {
 struct Block {
     uint4 w[4];
 };
+
+// One LF step of bwt_sa (bwt_invPsi, bwt.c:53-59): the row of the suffix one text
+// position earlier; the primary row steps to row 0 (BWA's "$" convention).
+__device__ __forceinline__ uint64_t lf_step(const DevFM &F, uint64_t k);
 
 __device__ __forceinline__ Block load_block(const DevFM &F, uint64_t kk)
 {
@@ -124,4 +129,16 @@ __device__ __forceinline__ DevIntv set_intv(const DevFM &F, int c)   // bwt.h:80
     r.x1 = l2_at(F, 3 - c) + 1;
     r.info = 0;
     return r;
+}
+
+__device__ __forceinline__ uint64_t lf_step(const DevFM &F, uint64_t k)
+{
+    if (k == F.primary) return 0;
+    const uint64_t kk = k - (k >= F.primary);
+    const Block b = load_block(F, kk);
+    const uint64_t xs = k - (k > F.primary);        // symbol row (bwt_invPsi uses >, bwt.c:55)
+    const int c = (int)(block_word(b, (int)((xs & 127) >> 4)) >> ((~xs & 15) << 1) & 3);
+    // xs and kk differ only when k == primary, handled above, so one block serves both
+    const Occ4 o = occ_in_block(b, kk);
+    return l2_at(F, c) + (c == 0 ? o.c[0] : c == 1 ? o.c[1] : c == 2 ? o.c[2] : o.c[3]);
 }

@@ -449,8 +449,14 @@ __global__ void compact_seeds(const DevIntv *__restrict__ padded, const int64_t 
     }
 }
 
-// bwt_sa: LF-walk to the nearest sampled row (bwt.c:53-59, 86-96).
-// Rows beyond seq_len are answered with (uint64_t)-2 and never walked.
+// Longest LF walk between sampled rows accepted: a valid index needs a few hundred
+// steps at most (rows are sampled every sa_intv by row number); a corrupt one must not
+// loop forever.
+constexpr uint64_t kMaxWalk = 1ull << 20;
+
+// bwt_sa: LF-walk to the nearest sampled row (bwt.c:53-59, 86-96), or one load when
+// the full suffix array is resident.  Rows beyond seq_len are answered with
+// (uint64_t)-2 and never walked; a walk longer than kMaxWalk with (uint64_t)-3.
 __global__ void sa_kernel(DevFM F, const uint64_t *__restrict__ rows, int64_t n, uint64_t *__restrict__ pos)
 {
     const uint64_t mask = (1ull << F.sa_shift) - 1;
@@ -460,21 +466,41 @@ __global__ void sa_kernel(DevFM F, const uint64_t *__restrict__ rows, int64_t n,
             pos[i] = ~(uint64_t)1;
             continue;
         }
-        while (k & mask) {
-            ++steps;
-            if (k == F.primary) {
-                k = 0;
-                continue;
-            }
-            const uint64_t kk = k - (k >= F.primary);
-            const Block b = load_block(F, kk);
-            const uint64_t xs = k - (k > F.primary);    // symbol row (bwt_invPsi uses >, bwt.c:55)
-            const int c = (int)(block_word(b, (int)((xs & 127) >> 4)) >> ((~xs & 15) << 1) & 3);
-            // xs and kk differ only when k == primary, handled above, so one block serves both
-            const Occ4 o = occ_in_block(b, kk);
-            k = l2_at(F, c) + (c == 0 ? o.c[0] : c == 1 ? o.c[1] : c == 2 ? o.c[2] : o.c[3]);
+        if (F.sa_full) {
+            pos[i] = __ldg(F.sa_full + k);
+            continue;
         }
-        pos[i] = steps + __ldg(F.sa + (k >> F.sa_shift));
+        while ((k & mask) && steps < kMaxWalk) {
+            ++steps;
+            k = lf_step(F, k);
+        }
+        pos[i] = (k & mask) ? ~(uint64_t)2 : steps + __ldg(F.sa + (k >> F.sa_shift));
+    }
+}
+
+// The full suffix array from the sampled one: sampled row s holds its sample, and the
+// rows LF(s), LF^2(s), ... up to the next sampled row hold sa(s) - 1, sa(s) - 2, ...
+// (bwt_sa's own walk, read backwards: every row's walk ends at the sampled row this
+// fill starts from, so each row gets the value bwt_sa gives it).  Row 0 answers BWA's
+// sample, (uint64_t)-1; the rows after it count down from seq_len.
+__global__ void sa_fill_kernel(DevFM F, int64_t n_sa, uint64_t *__restrict__ full, int *__restrict__ failed)
+{
+    const uint64_t mask = (1ull << F.sa_shift) - 1;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_sa; t += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = (uint64_t)t << F.sa_shift;
+        if (s > F.seq_len) continue;
+        const uint64_t sv = F.sa[t];
+        full[s] = sv;
+        uint64_t v = s == 0 ? F.seq_len : sv, k = s;
+        for (uint64_t step = 0;; ++step) {
+            if (step >= kMaxWalk) {                      // not a valid index: the walk is kept
+                atomicExch(failed, 1);
+                break;
+            }
+            k = lf_step(F, k);
+            if (!(k & mask)) break;                     // the next sampled row starts its own run
+            full[k] = --v;
+        }
     }
 }
 
@@ -535,6 +561,14 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
     scan_counts<<<1, 1024, 0, st>>>(d_count, d_offs, n_reads, d_out_off);
     compact_seeds<<<n_sm * 4, 128, 0, st>>>((const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off,
                                             (DevIntv *)d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t sa_full_build(const DevFM &F, int64_t n_sa, uint64_t *full, int *failed, int n_sm, cudaStream_t st)
+{
+    const int64_t want = (n_sa + 255) / 256;
+    const int blocks = (int)(want < (int64_t)n_sm * 32 ? want : (int64_t)n_sm * 32);
+    sa_fill_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(F, n_sa, full, failed);
     return cudaGetLastError();
 }
 

@@ -168,6 +168,13 @@ int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *view);
  * bwt.c:420-457) and uploads them.  BSB_EIO on a missing or short file. */
 int bsb_index_load(bsb_ctx *ctx, const char *prefix);
 
+/* Full suffix array (no counterpart in the reference).  An uploaded index also gets
+ * every row's SA value in device memory (8 bytes per row), built from the sampled SA,
+ * so each bwt_sa is one load instead of an LF walk; results are identical.  When it
+ * does not fit, lookups walk as the reference does.  enable = 0 frees it (lookups
+ * walk); 1 builds it again (BSB_ENOMEM when it does not fit). */
+int bsb_index_full_sa(bsb_ctx *ctx, int enable);
+
 /* ---- SMEM seeding: mem_collect_intv ------------------------------------- */
 
 /* The seeding fields of mem_opt_t (bwamem.h:33-40). */

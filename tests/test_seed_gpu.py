@@ -70,16 +70,20 @@ def test_seeds_random_reads_vs_oracle(ctx_idx, idx):
     assert np.array_equal(got, exp)
 
 
-def test_sa_lookup_vs_suffix_array(ctx_idx, idx):
+@pytest.mark.parametrize("resident", [True, False], ids=["full-sa", "lf-walk"])
+def test_sa_lookup_vs_suffix_array(ctx_idx, idx, resident):
+    """Every row, with the full suffix array resident and with the reference's LF walk."""
     bi = index.BwaIndex(idx)
     pac = bi.pac_codes()
     text = np.concatenate([pac, 3 - pac[::-1]]).astype(np.uint8)
     full = index.suffix_array(text).astype(np.int64)
-    rng = np.random.Generator(np.random.PCG64(5))
-    rows = np.concatenate([np.arange(0, 200), rng.integers(0, len(full), 200000)]).astype(np.uint64)
-    got = seed.sa_batch(ctx_idx, rows).astype(np.int64)
-    exp = full[rows.astype(np.int64)]
-    exp = np.where(exp == len(text), -1, exp)
+    rows = np.arange(0, len(full)).astype(np.uint64)
+    _lib.check(ctx_idx.handle, ctx_idx.L.bsb_index_full_sa(ctx_idx.handle, int(resident)))
+    try:
+        got = seed.sa_batch(ctx_idx, rows).astype(np.int64)
+    finally:
+        _lib.check(ctx_idx.handle, ctx_idx.L.bsb_index_full_sa(ctx_idx.handle, 1))
+    exp = np.where(full == len(text), -1, full)
     assert np.array_equal(got, exp)
 
 
