@@ -565,7 +565,7 @@ __device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, 
     // reference with repeats and 2x150 reads, and by 2 % on a 2 Mb one with 2x100).
     const int need = (qlen + 32) >> 5;
     if constexpr (MaxC <= 8) {
-        return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
+        return run_ext<MaxC>(P, qlen, tlen, h0, w, eb, acc, lane);
     } else {
         if (need <= 8) return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
         return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
@@ -573,11 +573,11 @@ __device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, 
 }
 
 // One warp per read.  regs: the read's region slots start at its row offset.
-// MaxC = 8 serves reads of up to 255 bases, 16 every read the batch accepts; the
-// narrow variant is held to 3 blocks (12 warps) per SM, which costs it 16 bytes of
-// spill.
+// MaxC = 4, 5, 8 serve batches whose reads are at most 127, 159, 255 bases long (one DP
+// copy of that width), 16 every read the batch accepts; the 4- and 5-column variants are
+// held to 4 blocks (16 warps) per SM, the 8-column one to 3.
 template <int MaxC>
-__global__ void __launch_bounds__(128, MaxC <= 8 ? 3 : 1)
+__global__ void __launch_bounds__(128, MaxC <= 5 ? 4 : MaxC <= 8 ? 3 : 1)
 chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *__restrict__ reads,
                  const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
                  const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
@@ -868,7 +868,14 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     P.mat_max = mx;
     chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
                                                  pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
-    if (max_len <= 255)       // every extension of these reads fits 8 columns per lane
+    // every extension of these reads fits (max_len + 1) columns: the narrowest variant that holds them
+    if (max_len <= 127)
+        chain2aln_kernel<4><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+    else if (max_len <= 159)
+        chain2aln_kernel<5><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+    else if (max_len <= 255)
         chain2aln_kernel<8><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
     else

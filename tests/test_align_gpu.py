@@ -51,16 +51,19 @@ def test_regions_match_reference(gpu_ctx, indexes, fn, tag):
     assert np.array_equal(regs["frac_rep"].view(np.int32), gr[:, 10].astype(np.int32))
 
 
-def test_regions_random_reads_vs_oracle(gpu_ctx, indexes):
-    """Reads of every length 0..300 with errors and N runs, both strands, repeats."""
+@pytest.mark.parametrize("lmin,lmax", [(0, 127), (128, 159), (160, 255), (0, 300)],
+                         ids=["up-to-127", "128-159", "160-255", "up-to-300"])
+def test_regions_random_reads_vs_oracle(gpu_ctx, indexes, lmin, lmax):
+    """Reads with errors and N runs, both strands, repeats; each length band runs a
+    different chain-extension kernel variant (the batch's longest read picks it)."""
     prefix = indexes["rep"]
     seed.load_index(gpu_ctx, prefix)
     bi = index.BwaIndex(prefix)
     pac = bi.pac_codes()
-    rng = np.random.Generator(np.random.PCG64(17))
+    rng = np.random.Generator(np.random.PCG64(17 + lmin))
     reads = []
-    for k in range(2500):
-        L = int(rng.integers(0, 301))
+    for k in range(2500 if lmax == 300 else 1200):
+        L = int(rng.integers(lmin, lmax + 1))
         st = int(rng.integers(0, len(pac) - L - 1))
         r = pac[st:st + L].copy()
         if k % 2:
