@@ -1,11 +1,13 @@
 // bsb_index.cu -- device-resident FM-index and the seeding / SA-lookup entry points.
 //
-// The index arrays are uploaded once per context in the reference's own
-// layout (64-byte occurrence blocks, uint64 sampled SA, 2-bit pac), so the
-// BWA driver can hand over what bwa_idx_load already read (bwa.c:363-524)
-// or the library can read the files itself (bwt_restore_bwt / bwt_restore_sa,
-// bwt.c:420-457).
+// The index arrays are taken once per context in the reference's own layout
+// (64-byte occurrence blocks, uint64 sampled SA, 2-bit pac), so the BWA driver
+// can hand over what bwa_idx_load already read (bwa.c:363-524) or the library
+// can read the files itself (bwt_restore_bwt / bwt_restore_sa, bwt.c:420-457).
+// On the device the occurrence array is re-cut into 32-symbol sectors
+// (fm_index.cuh); the SA and pac stay as they are.
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -94,6 +96,23 @@ extern "C" int bsb_index_full_sa(bsb_ctx *ctx, int enable)
     return ctx->idx_sa_full ? 0 : bsb_fail(ctx, BSB_ENOMEM, "the full suffix array does not fit in device memory");
 }
 
+// Re-cuts the reference's occurrence array (64-byte blocks of 128 symbols: four uint64
+// counts, eight symbol words) into the 32-byte sectors occ_at reads; one thread per sector.
+__global__ void occ_sectors_kernel(const uint32_t *__restrict__ ref, uint64_t n_sectors, uint4 *__restrict__ out)
+{
+    const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (s >= n_sectors) return;
+    const uint32_t *b = ref + (s >> 2) * 16;
+    const int q = (int)(s & 3);
+    uint32_t a = 0, c = 0, g = 0;
+    for (int w = 0; w < 2 * q; ++w) word_counts(b[8 + w], 16, a, c, g);
+    const uint64_t ca = ((uint64_t)b[1] << 32 | b[0]) + a;
+    const uint64_t cc = ((uint64_t)b[3] << 32 | b[2]) + c;
+    const uint64_t cg = ((uint64_t)b[5] << 32 | b[4]) + g;
+    out[2 * s] = make_uint4((uint32_t)ca, (uint32_t)(ca >> 32), (uint32_t)cc, (uint32_t)(cc >> 32));
+    out[2 * s + 1] = make_uint4((uint32_t)cg, (uint32_t)(cg >> 32), b[8 + 2 * q], b[9 + 2 * q]);
+}
+
 extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
 {
     if (!ctx) return BSB_EINVAL;
@@ -110,13 +129,26 @@ extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
     int rc;
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     bsb_index_release(ctx);
-    // the occurrence array is padded to whole 64-byte blocks so every block load stays inside it
-    const size_t bwt_bytes = n_blocks * 64;
-    if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_bwt, bwt_bytes), "index: occurrence array"))) return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ctx->idx_bwt, 0, bwt_bytes, ctx->stream), "index memset"))) return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_bwt, v->bwt, v->bwt_size * 4, cudaMemcpyHostToDevice, ctx->stream),
-                       "index: occurrence upload")))
-        return rc;
+    {
+        // the reference blocks go to a zero-padded staging buffer of whole blocks, then are re-cut
+        // into sectors (four per block, one extra block of padding past the last symbol)
+        const size_t ref_bytes = n_blocks * 64, copy = std::min<size_t>(v->bwt_size * 4, ref_bytes);
+        const uint64_t n_sectors = n_blocks * 4;
+        void *stage = nullptr;
+        if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_bwt, n_sectors * 32), "index: occurrence array"))) return rc;
+        if ((rc = bsb_cuda(ctx, cudaMalloc(&stage, ref_bytes), "index: occurrence staging"))) return rc;
+        rc = bsb_cuda(ctx, cudaMemsetAsync(stage, 0, ref_bytes, ctx->stream), "index memset");
+        if (!rc) rc = bsb_cuda(ctx, cudaMemcpyAsync(stage, v->bwt, copy, cudaMemcpyHostToDevice, ctx->stream),
+                               "index: occurrence upload");
+        if (!rc) {
+            occ_sectors_kernel<<<(unsigned)((n_sectors + 255) / 256), 256, 0, ctx->stream>>>(
+                (const uint32_t *)stage, n_sectors, (uint4 *)ctx->idx_bwt);
+            rc = bsb_cuda(ctx, cudaGetLastError(), "index: occurrence sectors");
+        }
+        if (!rc) rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "index: occurrence sectors");
+        cudaFree(stage);
+        if (rc) return rc;
+    }
     if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_sa, v->n_sa * 8), "index: suffix array"))) return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_sa, v->sa, v->n_sa * 8, cudaMemcpyHostToDevice, ctx->stream),
                        "index: SA upload")))
