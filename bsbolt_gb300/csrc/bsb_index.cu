@@ -14,6 +14,7 @@
 
 #include "bsb_internal.cuh"
 #include "fm_index.cuh"
+#include "scan.cuh"
 
 size_t seed_scratch_bytes(int n_threads, int max_len);
 size_t seed_padded_entries(int64_t total_bases, int n_reads);
@@ -22,7 +23,8 @@ int seed_threads(int n_sm, int max_len, int n_reads);
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
-                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int n_sm, cudaStream_t st);
+                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int *d_tot,
+                        int64_t *d_scan_tmp, int n_sm, cudaStream_t st);
 cudaError_t sa_launch(const DevFM &F, const uint64_t *d_rows, int64_t n, uint64_t *d_pos, int n_sm, cudaStream_t st);
 cudaError_t sa_full_build(const DevFM &F, int64_t n_sa, uint64_t *full, int *failed, int n_sm, cudaStream_t st);
 
@@ -282,7 +284,9 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     if (max_len > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "max_len %d > %d", max_len, BSB_SEED_MAX_LEN);
     const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len, n_reads), max_len);
     const size_t qn = seed_queue_entries(total_bases, n_reads);
-    const size_t need = padded + lists + 256 * 5 + sizeof(int) * (2 * (size_t)n_reads + 64) + 8 * qn;
+    const size_t tot_b = (sizeof(int) * (size_t)n_reads + 255) & ~(size_t)255;
+    const size_t need = padded + lists + 256 * 6 + sizeof(int) * (2 * (size_t)n_reads + 64) + 8 * qn + tot_b +
+                        sizeof(int64_t) * (size_t)scan_tmp_words(n_reads);
     if ((rc = bsb_ensure(ctx, &ctx->seed_scratch, &ctx->seed_scratch_bytes, need, "seed scratch"))) return rc;
     char *s = (char *)ctx->seed_scratch;
     void *d_padded = s;
@@ -290,10 +294,12 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     int *d_count = (int *)((char *)d_lists + ((lists + 255) & ~(size_t)255));
     int *d_ctrl = d_count + ((2 * n_reads + 63) & ~63);     // two counts per read (seed_kernel's two parts)
     void *d_queue = d_ctrl + 64;                              // pass-2 work items (int2)
+    int *d_tot = (int *)((char *)d_queue + ((8 * qn + 255) & ~(size_t)255));     // seeds kept per read
+    int64_t *d_scan_tmp = (int64_t *)((char *)d_tot + tot_b);
     const DevFM F = dev_fm(ctx);
     cudaError_t e = seed_launch(F, opt->min_seed_len, opt->split_factor, opt->split_width, opt->max_mem_intv, n_reads,
                                 d_seqs, d_offs, max_len, d_padded, d_count, d_out_off, d_out, d_lists, d_ctrl,
-                                d_queue, (int64_t)qn, ctx->n_sm, ctx->stream);
+                                d_queue, (int64_t)qn, d_tot, d_scan_tmp, ctx->n_sm, ctx->stream);
     ctx->seed_ctrl = d_ctrl;
     return bsb_cuda(ctx, e, "seed launch");
 }

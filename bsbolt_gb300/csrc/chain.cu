@@ -909,14 +909,19 @@ extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
         return 0;
     }
     int max_len = 0;
+    signed char sw_filter[BSB_ALIGN_MAX_LEN + 1];        // per length: -1 not yet known, 0 / 1
+    memset(sw_filter, -1, sizeof sw_filter);
     for (int r = 0; r < n_reads; ++r) {
         const int64_t l = offs[r + 1] - offs[r];
         if (l < 0) return bsb_fail(ctx, BSB_EINVAL, "read %d: negative length", r);
         if (l > BSB_ALIGN_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld > %d", r, (long long)l, BSB_ALIGN_MAX_LEN);
         // mem_flt_chained_seeds (bwamem.c:604-606) runs its seed-level SW only past this
         // point; reads shorter than min_seed_len never have chains (bwamem.c:266)
-        const double min_l = o->min_chain_weight ? 1.1f * o->min_chain_weight : 5.5f * log((double)l);
-        if (l >= o->min_seed_len && !(min_l > 0.05f * l))
+        if (sw_filter[l] < 0) {
+            const double min_l = o->min_chain_weight ? 1.1f * o->min_chain_weight : 5.5f * log((double)l);
+            sw_filter[l] = l >= o->min_seed_len && !(min_l > 0.05f * l);
+        }
+        if (sw_filter[l])
             return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld needs the seed-level SW filter", r, (long long)l);
         if (l > max_len) max_len = (int)l;
     }

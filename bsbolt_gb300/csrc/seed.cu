@@ -10,13 +10,15 @@
 // substring and so the same interval, so the sort needs no tie rule.  The interval
 // lists of bwt_smem1 live in a per-thread slice of device scratch (they are short in
 // practice, but a repeat can make them as long as the read).  Every occurrence query
-// reads one or two 64-byte BWT blocks (fm_index.cuh).
+// reads one 32-byte sector of the occurrence array (fm_index.cuh).
 //
-// bwt_sa (bwt.c:86-96) is one thread per suffix-array row: LF steps until a
-// sampled row, each step one 64-byte block.
+// bwt_sa (bwt.c:86-96) is one thread per suffix-array row: one load from the full
+// suffix array when it is resident, else LF steps until a sampled row, each step
+// one 32-byte sector.
 
 #include "bsb_internal.cuh"
 #include "fm_index.cuh"
+#include "scan.cuh"
 
 namespace {
 
@@ -378,38 +380,14 @@ __device__ __forceinline__ void part_counts(const int *__restrict__ count, const
     nb = min(count[2 * r + 1], part_cap1(len));
 }
 
-// Exclusive scan of per-read counts into out_off[0..n] (single block, chunked).
-__global__ void scan_counts(const int *__restrict__ count, const int64_t *__restrict__ offs, int n,
-                            int64_t *__restrict__ out_off)
+// Seeds each read keeps (both parts, clamped to their caps), for the offset scan.
+__global__ void read_totals(const int *__restrict__ count, const int64_t *__restrict__ offs, int n,
+                            int *__restrict__ tot)
 {
-    __shared__ int64_t part[1024];
-    const int t = threadIdx.x, T = blockDim.x;
-    const int per = (n + T - 1) / T;
-    const int lo = t * per, hi = min(n, lo + per);
-    int64_t s = 0;
-    for (int i = lo; i < hi; ++i) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int na, nb;
-        part_counts(count, offs, i, na, nb);
-        s += na + nb;
-    }
-    part[t] = s;
-    __syncthreads();
-    if (t == 0) {
-        int64_t acc = 0;
-        for (int i = 0; i < T; ++i) {
-            const int64_t v = part[i];
-            part[i] = acc;
-            acc += v;
-        }
-        out_off[n] = acc;
-    }
-    __syncthreads();
-    int64_t acc = part[t];
-    for (int i = lo; i < hi; ++i) {
-        out_off[i] = acc;
-        int na, nb;
-        part_counts(count, offs, i, na, nb);
-        acc += na + nb;
+        part_counts(count, offs, r, na, nb);
+        tot[r] = na + nb;
     }
 }
 
@@ -544,7 +522,8 @@ size_t seed_padded_entries(int64_t total_bases, int n_reads)
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
-                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int n_sm, cudaStream_t st)
+                        void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int *d_tot,
+                        int64_t *d_scan_tmp, int n_sm, cudaStream_t st)
 {
     SeedOpt o;
     o.min_seed_len = min_seed_len;
@@ -558,7 +537,9 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
     for (int mode = 0; mode < 2; ++mode)        // passes 1 and 3, then the pass-2 re-seeds
         seed_kernel<<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs, (DevIntv *)d_padded, d_count,
                                                    (DevIntv *)d_lists, max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
-    scan_counts<<<1, 1024, 0, st>>>(d_count, d_offs, n_reads, d_out_off);
+    read_totals<<<n_sm * 4, 256, 0, st>>>(d_count, d_offs, n_reads, d_tot);
+    e = scan_i32_i64(d_tot, n_reads, d_out_off, d_scan_tmp, st);
+    if (e != cudaSuccess) return e;
     compact_seeds<<<n_sm * 4, 128, 0, st>>>((const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off,
                                             (DevIntv *)d_out);
     return cudaGetLastError();

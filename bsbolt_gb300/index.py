@@ -91,6 +91,9 @@ class BwaIndex:
         self.crick_l = next((a.offset for a in self.anns if a.is_crick), 0)
         raw = np.fromfile(prefix + ".pac", np.uint8)
         self.pac = raw[: (self.l_pac + 3) // 4].copy()
+        # the original (unconverted) bases in the same layout: the methylation calls' reference
+        self.opac = (np.fromfile(prefix + ".opac", np.uint8)[: (self.l_pac + 3) // 4].copy()
+                     if os.path.exists(prefix + ".opac") else None)
 
     def pac_codes(self) -> np.ndarray:
         """The forward pac (Watson C->T then Crick G->A) as one code per base."""

@@ -63,8 +63,13 @@ def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.Alig
     opt = opt or _lib.AlignOpt.bwa_defaults()
     n = len(offs) - 1
     cap = int(offs[-1] - offs[0]) * 4 + 64 * max(n, 1)
-    regs = np.zeros(cap, REG_DTYPE)
-    regs_off = np.zeros(n + 1, np.int64)
+    # the worst-case region buffer is large and mostly unused: keep one per context and
+    # hand back a copy of the part the call filled
+    regs = getattr(ctx, "_regs_buf", None)
+    if regs is None or len(regs) < cap:
+        regs = np.empty(cap, REG_DTYPE)
+        ctx._regs_buf = regs
+    regs_off = np.empty(n + 1, np.int64)
     rc = ctx.L.bsb_align_regs_batch(ctx.handle, ctypes.byref(opt), n, _ptr(seqs) if len(seqs) else None,
                                     _ptr(offs), _ptr(regs), cap, _ptr(regs_off))
     _lib.check(ctx.handle, rc)

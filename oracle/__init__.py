@@ -21,8 +21,8 @@ _SO = os.path.join(_HERE, "_build", "liborc.so")
 _lib = None
 
 
-_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c")
-_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h")
+_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c", "bsb_oracle_cigar.c")
+_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h", "bsb_oracle_cigar.h")
 
 
 def build(force: bool = False) -> str:
@@ -55,6 +55,10 @@ def lib():
         L.orc_collect_intv_batch.argtypes = [P, P, ctypes.c_int, P, P, P, ctypes.c_int64, P,
                                              ctypes.c_int]
         L.orc_bwt_sa_batch.restype = None
+        L.orc_gen_cigar_batch.restype = ctypes.c_int64
+        L.orc_gen_cigar_batch.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int64, P, P, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P,
+                                          ctypes.c_int64, ctypes.c_int]
         L.orc_bwt_sa_batch.argtypes = [P, ctypes.c_int64, P, P, ctypes.c_int]
         _lib = L
     return _lib
@@ -204,3 +208,33 @@ def align_regs(obwt: "OracleBwt", anns: np.ndarray, pac: np.ndarray, l_pac: int,
     if rc != 0:
         raise RuntimeError(f"oracle align_regs failed ({rc})")
     return res
+
+
+CIGAR_OUT_DTYPE = np.dtype([("score", "<i4"), ("n_cigar", "<i4"), ("NM", "<i4"), ("cg_meth", "<i4"),
+                            ("cg_unmeth", "<i4"), ("ch_meth", "<i4"), ("ch_unmeth", "<i4"), ("status", "<i4"),
+                            ("off", "<i8"), ("bytes", "<i4"), ("pad", "<i4")])
+
+
+def gen_cigar_batch(mat, o_del, e_del, o_ins, e_ins, l_pac, pac, opac, crick_l, jobs, qbuf, obuf,
+                    n_threads: int = 1):
+    """Reference bwa_gen_cigar2 (bwa.c:199-351) over a job table, as mem_reg2aln calls it.
+
+    Returns (out[CIGAR_OUT_DTYPE], blob uint8): for status 0 a job's bytes are its
+    CIGAR words then the NUL-terminated "MD\tXB:Z:calls" string; status 2 has the
+    words only."""
+    mat = np.ascontiguousarray(mat, dtype=np.int8)
+    pac = np.ascontiguousarray(pac, dtype=np.uint8)
+    opac = np.ascontiguousarray(opac, dtype=np.uint8)
+    jobs = np.ascontiguousarray(jobs)
+    qbuf = np.ascontiguousarray(qbuf, dtype=np.uint8)
+    obuf = np.ascontiguousarray(obuf, dtype=np.uint8)
+    n = len(jobs)
+    out = np.zeros(n, CIGAR_OUT_DTYPE)
+    cap = int(np.maximum(jobs["l_query"], 0).sum() + np.maximum(jobs["re"] - jobs["rb"], 0).clip(0, 1 << 20).sum()) * 16 + 64 * n + 64
+    blob = np.zeros(cap, np.uint8)
+    used = lib().orc_gen_cigar_batch(_p(mat), o_del, e_del, o_ins, e_ins, l_pac, _p(pac), _p(opac), crick_l, n,
+                                     _p(jobs), _p(qbuf) if len(qbuf) else None, _p(obuf) if len(obuf) else None,
+                                     _p(out), _p(blob), cap, n_threads)
+    if used < 0:
+        raise RuntimeError("oracle CIGAR blob too small")
+    return out, blob[:used].copy()

@@ -109,3 +109,134 @@ def golden_reads_rep(n=400, seed=20261203 + 100):
         r[e] = rng.integers(0, 4, int(e.sum()))
         reads.append(synth.bs_convert(r.astype(np.uint8), g2a=bool(k & 1)))
     return reads
+
+
+# ------------------------------------------------------- CIGAR / MD / XB jobs
+
+CIGAR_JOB_DTYPE = np.dtype([("rb", "<i8"), ("re", "<i8"), ("qoff", "<i8"), ("ooff", "<i8"),
+                            ("l_query", "<i4"), ("w", "<i4")])
+
+
+def pac_codes(pac, lo, hi):
+    """Forward-strand codes of positions [lo, hi) of a 2-bit pac (_get_pac, bntseq.h:79)."""
+    k = np.arange(lo, hi, dtype=np.int64)
+    return ((pac[k >> 2] >> ((~k & 3) << 1)) & 3).astype(np.uint8)
+
+
+def doubled_seq(pac, l_pac, beg, end):
+    """Bases of [beg, end) of the doubled sequence (one strand, no clamping): bns_get_seq."""
+    if beg >= l_pac:
+        return (3 - pac_codes(pac, 2 * l_pac - end, 2 * l_pac - beg)[::-1]).astype(np.uint8)
+    return pac_codes(pac, beg, end)
+
+
+def _edit(rng, seqs, sub, n_indel):
+    """The same substitutions and indels applied to parallel sequences."""
+    seqs = [s.copy() for s in seqs]
+    L = len(seqs[0])
+    e = np.nonzero(rng.random(L) < sub)[0]
+    for s in seqs:
+        s[e] = (s[e] + 1 + (e % 3)) % 4
+    for _ in range(n_indel):
+        at = int(rng.integers(1, max(2, len(seqs[0]) - 1)))
+        ln = int(rng.integers(1, 6))
+        if rng.random() < 0.5:
+            ins = rng.integers(0, 4, ln).astype(np.uint8)
+            seqs = [np.concatenate([s[:at], ins, s[at:]]) for s in seqs]
+        else:
+            seqs = [np.concatenate([s[:at], s[at + ln:]]) for s in seqs]
+    return seqs
+
+
+def golden_cigar_jobs(pac, opac, l_pac, crick_l, n_random=500, seed=20261203 + 11):
+    """bwa_gen_cigar2 jobs against a bisulfite index (pac = converted, opac = original
+    bases): reads drawn from both strands of Watson and Crick contigs with mismatches,
+    indels and partial methylation, region starts inside the read (mem_reg2aln hands the
+    whole original read with query + qb, bwamem.c:1228), the bands mem_reg2aln tries,
+    the ungapped w = 0 path, unrelated sequences, and the rejected / no-MD corner cases.
+    Returns (jobs[CIGAR_JOB_DTYPE], qbuf, obuf, tags) -- tags name each job's kind."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    jobs, qparts, oparts, tags = [], [], [], []
+    qn = on = 0
+
+    def add(rb, re, q, oq, w, tag, qb=0):
+        nonlocal qn, on
+        q = np.asarray(q, np.uint8)
+        oq = np.asarray(oq, np.uint8)
+        jobs.append((rb, re, qn + qb, on, len(q) - qb, w))
+        qparts.append(q)
+        oparts.append(oq)
+        qn += len(q)
+        on += len(oq)
+        tags.append(tag)
+
+    def methylate(oref, frac):
+        oq = oref.copy()
+        for c, t in ((1, 3), (2, 0)):
+            m = (oq == c) & (rng.random(len(oq)) > frac)
+            oq[m] = t
+        return oq
+
+    widths = np.array([0, 1, 2, 5, 10, 20, 40, 100, 200, 400])
+    for i in range(n_random):
+        L = int(rng.integers(20, 251))
+        rev = bool(rng.random() < 0.5)
+        base = int(rng.integers(3, l_pac - L - 10))
+        rb = base + (l_pac if rev else 0)
+        ref = doubled_seq(pac, l_pac, rb, rb + L)
+        oref = doubled_seq(opac, l_pac, rb, rb + L)
+        oq0 = methylate(oref, rng.random())
+        n_indel = int(rng.choice([0, 0, 0, 1, 2, 3]))
+        q, oq = _edit(rng, [ref, oq0], float(rng.choice([0.0, 0.01, 0.03, 0.08])), n_indel)
+        if rng.random() < 0.1:
+            q[rng.random(len(q)) < 0.05] = 4                    # N in the read
+        re = rb + L + int(rng.integers(-3, 4)) * (i % 3 == 0)
+        w = int(rng.choice(widths))
+        if len(q) != re - rb and w == 0:
+            w = int(rng.choice(widths[1:]))
+        qb = int(rng.integers(0, 12)) if i % 4 == 0 else 0      # region starting inside the read
+        if qb:
+            pre = rng.integers(0, 4, qb).astype(np.uint8)
+            q = np.concatenate([pre, q])
+            oq = np.concatenate([pre, oq])
+        add(rb, re, q, oq, w, "random", qb)
+    for rev in (0, 1):                                          # ungapped path (bwa.c:222-230)
+        for L in (30, 100, 151):
+            rb = int(rng.integers(10, l_pac - 300)) + rev * l_pac
+            ref = doubled_seq(pac, l_pac, rb, rb + L)
+            oq = methylate(doubled_seq(opac, l_pac, rb, rb + L), 0.5)
+            q, oq = _edit(rng, [ref, oq], 0.02, 0)
+            add(rb, rb + L, q, oq, 0, "ungapped")
+    for w in (10, 100, 400):                                    # unrelated sequences: long CIGARs
+        for L in (40, 120, 250):
+            rb = int(rng.integers(10, 2 * l_pac - 400))
+            if rb < l_pac < rb + L + 5:
+                rb = l_pac + 10
+            q = rng.integers(0, 4, L).astype(np.uint8)
+            add(rb, rb + L + 5, q, rng.integers(0, 4, L), w, "unrelated")
+    # corner cases of the interval (bwa.c:211-215, 264-266)
+    q = doubled_seq(pac, l_pac, 1000, 1100)
+    oq = doubled_seq(opac, l_pac, 1000, 1100)
+    add(1000, 1100, q[:0], oq[:0], 10, "reject_empty_query")
+    add(1000, 1000, q, oq, 10, "reject_empty_ref")
+    add(1100, 1000, q, oq, 10, "reject_reversed")
+    add(l_pac - 50, l_pac + 50, q, oq, 10, "reject_bridging")
+    for rb, re, tag in ((l_pac - 100, l_pac, "no_md_forward_end"), (l_pac - 101, l_pac - 1, "no_md_forward_end1"),
+                        (l_pac, l_pac + 100, "no_md_reverse_start"), (l_pac + 1, l_pac + 101, "no_md_reverse_start1"),
+                        (l_pac + 2, l_pac + 102, "reverse_first_context"), (l_pac - 102, l_pac - 2, "forward_last_context"),
+                        (2, 102, "forward_first_context"), (2 * l_pac - 102, 2 * l_pac - 2, "reverse_last_context"),
+                        (crick_l - 50, crick_l + 50, "crick_boundary"), (crick_l, crick_l + 100, "crick_start"),
+                        (crick_l + l_pac - 50, crick_l + l_pac + 50, "crick_boundary_rev"),
+                        (crick_l + l_pac, crick_l + l_pac + 100, "crick_start_rev")):
+        ref = doubled_seq(pac, l_pac, rb, re)
+        oref = doubled_seq(opac, l_pac, rb, re)
+        q, oq = _edit(rng, [ref, methylate(oref, 0.4)], 0.02, 1)
+        add(rb, re, q, oq, 20, tag)
+    for rb, re, tag in ((0, 100, "clipped_start"), (1, 101, "clipped_start1"),
+                        (2 * l_pac - 100, 2 * l_pac, "clipped_end"), (2 * l_pac - 101, 2 * l_pac - 1, "clipped_end1")):
+        ref = doubled_seq(pac, l_pac, rb, re)
+        oref = doubled_seq(opac, l_pac, rb, re)
+        add(rb, re, ref, oref, 20, tag)
+    add(5000, 5100, doubled_seq(pac, l_pac, 5000, 5100), doubled_seq(opac, l_pac, 5000, 5100), 0, "perfect_w0")
+    jobs = np.array(jobs, CIGAR_JOB_DTYPE)
+    return jobs, np.concatenate(qparts), np.concatenate(oparts), np.array(tags)

@@ -7,6 +7,7 @@ sources (this script, and only this script, reads them):
     python tests/golden/make_golden.py ksw     # ksw_extend2 tuples
     python tests/golden/make_golden.py index   # reference `bwa index` checksums
     python tests/golden/make_golden.py reads   # seeds / chains / regions / job stream
+    python tests/golden/make_golden.py cigar   # bwa_gen_cigar2 records (CIGAR, MD, XB)
 
 Every output value in the fixtures comes from the reference code compiled
 from BSBolt's bsbolt/External/BWA sources (oracle/_ref/golden_dump,
@@ -28,8 +29,8 @@ sys.path.insert(0, ROOT)
 from bsbolt_gb300 import synth  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from golden_data import (GENOME, GENOME_REP, OPTS, golden_genome, golden_genome_rep,  # noqa: E402
-                         golden_reads, golden_reads_rep)
+from golden_data import (GENOME, GENOME_REP, OPTS, golden_cigar_jobs, golden_genome,  # noqa: E402
+                         golden_genome_rep, golden_reads, golden_reads_rep)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
@@ -240,10 +241,88 @@ def make_reads(td, prefix, reads=None, names=("L5", "L30"), tag=""):
         print(fn, os.path.getsize(fn), "smem", len(d["smem"]), "regs", len(d["regs"]), "ksw", len(d["ksw_out"]))
 
 
+# ------------------------------------------------------------------ cigar
+
+CIGAR_SCORINGS = [("default", 1, 4, 6, 1, 6, 1), ("asym", 2, 5, 5, 3, 7, 2)]
+
+
+def run_ref_gen_cigar(L, mat, o_del, e_del, o_ins, e_ins, bi, jobs, qbuf, obuf):
+    """The reference bwa_gen_cigar2 (bwa.c:199-351), one call per job as mem_reg2aln
+    makes it (bwamem.c:1228).  Returns (records[n, 8] int32, blob, offsets)."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.free.argtypes = [ctypes.c_void_p]
+    f = L.bwa_gen_cigar2
+    f.restype = ctypes.POINTER(ctypes.c_uint32)
+    I = ctypes.c_int
+    P = ctypes.c_void_p
+    f.argtypes = [P, I, I, I, I, I, ctypes.c_int64, P, P, I, P, ctypes.c_int64, ctypes.c_int64,
+                  ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_int64, P,
+                  ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
+    mat = np.ascontiguousarray(mat, np.int8)
+    pac = np.ascontiguousarray(bi.pac)
+    opac = np.ascontiguousarray(bi.opac)
+    recs, parts, offs = [], [], [0]
+    for j in jobs:
+        lq = int(j["l_query"])
+        q = np.ascontiguousarray(qbuf[j["qoff"]:j["qoff"] + max(lq, 0)].copy())
+        oq = np.ascontiguousarray(obuf[j["ooff"]:].copy())
+        v = [I(0) for _ in range(7)]
+        v[2].value = -7                                       # NM: -1 is written by the callee
+        ptr = f(mat.ctypes.data, o_del, e_del, o_ins, e_ins, int(j["w"]), bi.l_pac, pac.ctypes.data,
+                opac.ctypes.data, lq, q.ctypes.data if len(q) else None, int(j["rb"]), int(j["re"]),
+                ctypes.byref(v[0]), ctypes.byref(v[1]), ctypes.byref(v[2]), bi.crick_l,
+                oq.ctypes.data if len(oq) else None, ctypes.byref(v[3]), ctypes.byref(v[4]),
+                ctypes.byref(v[5]), ctypes.byref(v[6]))
+        score, n_cigar, nm = v[0].value, v[1].value, v[2].value
+        if not ptr:
+            status, data = 1, b""
+            score = 0
+        else:
+            words = bytes(np.ctypeslib.as_array(ptr, (max(n_cigar, 1),))[:n_cigar].tobytes())
+            if nm == -1:
+                status, data = 2, words
+            else:
+                s = ctypes.string_at(ctypes.addressof(ptr.contents) + 4 * n_cigar)
+                status, data = 0, words + s + b"\0"
+            libc.free(ctypes.cast(ptr, ctypes.c_void_p))
+        meth = [v[k].value for k in range(3, 7)] if status == 0 else [0, 0, 0, 0]
+        recs.append([score, n_cigar if status != 1 else 0, nm if status == 0 else -1] + meth + [status])
+        parts.append(data)
+        offs.append(offs[-1] + len(data))
+    return np.array(recs, np.int32), np.frombuffer(b"".join(parts), np.uint8).copy(), np.array(offs, np.int64)
+
+
+def make_cigar(td):
+    import ctypes
+    import oracle
+    from bsbolt_gb300 import index
+    prefix = make_index(td)
+    bi = index.BwaIndex(prefix)
+    jobs, qbuf, obuf, tags = golden_cigar_jobs(bi.pac, bi.opac, bi.l_pac, bi.crick_l)
+    L = ctypes.CDLL(os.path.join(REF, "libbwaref.so"))
+    for name, a, b, o_del, e_del, o_ins, e_ins in CIGAR_SCORINGS:
+        mat = synth.fill_scmat(a, b)
+        # jobs where the reference reads memory it never wrote are left out (the oracle
+        # reports them by status)
+        o, _ = oracle.gen_cigar_batch(mat, o_del, e_del, o_ins, e_ins, bi.l_pac, bi.pac, bi.opac, bi.crick_l,
+                                      jobs, qbuf, obuf)
+        keep = np.nonzero(o["status"] < 3)[0]
+        recs, blob, boff = run_ref_gen_cigar(L, mat, o_del, e_del, o_ins, e_ins, bi, jobs[keep], qbuf, obuf)
+        fn = os.path.join(HERE, f"cigar_{name}.npz")
+        np.savez_compressed(fn, keep=keep, scoring=np.array([a, b, o_del, e_del, o_ins, e_ins], np.int32),
+                            recs=recs, blob=blob, blob_off=boff)
+        print(fn, os.path.getsize(fn), "jobs", len(keep), "of", len(jobs),
+              "status", np.bincount(recs[:, 7], minlength=3))
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["ksw"]
     if "ksw" in what:
         make_ksw()
+    if "cigar" in what:
+        with tempfile.TemporaryDirectory() as td:
+            make_cigar(td)
     if "index" in what or "reads" in what:
         with tempfile.TemporaryDirectory() as td:
             prefix = make_index(td)
