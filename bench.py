@@ -140,20 +140,97 @@ def ref2mb_workload(n_pairs=20000):
     d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"ref2mb_{n_pairs}")
     os.makedirs(d, exist_ok=True)
     prefix = os.path.join(d, "ref")
-    if not os.path.exists(prefix + ".sa"):
+    if not os.path.exists(prefix + ".sa") or not os.path.exists(os.path.join(d, "oreads.npy")):
         contigs = synth.bs_genome(4, 500_000, gc=0.41, cpg_frac=0.01, seed=20261203)
         synth.write_fasta(prefix + ".fa", contigs)
         index.build_index(prefix + ".fa", prefix)
         r1, r2 = synth.bs_reads_pe(contigs, n_pairs, 100, 300, 30, seed=20261203)
-        reads = []
+        reads, oreads = [], []
         for a, b in zip(r1, r2):
             reads.append(synth.bs_convert(a, g2a=False))
             reads.append(synth.bs_convert(b, g2a=True))
+            oreads += [a, b]
         offs = np.zeros(len(reads) + 1, np.int64)
         offs[1:] = np.cumsum([len(r) for r in reads])
         np.save(os.path.join(d, "reads.npy"), np.concatenate(reads))
+        np.save(os.path.join(d, "oreads.npy"), np.concatenate(oreads))
         np.save(os.path.join(d, "offs.npy"), offs)
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
+
+
+def ref2mb_original_reads(n_pairs=20000):
+    """The 2 Mb workload's reads as sequenced (before the in-silico conversion), same offsets."""
+    ref2mb_workload(n_pairs)
+    return np.load(os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"ref2mb_{n_pairs}", "oreads.npy"))
+
+
+def infer_bw(l1, l2, score, a, q, r):
+    """infer_bw (bwamem.c:796-803), vectorised; the double is truncated as C converts it."""
+    l1, l2, score = (np.asarray(v, np.int64) for v in (l1, l2, score))
+    w = np.trunc((np.minimum(l1, l2) * a - score - q) / r + 2.0).astype(np.int64)
+    w = np.maximum(w, np.abs(l1 - l2))
+    return np.where((l1 == l2) & (l1 * a - score < ((q + r - a) << 1)), 0, w)
+
+
+def cigar_jobs_from_regions(regs, roff, offs, opt):
+    """One bwa_gen_cigar2 job per read -- its best region, with the first band mem_reg2aln
+    tries (bwamem.c:1219-1228): query = read + qb, the original read from its start."""
+    n = len(roff) - 1
+    has = np.nonzero(roff[1:] > roff[:-1])[0]
+    best = np.array([roff[r] + int(np.argmax(regs["score"][roff[r]:roff[r + 1]])) for r in has], np.int64)
+    g = regs[best]
+    l1, l2 = g["qe"] - g["qb"], g["re"] - g["rb"]
+    w2 = np.maximum(infer_bw(l1, l2, g["truesc"], opt.a, opt.o_del, opt.e_del),
+                    infer_bw(l1, l2, g["truesc"], opt.a, opt.o_ins, opt.e_ins))
+    w2 = np.where(w2 > opt.w, np.minimum(w2, g["w"]), w2)
+    w2 = np.minimum(w2, opt.w << 2)
+    from bsbolt_gb300 import cigar
+    jobs = np.zeros(len(best), cigar.JOB_DTYPE)
+    jobs["rb"], jobs["re"] = g["rb"], g["re"]
+    jobs["qoff"] = offs[has] + g["qb"]
+    jobs["ooff"] = offs[has]
+    jobs["l_query"] = l1
+    jobs["w"] = w2
+    return jobs, n
+
+
+def cigar_block(ctx, steps):
+    """bwa_gen_cigar2 for the best region of every read of the 2 Mb workload: GPU batch
+    (host buffers, copies included) against the CPU oracle on all host threads."""
+    import oracle
+    from bsbolt_gb300 import _lib, cigar, index, seed, synth
+    prefix, reads, offs = ref2mb_workload()
+    oreads = ref2mb_original_reads()
+    seed.load_index(ctx, prefix)
+    bi = index.BwaIndex(prefix)
+    opt = _lib.AlignOpt.bwa_defaults()
+    regs, roff = seed.align_regs(ctx, reads, offs, opt)
+    jobs, n_reads = cigar_jobs_from_regions(regs, roff, offs, opt)
+    out, blob = cigar.gen_cigar_batch(ctx, jobs, reads, oreads, bi.crick_l, opt)        # warm-up
+    k = max(3, min(steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        out, blob = cigar.gen_cigar_batch(ctx, jobs, reads, oreads, bi.crick_l, opt)
+    gpu_s = (time.perf_counter() - t0) / k
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref, rblob = oracle.gen_cigar_batch(synth.fill_scmat(opt.a, opt.b), opt.o_del, opt.e_del, opt.o_ins, opt.e_ins,
+                                        bi.l_pac, bi.pac, bi.opac, bi.crick_l, jobs, reads, oreads, n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    same = bool(all(np.array_equal(out[f], ref[f]) for f in ref.dtype.names if f != "pad")
+                and np.array_equal(blob, rblob))
+    n = len(jobs)
+    return {
+        "workload": "2 Mb bisulfite reference, the best region of each of the 40k reads of the 20k-pair "
+                    "2x100 workload, first band of mem_reg2aln (infer_bw), bwa_gen_cigar2 as mem_reg2aln calls it",
+        "jobs": n, "gapped_jobs": int((jobs["w"] > 0).sum()), "mean_band_w": round(float(jobs["w"].mean()), 2),
+        "gpu_alignments_per_s": round(n / gpu_s, 1), "gpu_ms_per_batch": round(gpu_s * 1e3, 3),
+        "h2d_bytes_per_batch": int(jobs.nbytes + reads.nbytes + oreads.nbytes),
+        "d2h_bytes_per_batch": int(out.nbytes + len(blob)),
+        "cpu_oracle_alignments_per_s": round(n / cpu_s, 1), "cpu_oracle_threads": threads,
+        "records_bit_exact_vs_oracle": same,
+        "status_counts": {str(s): int(c) for s, c in enumerate(np.bincount(out["status"], minlength=5))},
+    }
 
 
 def ref100mb_workload(n_pairs=100_000):
@@ -606,6 +683,13 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             secondary = {"error": f"{type(e).__name__}: {e}"}
 
+    cig = None
+    if rank == 0 and not args.no_cigar:
+        try:
+            cig = cigar_block(ctx, args.steps)
+        except Exception as e:   # reported, never hidden
+            cig = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
@@ -637,6 +721,7 @@ def run_ours(args, ws, rank, local):
             "learned_schedule": learned,
             "autotune": tuned,
             "pipeline_100mb_ref": big,
+            "gen_cigar": cig,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -656,6 +741,7 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true", help="skip the seeds->regions secondary block")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
     ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
+    ap.add_argument("--no-cigar", action="store_true", help="skip the bwa_gen_cigar2 block")
     ap.add_argument("--ref100mb", action="store_true",
                     help="add the 100 Mb-reference seed->region block (builds a 100 Mb index: ~2 min the first time)")
     args = ap.parse_args()

@@ -35,6 +35,8 @@ void bsb_index_release(bsb_ctx *ctx)
     if (ctx->idx_pac) cudaFree(ctx->idx_pac);
     if (ctx->idx_sa_full) cudaFree(ctx->idx_sa_full);
     ctx->idx_sa_full = nullptr;
+    if (ctx->idx_opac) cudaFree(ctx->idx_opac);
+    ctx->idx_opac = nullptr;
     if (ctx->idx_ann_off) cudaFree(ctx->idx_ann_off);
     if (ctx->idx_ann_len) cudaFree(ctx->idx_ann_len);
     ctx->idx_bwt = ctx->idx_sa = ctx->idx_pac = ctx->idx_ann_off = ctx->idx_ann_len = nullptr;
@@ -265,7 +267,13 @@ extern "C" int bsb_index_load(bsb_ctx *ctx, const char *prefix)
             v.pac = (const uint8_t *)pac.data();
         }
     }
-    return bsb_index_upload(ctx, &v);
+    int rc = bsb_index_upload(ctx, &v);
+    if (rc) return rc;
+    // the original bases, when the index has them (bwa_idx_load reads <prefix>.opac too)
+    std::vector<char> opac;
+    if (v.l_pac > 0 && read_all((p + ".opac").c_str(), opac) && opac.size() >= (size_t)(v.l_pac + 3) / 4)
+        return bsb_index_upload_opac(ctx, (const uint8_t *)opac.data(), v.l_pac);
+    return 0;
 }
 
 extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *d_seqs,

@@ -47,6 +47,7 @@ struct bsb_ctx {
     int has_index = 0;
     void *idx_bwt = nullptr, *idx_sa = nullptr, *idx_pac = nullptr;
     void *idx_sa_full = nullptr;  // every row's SA value (built at upload when it fits), or NULL
+    void *idx_opac = nullptr;     // original (unconverted) reference, 2-bit, for the methylation calls
     uint64_t primary = 0, seq_len = 0, n_sa = 0;
     uint64_t L2[5] = {0, 0, 0, 0, 0};
     int sa_intv = 0;

@@ -251,6 +251,52 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_rea
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
 
+/* ---- CIGAR, MD and methylation strings: bwa_gen_cigar2 ------------------ */
+
+/* Replaces bwa_gen_cigar2 (bwa.c:199-351; its ksw_global2, ksw.c:504-606) for a
+ * batch of alignments, each called as mem_reg2aln calls it (bwamem.c:1228):
+ * job = (rb, re) on the doubled sequence, the converted query (nt4) of
+ * l_query bases at qbuf + qoff, the original read (nt4) at obuf + ooff (read
+ * from its first base, as the reference does), band w_.  Needs an index with
+ * pac and opac (bsb_index_upload_opac, or <prefix>.opac at bsb_index_load);
+ * crick_l is bntseq_t.crick_l.  Per job, out[i] and, for status OK, the
+ * reference's returned buffer -- n_cigar uint32 CIGAR words (len<<4|op), then
+ * the NUL-terminated "MD\tXB:Z:calls" string -- at blob + out[i].off
+ * (out[i].bytes bytes; jobs packed in order).  Host buffers; synchronous. */
+#define BSB_CIGAR_OK 0          /* CIGAR words + MD/XB string */
+#define BSB_CIGAR_REJECT 1      /* the reference returns no CIGAR (bwa.c:211, 214-215); bytes 0 */
+#define BSB_CIGAR_NO_MD 2       /* the 2-base context window bridges the strands (bwa.c:264-266):
+                                   CIGAR words only, NM -1, counts 0 */
+#define BSB_CIGAR_CLIPPED 3     /* the context window is clipped at an end of the doubled sequence
+                                   (rb < 2 or re > 2*l_pac - 2): the reference reads past its
+                                   buffer there; no output */
+#define BSB_CIGAR_BAND_EXIT 4   /* the traceback leaves the stored band, where the reference reads
+                                   backtrack cells it never wrote; no output */
+#define BSB_CIGAR_MAX_LEN 1024  /* longest query and reference interval of a job that is not rejected */
+typedef struct {
+    int64_t rb, re;
+    int64_t qoff, ooff;
+    int32_t l_query, w;
+} bsb_cigar_job_t;
+typedef struct {
+    int32_t score, n_cigar, NM;
+    int32_t cg_meth, cg_unmeth, ch_meth, ch_unmeth;
+    int32_t status;
+    int64_t off;
+    int32_t bytes, pad_;
+} bsb_cigar_out_t;
+
+/* The original (unconverted) reference, 2-bit packed like the pac (bns->opac
+ * as bwa_idx_load holds it).  Needs a loaded index with the same l_pac. */
+int bsb_index_upload_opac(bsb_ctx *ctx, const uint8_t *opac, int64_t l_pac);
+/* Uses opt's mat, o_del, e_del, o_ins, e_ins.  BSB_EINVAL when a job's bytes
+ * lie outside qbuf / obuf or blob_cap is short (*blob_used then holds the bytes
+ * needed); BSB_ETOOLONG for a job over BSB_CIGAR_MAX_LEN. */
+int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int64_t crick_l, int32_t n,
+                        const bsb_cigar_job_t *jobs, const uint8_t *qbuf, int64_t q_bytes,
+                        const uint8_t *obuf, int64_t o_bytes, bsb_cigar_out_t *out,
+                        uint8_t *blob, int64_t blob_cap, int64_t *blob_used);
+
 /* ---- learned cost model for the extension scheduler ---------------------- */
 
 /* No reference counterpart: BWA runs extensions in call order on CPU threads.
