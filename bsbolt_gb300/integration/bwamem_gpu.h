@@ -28,6 +28,21 @@ void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o);
 int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
                         int n, bseq1_t *seqs, mem_alnreg_v *regs);
 
+/* CIGAR pre-pass (bwa_gen_cigar2 on the GPU).  Called after mem_align_batch_gpu
+ * and before worker2: runs bsb_gen_cigar_batch for every region of the batch
+ * that worker2 may turn into a SAM record (score >= opt->T), with the first band
+ * mem_reg2aln tries (bwamem.c:1219-1228), and keeps the records.  The glue's
+ * __wrap_bwa_gen_cigar2 (link with -Wl,--wrap=bwa_gen_cigar2) answers a call
+ * whose job -- interval, band, query and original-read bytes, scoring -- equals a
+ * kept record with a copy of it, and passes every other call (band retries,
+ * mate-rescued regions, score-only calls) to the reference's own function, so
+ * the output is the reference's either way.  The records live until the next
+ * pre-pass.  Returns 0 or a BSB_E* code. */
+int mem_gen_cigar_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, int n, const bseq1_t *seqs,
+                              const mem_alnreg_v *regs);
+/* Records kept by the last pre-pass, and calls answered from them since. */
+void mem_gen_cigar_stats(int64_t *kept, int64_t *served);
+
 #ifdef __cplusplus
 }
 #endif

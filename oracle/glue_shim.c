@@ -2,12 +2,13 @@
  * glue_shim.c -- TEST INFRASTRUCTURE ONLY.
  *
  * Lets the BWA glue (bsbolt_gb300/integration/bwamem_gpu.c) be tested on a
- * machine without a GPU: bsb_align_regs_batch is answered by the CPU oracle
- * (whose regions equal the GPU's, by the GPU tests), and the worker1 call of
- * the reference's mem_process_seqs is redirected to mem_align_batch_gpu by a
- * link-time wrap of kt_for (-Wl,--wrap=kt_for), so the reference sources stay
- * untouched.  The resulting `bwa_glue mem` must write the same SAM as the
- * reference `bwa mem`.
+ * machine without a GPU: bsb_align_regs_batch and bsb_gen_cigar_batch are
+ * answered by the CPU oracle (whose results equal the GPU's, by the GPU tests),
+ * and the worker1 call of the reference's mem_process_seqs is redirected to
+ * mem_align_batch_gpu + mem_gen_cigar_prepass_gpu by a link-time wrap of kt_for
+ * (-Wl,--wrap=kt_for); bwa_gen_cigar2 is wrapped by the glue itself
+ * (-Wl,--wrap=bwa_gen_cigar2).  The reference sources stay untouched.  The
+ * resulting `bwa_glue mem` must write the same SAM as the reference `bwa mem`.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -16,11 +17,14 @@
 #include "bwamem_gpu.h"
 #include "bsb_oracle.h"
 #include "bsb_oracle_chain.h"
+#include "bsb_oracle_cigar.h"
+#include <stdio.h>
 
 struct bsb_ctx {
     orc_bwt_t bwt;
     orc_bns_t bns;
     orc_ann_t *anns;
+    const uint8_t *opac;
     int ready;
 };
 static struct bsb_ctx g_ctx;
@@ -61,6 +65,35 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads
     return rc ? BSB_EINVAL : 0;
 }
 
+int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int64_t crick_l, int32_t n,
+                        const bsb_cigar_job_t *jobs, const uint8_t *qbuf, int64_t q_bytes, const uint8_t *obuf,
+                        int64_t o_bytes, bsb_cigar_out_t *out, uint8_t *blob, int64_t blob_cap, int64_t *blob_used)
+{
+    int64_t used, i;
+    (void)q_bytes, (void)o_bytes;
+    used = orc_gen_cigar_batch(o->mat, o->o_del, o->e_del, o->o_ins, o->e_ins, ctx->bns.l_pac, ctx->bns.pac, ctx->opac,
+                               crick_l, n, (const orc_cigar_job_t *)jobs, qbuf, obuf, (orc_cigar_out_t *)out, blob,
+                               blob_cap, 4);
+    *blob_used = used;
+    if (used < 0) return BSB_EINVAL;
+    /* self-check of the test: with BSB_SHIM_PERTURB_CIGAR set, change one MD digit of
+     * the first record that has one, so the SAM must change if records are served */
+    if (getenv("BSB_SHIM_PERTURB_CIGAR"))
+        for (i = 0; i < n; ++i)
+            if (out[i].status == BSB_CIGAR_OK) {
+                char *md = (char *)blob + out[i].off + 4 * out[i].n_cigar;
+                if (md[0] >= '0' && md[0] <= '8') { md[0] += 1; break; }
+            }
+    return 0;
+}
+
+static void print_stats(void)
+{
+    int64_t kept, served;
+    mem_gen_cigar_stats(&kept, &served);
+    fprintf(stderr, "[bsb_glue] cigar records kept %lld served %lld\n", (long long)kept, (long long)served);
+}
+
 /* worker_t of bwamem.c:1274-1285 */
 typedef struct {
     const mem_opt_t *opt;
@@ -96,9 +129,13 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
             g_ctx.bns.n_seqs = w->bns->n_seqs;
             g_ctx.bns.anns = g_ctx.anns;
             g_ctx.bns.pac = w->pac;
+            g_ctx.opac = w->opac;
             g_ctx.ready = 1;
+            if (getenv("BSB_SHIM_STATS")) atexit(print_stats);
         }
-        if (mem_align_batch_gpu(&g_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs) != 0) abort();
+        if (mem_align_batch_gpu(&g_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs) != 0 ||
+            mem_gen_cigar_prepass_gpu(&g_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs) != 0)
+            abort();
         return;
     }
     __real_kt_for(n_threads, func, data, n);

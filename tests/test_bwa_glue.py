@@ -75,3 +75,17 @@ def test_glue_path_is_live(data):
     extra = ["-L", "5,5"]
     env = dict(os.environ, BSB_SHIM_PERTURB="1")
     assert run_mem(GLUE, fa, r1, r2, extra, env) != run_mem(BWA, fa, r1, r2, extra)
+
+
+def test_glue_cigar_records_are_served(data):
+    """The CIGAR pre-pass answers most of worker2's bwa_gen_cigar2 calls (the SAM above is
+    identical with them), and a perturbed record reaches the SAM."""
+    fa, r1, r2 = data
+    extra = ["-L", "5,5"]
+    cmd = [GLUE, "mem", "-Y", "-t", "4", "-K", "10000000"] + extra + [fa, r1, r2]
+    res = subprocess.run(cmd, capture_output=True, check=True, env=dict(os.environ, BSB_SHIM_STATS="1"))
+    line = [x for x in res.stderr.decode().splitlines() if x.startswith("[bsb_glue] cigar records")][-1]
+    kept, served = int(line.split()[4]), int(line.split()[6])
+    assert kept > 5000 and served > 0.9 * 6000, line
+    env = dict(os.environ, BSB_SHIM_PERTURB_CIGAR="1")
+    assert run_mem(GLUE, fa, r1, r2, extra, env) != run_mem(BWA, fa, r1, r2, extra)
