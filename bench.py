@@ -14,7 +14,9 @@ value  = GCUPS with every input resident in HBM, cells = the reference cell
 e2e    = GCUPS through the C ABI bsb_extend_batch with pinned host buffers:
          H2D of jobs + sequences, kernels, D2H of the tuples, every step.
 roofline = integer pipe: 14 int ops per reference cell against the measured
-         add+max throughput of this GPU (bsb_probe_int_peak).
+         add+max throughput of this GPU for the cell width the dominant kernel
+         computes in (bsb_probe_int16x2_peak for the 16-bit two-cells-per-register
+         kernels of even-C shapes, bsb_probe_int_peak for the 32-bit ones).
 cpu_baseline = the CPU port of ksw_extend2 (oracle/) on a bounded sample,
          all host cores.
 
@@ -42,7 +44,9 @@ sys.path.insert(0, ROOT)
 METRIC = "extension GCUPS (batched ksw_extend2, plain schedule)"
 UNIT = "GCUPS"
 INT_OPS_PER_CELL = 14          # add+select, 2 max, select+max, 2x(sub, max0, sub, max): ksw.c:431-447
-SCHED_KERNELS = 3              # schedule: hist, scan, scatter (then one persistent kernel per tile shape)
+SCHED_KERNELS = 3              # schedule: hist, scan, scatter (then the persistent kernels of each tile shape:
+                               # 16-bit cells + the 32-bit kernel for jobs over the 16-bit limit when C is even,
+                               # the 32-bit kernel alone when C is odd)
 
 
 def dist_env():
@@ -549,10 +553,12 @@ def run_ours(args, ws, rank, local):
                                        ctypes.c_void_p(d_cells.data_ptr()) if with_cells else None)
         _lib.check(ctx.handle, rc)
 
-    # measured integer peak
+    # measured integer peaks (32-bit cells; 16-bit cells two per register)
     tops = ctypes.c_double()
     _lib.check(ctx.handle, L.bsb_probe_int_peak(ctx.handle, ctypes.byref(tops), None))
     int_peak = tops.value
+    _lib.check(ctx.handle, L.bsb_probe_int16x2_peak(ctx.handle, ctypes.byref(tops), None))
+    int16_peak = tops.value
 
     # reference cell count of this batch (the kernel's per-job count equals the
     # reference loop's, which the parity tests pin), and a parity sample
@@ -609,7 +615,12 @@ def run_ours(args, ws, rank, local):
     dom = int(np.argmax(tile_ms))
     dom_ms = float(tile_ms[dom])
     achieved = tile_cells[dom] * INT_OPS_PER_CELL / (dom_ms * 1e-3) / 1e12
-    dom_name = "ksw_tile_kernel<%d,%d>" % (shape_list[dom][1], shape_list[dom][0])
+    dom_g, dom_c = shape_list[dom]
+    dom16 = dom_c % 2 == 0             # even C: 16-bit cells (the jobs of this batch all fit)
+    dom_name = ("ksw_tile16_kernel<%d,%d>" % (dom_c // 2, dom_g)) if dom16 else ("ksw_tile_kernel<%d,%d>" % (dom_c, dom_g))
+    dom_peak = int16_peak if dom16 else int_peak
+    cells16_frac = float(sum(tile_cells[t] for t in range(len(shape_list)) if shape_list[t][1] % 2 == 0)
+                         / max(tile_cells.sum(), 1.0))
     traffic = None
     prof = os.path.join(ROOT, "profiles", "ksw_tile_kernel_traffic.txt")
     if os.path.exists(prof):       # DRAM bytes per job of this shape from an ncu capture
@@ -694,28 +705,35 @@ def run_ours(args, ws, rank, local):
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16x2" if cells16_frac >= 0.5 else "int32",
             "data": "synthetic (seeded PCG64): the 4M-job extension workload's shapes",
             "config": {"workload": "batched ksw_extend2, 4M jobs, qlen U[10,140], target=query+100nt "
                                    "(1% sub, 0.1% indel, 20% unrelated), h0 U[19,100], w=100, a1 b4 o6 e1 z100 L5",
                        "jobs": n, "cells_per_step": total_cells, "seq_bytes": int(len(seq)),
                        "l2": "inputs 1.0 GB > 129 MB L2 per step (no flush needed)",
                        "schedule": "plain (default tile map, longest bound first)", "parallelism": f"replicas x{ws}"},
-            "roofline": {"bound": "int", "achieved": round(achieved, 3), "peak": round(int_peak, 3),
-                         "unit": "Tops/s", "frac": round(achieved / int_peak, 4), "traffic": traffic,
+            "roofline": {"bound": "int", "achieved": round(achieved, 3), "peak": round(dom_peak, 3),
+                         "unit": "Tops/s", "frac": round(achieved / dom_peak, 4), "traffic": traffic,
                          "kernel": dom_name, "kernel_ms_per_launch": round(dom_ms, 4),
                          "kernel_cells_per_launch": int(tile_cells[dom]),
                          "kernel_share_of_step": round(dom_ms / kernel_ms, 4),
-                         "peak_source": "measured add+max int32 throughput (bsb_probe_int_peak) on this GPU; "
-                                        "MEASURED_PEAKS.json has no integer figure",
+                         "peak_source": ("measured add+max throughput on 16-bit pairs (__viaddmax_s16x2, "
+                                         "bsb_probe_int16x2_peak) on this GPU, the width this kernel computes in"
+                                         if dom16 else
+                                         "measured add+max int32 throughput (bsb_probe_int_peak) on this GPU") +
+                                        "; MEASURED_PEAKS.json has no integer figure",
+                         "int32_peak": round(int_peak, 3), "int16x2_peak": round(int16_peak, 3),
                          "ops_per_cell": INT_OPS_PER_CELL,
-                         "all_kernels": {"achieved": round(achieved_all, 3), "frac": round(achieved_all / int_peak, 4),
+                         "all_kernels": {"achieved": round(achieved_all, 3),
+                                         "frac": round(achieved_all / (int16_peak if cells16_frac >= 0.5 else int_peak), 4),
+                                         "cells_on_16bit_kernels": round(cells16_frac, 4),
                                          "ms_per_step": round(kernel_ms, 4)}},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
                     "h2d_bytes_per_step": int(jobs_u8.nbytes + len(seq)), "d2h_bytes_per_step": int(n * 24),
                     "tuples_match_device_run": e2e_match, "s_per_step": round(e2e_s, 4)},
-            "gpu_launches": (SCHED_KERNELS + len(mapped)) * args.steps,
+            "gpu_launches": (SCHED_KERNELS + sum(2 if shape_list[t][1] % 2 == 0 else 1 for t in mapped)) * args.steps,
             "clocks": clocks,
             "pipeline": secondary,
             "learned_schedule": learned,

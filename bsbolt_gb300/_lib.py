@@ -29,7 +29,7 @@ BSB_TILE_MAP_LEN = 1025
 EXPORTS = (
     "bsb_ctx_create", "bsb_ctx_destroy", "bsb_last_error", "bsb_strerror", "bsb_ctx_stream",
     "bsb_extend_batch", "bsb_extend_batch_device", "bsb_sync", "bsb_last_kernel_ms",
-    "bsb_probe_int_peak",
+    "bsb_probe_int_peak", "bsb_probe_int16x2_peak",
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
@@ -123,6 +123,8 @@ def load(path: str = LIB_PATH):
     L.bsb_sync.restype = I32
     L.bsb_probe_int_peak.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     L.bsb_probe_int_peak.restype = I32
+    L.bsb_probe_int16x2_peak.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    L.bsb_probe_int16x2_peak.restype = I32
     L.bsb_index_upload.argtypes = [P, P]
     L.bsb_index_upload.restype = I32
     L.bsb_index_load.argtypes = [P, ctypes.c_char_p]

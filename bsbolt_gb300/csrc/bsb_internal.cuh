@@ -97,6 +97,7 @@ struct KswParams {
     int8_t mat[25];
     int o_del, e_del, o_ins, e_ins, zdrop;
     int mat_max;
+    int pack16;        // set by ksw_launch: the penalties allow 16-bit cells
 };
 
 // Launches the extension of n jobs (device buffers) on stream, scheduled by

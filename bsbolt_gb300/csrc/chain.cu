@@ -866,6 +866,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     int mx = 0;
     for (int i = 0; i < 25; ++i) mx = mx > o->mat[i] ? mx : o->mat[i];
     P.mat_max = mx;
+    P.pack16 = 0;
     chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
                                                  pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
     // every extension of these reads fits (max_len + 1) columns: the narrowest variant that holds them

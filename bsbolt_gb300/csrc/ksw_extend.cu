@@ -25,18 +25,25 @@
 // assigns to its query length (ksw_tiles.cuh), and within a shape jobs are
 // issued longest-bound-first (qlen x min(tlen, qlen+w), or a caller supplied
 // cost key); each shape runs as a persistent kernel whose groups pull jobs
-// from a device counter.  Results never depend on the shape or the order.
+// from a device counter.  Shapes with an even C run their jobs on 16-bit cells,
+// two per register (ksw_group16.cuh); a job whose scores could leave 16 bits
+// (h0 + qlen * max(mat) > kPack16MaxH) is binned last in its shape and runs on
+// the 32-bit kernel.  Results never depend on the shape, the cell width or the
+// order.
 
 #include <climits>
 #include <cstdio>
 
+#include "ksw_group16.cuh"
 #include "ksw_tiles.cuh"
 
 __constant__ KswTileMap c_default_tile_map = kDefaultTileMap;
 
 namespace {
 
-constexpr int kClasses = 128;           // cost classes within a tile shape
+constexpr int kClasses = 128;           // cost classes within a tile shape; the last one holds the
+                                        // jobs that need 32-bit cells
+constexpr int kWideClass = kClasses - 1;
 
 __device__ __forceinline__ int cost_class(uint32_t key)
 {
@@ -45,8 +52,18 @@ __device__ __forceinline__ int cost_class(uint32_t key)
     const int msb = 31 - __clz(key);
     const int frac = msb >= 2 ? (int)((key >> (msb - 2)) & 3) : (int)((key << (2 - msb)) & 3);
     const int c = msb * 4 + frac;
-    return c < kClasses ? c : kClasses - 1;
+    return c < kWideClass ? c : kWideClass - 1;
 }
+
+// Shapes with a 16-bit kernel (even C), as a bit set.
+constexpr uint64_t pack16_tiles()
+{
+    uint64_t m = 0;
+    for (int t = 0; t < kNumTiles; ++t)
+        if (kTileList[t].C % 2 == 0) m |= 1ull << t;
+    return m;
+}
+constexpr uint64_t kPack16Tiles = pack16_tiles();
 
 // Histogram of (tile, class) keys.  Tiles are major; within a tile, classes
 // are laid out most expensive first so an ascending scan issues longest-first.
@@ -58,8 +75,8 @@ constexpr int kHistSlots = kNumTiles * kClasses + 1;
 constexpr int kScanThreads = 1024;
 
 __global__ void ksw_sched_hist(const bsb_ext_job_t *__restrict__ jobs, int n, long long seq_bytes,
-                               const int32_t *__restrict__ cost, const uint8_t *__restrict__ map,
-                               int *__restrict__ hist, int32_t *__restrict__ key_out)
+                               const int32_t *__restrict__ cost, const uint8_t *__restrict__ map, int pack16,
+                               int mat_max, int *__restrict__ hist, int32_t *__restrict__ key_out)
 {
     __shared__ int sh[kHistSlots];
     for (int i = threadIdx.x; i < kHistSlots; i += blockDim.x) sh[i] = 0;
@@ -82,7 +99,11 @@ __global__ void ksw_sched_hist(const bsb_ext_job_t *__restrict__ jobs, int n, lo
                 const long long c = (long long)jb.qlen * max(span, 0LL);
                 k = (uint32_t)min(c, (long long)0x7fffffff);
             }
-            key = t < kNumTiles ? t * kClasses + (kClasses - 1 - cost_class(k)) : kRejectKey;
+            const bool wide = pack16 && (kPack16Tiles >> t & 1) &&
+                              (long long)jb.h0 + (long long)jb.qlen * mat_max > kPack16MaxH;
+            key = t >= kNumTiles ? kRejectKey
+                  : wide         ? t * kClasses + kWideClass
+                                 : t * kClasses + (kWideClass - 1 - cost_class(k));
         }
         key_out[i] = key;
         atomicAdd(&sh[key], 1);
@@ -93,10 +114,13 @@ __global__ void ksw_sched_hist(const bsb_ext_job_t *__restrict__ jobs, int n, lo
 }
 
 // Exclusive scan of the histogram (one block: a contiguous chunk per thread,
-// then a scan of the chunk totals) -> cursors and tile starts.
-// bin_start[kNumTiles] is where the rejected jobs begin; rejected[0] counts them.
+// then a scan of the chunk totals) -> cursors and, per tile t, the ranges of its
+// launches: ranges[6t ..] = {start, wide start | wide start, end | start, end}
+// (the 16-bit kernel, the 32-bit kernel for the wide class, or one 32-bit kernel
+// for the whole tile).  rejected[0] counts the rejected jobs.
+constexpr int kRangeInts = 6;
 __global__ void __launch_bounds__(kScanThreads)
-ksw_sched_scan(const int *__restrict__ hist, int *__restrict__ cursor, int32_t *__restrict__ bin_start,
+ksw_sched_scan(const int *__restrict__ hist, int *__restrict__ cursor, int32_t *__restrict__ ranges,
                int *__restrict__ rejected)
 {
     constexpr int kChunk = (kHistSlots + kScanThreads - 1) / kScanThreads;
@@ -123,7 +147,13 @@ ksw_sched_scan(const int *__restrict__ hist, int *__restrict__ cursor, int32_t *
         const int i = lo + k;
         if (i < kHistSlots) {
             cursor[i] = acc;
-            if (i % kClasses == 0) bin_start[i / kClasses] = acc;      // also bin_start[kNumTiles] (reject slot)
+            const int tile = i / kClasses, cls = i % kClasses;
+            if (cls == 0) {
+                if (tile < kNumTiles) ranges[kRangeInts * tile] = ranges[kRangeInts * tile + 4] = acc;
+                if (tile > 0) ranges[kRangeInts * (tile - 1) + 3] = ranges[kRangeInts * (tile - 1) + 5] = acc;
+            }
+            if (cls == kWideClass && tile < kNumTiles)
+                ranges[kRangeInts * tile + 1] = ranges[kRangeInts * tile + 2] = acc;
             if (i == kRejectKey) rejected[0] = tot[kScanThreads - 1] - acc;
         }
         acc += v[k];
@@ -143,11 +173,11 @@ __global__ void ksw_sched_scatter(const int32_t *__restrict__ key, int n, int *_
 
 static_assert(kRejectKey % kClasses == 0, "the reject slot starts a bin");
 
-// scratch layout (int32 words): counter[kNumTiles] | rejected[1] | hist[kHistSlots] |
-//   cursor[kHistSlots] | bin_start[kNumTiles+1] | (256-byte aligned) key[n] | order[n]
+// scratch layout (int32 words): counter[3*kNumTiles] | rejected[1] | hist[kHistSlots] |
+//   cursor[kHistSlots] | ranges[kRangeInts*kNumTiles] | (256-byte aligned) key[n] | order[n]
 static size_t fixed_bytes()
 {
-    size_t fixed = sizeof(int) * (kNumTiles + 1 + 2 * kHistSlots + kNumTiles + 1);
+    size_t fixed = sizeof(int) * (3 * kNumTiles + 1 + 2 * kHistSlots + kRangeInts * kNumTiles);
     return (fixed + 255) & ~(size_t)255;
 }
 
@@ -157,7 +187,7 @@ int ksw_max_qlen() { return kMaxNeed - 1; }
 
 int64_t ksw_concurrent_below() { return (int64_t)1 << 20; }
 
-int *ksw_rejected_counter(void *scratch) { return (int *)scratch + kNumTiles; }
+int *ksw_rejected_counter(void *scratch) { return (int *)scratch + 3 * kNumTiles; }
 
 const uint8_t *ksw_default_tile_map() { return kDefaultTileMap.tile; }
 
@@ -182,21 +212,26 @@ cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t 
                        cudaEvent_t ev0, cudaEvent_t ev1, const cudaEvent_t *tile_ev, const KswStreams *ms)
 {
     char *p = (char *)scratch;
-    int *counter = (int *)p;
-    int *rejected = counter + kNumTiles;
+    int *counter = (int *)p;                // 3 per tile: 16-bit range, wide range, whole tile
+    int *rejected = counter + 3 * kNumTiles;
     int *hist = rejected + 1;
     int *cursor = hist + kHistSlots;
-    int32_t *bin_start = cursor + kHistSlots;
+    int32_t *ranges = cursor + kHistSlots;
     int32_t *key = (int32_t *)(p + fixed_bytes());
     int32_t *order = key + n;
+    // 16-bit cells need every value of the packed arithmetic inside 16 bits: penalties
+    // and their multiples by a lane's column count stay small (scores are checked per job)
+    KswParams Q = P;
+    Q.pack16 = P.o_del + P.e_del <= 8000 && P.o_ins + P.e_ins <= 8000 && P.e_del <= 500 && P.e_ins <= 500;
     cudaError_t e;
     if (ev0) cudaEventRecord(ev0, st);
-    e = cudaMemsetAsync(scratch, 0, sizeof(int) * (kNumTiles + 1 + kHistSlots), st);
+    e = cudaMemsetAsync(scratch, 0, sizeof(int) * (3 * kNumTiles + 1 + kHistSlots), st);
     if (e != cudaSuccess) return e;
     if (n > 0) {
         const int nb = (int)min((int64_t)n_sm * 8, (n + 255) / 256);
-        ksw_sched_hist<<<nb, 256, 0, st>>>(d_jobs, (int)n, (long long)seq_bytes, d_cost, d_map, hist, key);
-        ksw_sched_scan<<<1, kScanThreads, 0, st>>>(hist, cursor, bin_start, rejected);
+        ksw_sched_hist<<<nb, 256, 0, st>>>(d_jobs, (int)n, (long long)seq_bytes, d_cost, d_map, Q.pack16,
+                                           Q.mat_max, hist, key);
+        ksw_sched_scan<<<1, kScanThreads, 0, st>>>(hist, cursor, ranges, rejected);
         ksw_sched_scatter<<<nb, 256, 0, st>>>(key, (int)n, cursor, order);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -211,12 +246,19 @@ cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t 
         int k = 0;
         for (int t = 0; t < kNumTiles; ++t) {
             if (!(tiles >> t & 1)) continue;
-            KswTileLaunch f = ksw_tile_launcher(t);
+            KswTileLaunch f = ksw_tile_launcher(t), f16 = Q.pack16 ? ksw_tile16_launcher(t) : nullptr;
             if (!f) return cudaErrorInvalidValue;
             const int lane = k++ % (BSB_AUX_STREAMS + 1);
             cudaStream_t s = conc && lane ? ms->aux[lane - 1] : st;
+            const int32_t *r = ranges + kRangeInts * t;
             if (tile_ev) cudaEventRecord(tile_ev[2 * t], s);
-            e = f(P, d_jobs, d_seq, order, bin_start, t, counter, d_out, d_cells, n_sm, s);
+            if (f16) {
+                // the wide class is rare (very large h0): one block per SM drains it
+                e = f16(Q, d_jobs, d_seq, order, r, counter + 3 * t, d_out, d_cells, n_sm, s);
+                if (e == cudaSuccess) e = f(Q, d_jobs, d_seq, order, r + 2, counter + 3 * t + 1, d_out, d_cells, -n_sm, s);
+            } else {
+                e = f(Q, d_jobs, d_seq, order, r + 4, counter + 3 * t + 2, d_out, d_cells, n_sm, s);
+            }
             if (e != cudaSuccess) return e;
             if (tile_ev) cudaEventRecord(tile_ev[2 * t + 1], s);
         }

@@ -1,0 +1,305 @@
+// ksw_group16.cuh -- ksw_group.cuh's row step on 16-bit cells, two columns per register.
+//
+// Same groups, rows, band logic, reductions and results as ksw_group_run (and so
+// as ksw_extend2, ksw.c:380-479); what changes is the cell arithmetic.  A lane owns
+// C = 2*C2 query columns and holds column u in the low half and column u + C2 in
+// the high half of register u, as signed 16-bit values, so every cell operation --
+// M = H + score (or 0), E, F, H = max(M, E, F), the band-edge selects -- is one
+// 16x2 instruction for two cells (__viaddmax_s16x2, __vimax3_s16x2, ...).  The two
+// halves are two runs of the row's F recurrence, over columns [0, C2) and
+// [C2, C); the high run's carry-in is max(carry - e_ins*C2, F at the low run's
+// end), so the group scan is unchanged.  The row maximum and its last column
+// (ties keep the later column, ksw.c:437) are tracked per half with
+// __vibmax_s16x2 and combined with the high half winning ties.
+//
+// Values stay below 2^15 when h0 + qlen * max(mat) <= kPack16MaxH (scores are at
+// most that; E, F <= H; every subtraction is by a penalty or a column count); the
+// scheduler sends any other job of the shape to the 32-bit kernel.
+#pragma once
+
+#include "ksw_group.cuh"
+
+constexpr int kPack16MaxH = 30000;
+
+__device__ __forceinline__ uint32_t pk16(int lo, int hi)
+{
+    return ((uint32_t)lo & 0xffffu) | ((uint32_t)hi << 16);
+}
+__device__ __forceinline__ int lo16(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
+__device__ __forceinline__ int hi16(uint32_t x) { return (int)x >> 16; }
+
+// Two source words, one byte each, sign-extended into the two halves:
+// low half = byte b of x, high half = byte c of y (prmt's sign-replicate mode).
+__device__ __forceinline__ uint32_t prmt2(uint32_t x, uint32_t y, uint32_t sel)
+{
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(y), "r"(sel));
+    return r;
+}
+__host__ __device__ __forceinline__ constexpr uint32_t sext2_selector(int b, int c)
+{
+    return (uint32_t)b | ((uint32_t)b | 8u) << 4 | (uint32_t)(4 + c) << 8 | ((uint32_t)(4 + c) | 8u) << 12;
+}
+
+// 1 in a half where u < the half of t (t - u >= 1), else 0.
+__device__ __forceinline__ uint32_t below16(uint32_t t, int u)
+{
+    return __viaddmin_s16x2_relu(t, pk16(-u, -u), 0x00010001u);
+}
+
+// Clamp to a small range that keeps the packed thresholds exact.
+__device__ __forceinline__ int clamp64(int x) { return x < -64 ? -64 : x > 64 ? 64 : x; }
+
+template <int C2, int G>
+__device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ext_job_t *__restrict__ jobs,
+                                                const uint8_t *__restrict__ seq, const int32_t *__restrict__ order,
+                                                int lo, int hi, int *__restrict__ counter,
+                                                bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
+{
+    constexpr int C = 2 * C2;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+    const unsigned gm = group_mask<G>(lane);
+    const int e_del = P.e_del, e_ins = P.e_ins;
+    const int oe_del = P.o_del + e_del, oe_ins = P.o_ins + e_ins;
+    const int base = gl * C;
+    const int eC = e_ins * C;
+    const uint32_t ne_del = pk16(-e_del, -e_del), ne_ins = pk16(-e_ins, -e_ins);
+    const uint32_t noe_del = pk16(-oe_del, -oe_del), noe_ins = pk16(-oe_ins, -oe_ins);
+
+    // per-group job state
+    int qlen = 0, tlen = 0, h0 = 0, w = 0, job = -1;
+    const uint8_t *t = nullptr;
+    uint32_t prof[C];
+    uint32_t profN[(C + 3) / 4];
+    uint32_t Hs[C2], Es[C2];
+    int best = 0, best_i = -1, best_j = -1, max_ie = -1, gscore = -1, max_off = 0, beg = 0, end = 0, i = 0;
+    long long ncell = 0;
+    int q_lane = 0, q_slot = 0;
+    uint32_t tch = 4u, tnext = 4u;
+#pragma unroll
+    for (int s = 0; s < C; ++s) prof[s] = 0;
+#pragma unroll
+    for (int u = 0; u < C2; ++u) Hs[u] = 0, Es[u] = 0;
+#pragma unroll
+    for (int s = 0; s < (C + 3) / 4; ++s) profN[s] = 0;
+    bool have = false, exhausted = false;
+
+    for (;;) {
+        if (!have && !exhausted) {            // this group takes its next job
+            int idx = 0;
+            if (gl == 0) idx = atomicAdd(counter, 1);
+            idx = __shfl_sync(gm, idx, 0, G) + lo;
+            if (idx < hi) {
+                job = order[idx];
+                const bsb_ext_job_t jb = jobs[job];
+                qlen = jb.qlen; tlen = jb.tlen; h0 = jb.h0;
+                const uint8_t *q = seq + jb.qoff;
+                t = seq + jb.toff;
+                const int h1run = max(h0 - oe_ins, 0);
+#pragma unroll
+                for (int s = 0; s < (C + 3) / 4; ++s) profN[s] = 0;
+                int h_init[C];
+#pragma unroll
+                for (int s = 0; s < C; ++s) {
+                    const int j = base + s;
+                    const int qc = j < qlen ? q[j] : 0;
+                    prof[s] = profile_word(P, qc);
+                    profN[s >> 2] |= (uint32_t)(uint8_t)profile_n(P, qc) << ((s & 3) * 8);
+                    h_init[s] = j == 0 ? h0 : (j <= qlen ? max(h1run - e_ins * (j - 1), 0) : 0);   // ksw.c:395-397
+                }
+#pragma unroll
+                for (int u = 0; u < C2; ++u) Hs[u] = pk16(h_init[u], h_init[u + C2]), Es[u] = 0;
+                w = jb.w;                                                                  // ksw.c:399-407
+                {
+                    int max_ins = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_ins) / e_ins + 1.);
+                    max_ins = max_ins > 1 ? max_ins : 1;
+                    w = w < max_ins ? w : max_ins;
+                    int max_del = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_del) / e_del + 1.);
+                    max_del = max_del > 1 ? max_del : 1;
+                    w = w < max_del ? w : max_del;
+                }
+                best = h0; best_i = best_j = -1; max_ie = -1; gscore = -1; max_off = 0;
+                beg = 0; end = qlen; i = 0; ncell = 0;
+                q_lane = qlen / C; q_slot = qlen % C;
+                tch = gl < tlen ? t[gl] : 4u;
+                tnext = G + gl < tlen ? t[G + gl] : 4u;
+                have = tlen > 0;
+                if (!have && gl == 0) {        // no target: the reference returns h0 untouched
+                    bsb_ext_out_t o;
+                    o.score = h0; o.qle = 0; o.tle = 0; o.gtle = 0; o.gscore = -1; o.max_off = 0;
+                    out[job] = o;
+                    if (cells) cells[job] = 0;
+                }
+            } else {
+                exhausted = true;
+            }
+        }
+        const unsigned act = __ballot_sync(0xffffffffu, have);
+        if (!act) break;
+        if (!have) continue;
+
+        // ---- one target row of this group's job (ksw.c:412-470); per-job decisions
+        // are selects or warp-uniform branches, as in ksw_group_run.
+        const int tc = (int)__shfl_sync(act, tch, i & (G - 1), G);
+        if ((i & (G - 1)) == G - 1) {
+            tch = tnext;
+            const int ti = i + G + 1 + gl;
+            tnext = ti < tlen ? t[ti] : 4u;
+        }
+        const bool bump = beg < i - w;         // band edge (ksw.c:416-419)
+        beg = bump ? i - w : beg;
+        if (__any_sync(act, bump)) {           // cells left of the band are kept at zero
+            const uint32_t tb = pk16(clamp64(beg - base), clamp64(beg - base - C2));
+#pragma unroll
+            for (int u = 0; u < C2; ++u) {
+                const uint32_t keep = ~(below16(tb, u) * 0xffffu);
+                Hs[u] &= keep, Es[u] &= keep;
+            }
+        }
+        end = min(end, i + w + 1);
+        end = min(end, qlen);
+        const int h1_init = beg == 0 ? max(h0 - (P.o_del + e_del * (i + 1)), 0) : 0;   // ksw.c:421-424
+        const bool empty = beg >= end;         // empty band: the zero row max stops the job
+
+        // pass 1: M, next-row E, and the two halves' F runs from a zero carry-in.
+        // M = H(i-1,j-1) + score, or at most 0 when H(i-1,j-1) == 0 (ksw.c:431): the
+        // minimum with 0x7fff where H > 0 and with 0 where H == 0.
+        uint32_t Mv[C2], En[C2], Pf[C2];
+        uint32_t local = 0;
+        if (!__any_sync(act, tc >= 4)) {
+            const uint32_t sel = sext2_selector(tc, tc);
+#pragma unroll
+            for (int u = 0; u < C2; ++u) {
+                const uint32_t sc = prmt2(prof[u], prof[u + C2], sel);
+                const uint32_t Hp = Hs[u];
+                const uint32_t M = __viaddmin_s16x2(Hp, sc, __vimin_s16x2_relu(Hp, 0x00010001u) * 0x7fffu);
+                En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
+                Pf[u] = local;
+                local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
+                Mv[u] = M;
+            }
+        } else {                               // some group has an N in the target
+            const uint32_t sel = sext2_selector(tc < 4 ? tc : 0, tc < 4 ? tc : 0);
+#pragma unroll
+            for (int u = 0; u < C2; ++u) {
+                const uint32_t sc = tc < 4 ? prmt2(prof[u], prof[u + C2], sel)
+                                           : prmt2(profN[u >> 2], profN[(u + C2) >> 2],
+                                                   sext2_selector(u & 3, (u + C2) & 3));
+                const uint32_t Hp = Hs[u];
+                const uint32_t M = __viaddmin_s16x2(Hp, sc, __vimin_s16x2_relu(Hp, 0x00010001u) * 0x7fffu);
+                En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
+                Pf[u] = local;
+                local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
+                Mv[u] = M;
+            }
+        }
+        // the lane's map x -> max(x - e_ins*C, F_lane), then the group scan (ksw_group_run)
+        const int f_lo_end = lo16(local);
+        const int f_lane = max(f_lo_end - e_ins * C2, hi16(local));
+        int incl = f_lane;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1)
+            incl = __viaddmax_s32(__shfl_up_sync(act, incl, d, G), -eC * d, incl);
+        const int excl = __shfl_up_sync(act, incl, 1, G);
+        const int carry = gl == 0 ? 0 : excl;
+        const uint32_t carry2 = pk16(carry, max(carry - e_ins * C2, f_lo_end));
+
+        // pass 2a: F, H, and the row maximum with its last column, per half
+        const int rend = end - base;
+        const uint32_t t_lt = pk16(clamp64(rend), clamp64(rend - C2));
+        uint32_t Hv[C2];
+        uint32_t mx = 0xffffffffu;             // -1 in both halves: the first column always sets
+        int arg_lo = 0, arg_hi = 0;
+#pragma unroll
+        for (int u = 0; u < C2; ++u) {
+            const uint32_t F = __viaddmax_s16x2(carry2, pk16(-e_ins * u, -e_ins * u), Pf[u]);
+            const uint32_t H = __vimax3_s16x2(Mv[u], Es[u], F);
+            Hv[u] = H;
+            const uint32_t Hm = H & (below16(t_lt, u) * 0xffffu);   // columns past the band count as 0
+            bool p_hi, p_lo;
+            mx = __vibmax_s16x2(Hm, mx, &p_hi, &p_lo);             // ties: the later column
+            arg_lo = p_lo ? u : arg_lo;
+            arg_hi = p_hi ? u : arg_hi;
+        }
+        // pass 2b: the new eh[] -- E(i+1, j) inside the band, 0 at end, kept beyond;
+        // H shifted one column up to end, kept beyond -- and the non-zero cells
+        const uint32_t t_le = pk16(clamp64(rend + 1), clamp64(rend + 1 - C2));
+        int Hleft = __shfl_up_sync(act, hi16(Hv[C2 - 1]), 1, G);
+        if (gl == 0) Hleft = h1_init;
+        uint32_t nzw = 0;
+#pragma unroll
+        for (int u = 0; u < C2; ++u) {
+            const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = below16(t_le, u) * 0xffffu;
+            const uint32_t nE = (En[u] & ltm) | (Es[u] & ~lem);
+            Es[u] = nE;
+            const uint32_t prevH = u == 0 ? pk16(Hleft, lo16(Hv[C2 - 1])) : Hv[u - 1];
+            const uint32_t nH = (prevH & lem) | (Hs[u] & ~lem);
+            Hs[u] = nH;
+            nzw |= __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;
+        }
+        uint32_t nzb = (nzw & 0xffffu) | (nzw >> 16) << C2;
+        nzb &= rend < 0 ? 0u : rend >= C - 1 ? 0xffffffffu : (2u << rend) - 1u;   // columns s <= rend
+        // the lane's maximum: the high half (later columns) wins ties
+        const int m_lo = lo16(mx), m_hi = hi16(mx);
+        const int kmax = m_hi >= m_lo ? m_hi * 1024 + arg_hi + C2 : m_lo * 1024 + arg_lo;
+        const int kw = group_max<G>(act, kmax + base);
+        const int m = kw >> 10, mj = kw & 1023;
+        if (!empty) ncell += end - beg;
+
+        // query end reached: eh[qlen].h == H(i, qlen-1), or h1 for an empty band at qlen (ksw.c:450-453)
+        int hq = h1_init;
+        if (__any_sync(act, !empty && end == qlen)) {
+            int hsel = 0;
+#pragma unroll
+            for (int u = 0; u < C2; ++u) {
+                hsel = u == q_slot ? lo16(Hs[u]) : hsel;
+                hsel = u + C2 == q_slot ? hi16(Hs[u]) : hsel;
+            }
+            const int h1 = __shfl_sync(act, hsel, q_lane, G);
+            hq = empty ? hq : h1;
+        }
+        if (empty ? beg == qlen : end == qlen) {
+            max_ie = gscore > hq ? max_ie : i;
+            gscore = gscore > hq ? gscore : hq;
+        }
+
+        // row maximum, z-drop (ksw.c:454-464)
+        const bool live = !empty && m != 0;
+        const bool up = live && m > best;
+        const int di = i - best_i, dj = mj - best_j;
+        const int drop = di > dj ? best - m - (di - dj) * e_del : best - m - (dj - di) * e_ins;
+        const bool zd = live && !up && P.zdrop > 0 && drop > P.zdrop;
+        if (up) {
+            best = m, best_i = i, best_j = mj;
+            const int d = mj > i ? mj - i : i - mj;
+            max_off = max_off > d ? max_off : d;
+        }
+
+        // shrink to the non-zero cells (ksw.c:466-469), as in ksw_group_run
+        int fnz, lnz;
+        if constexpr (G == 32) {
+            fnz = __reduce_min_sync(act, nzb ? base + __ffs(nzb) - 1 : INT_MAX);
+            lnz = __reduce_max_sync(act, nzb ? base + 31 - __clz(nzb) : -1);
+        } else {
+            const uint32_t pk = nzb ? (uint32_t)(2048 - base - __ffs(nzb)) << 16 | (uint32_t)(base + 32 - __clz(nzb)) : 0u;
+            const uint32_t r = group_max_u16x2<G>(act, pk);
+            fnz = 2047 - (int)(r >> 16);
+            lnz = (int)(r & 0xffffu) - 1;
+        }
+        const int jj = fnz < end ? lnz : (lnz == end ? end : end - 1);
+        beg = fnz < end ? fnz : end;
+        end = jj + 2 < qlen ? jj + 2 : qlen;
+        ++i;
+        const bool done = !live || zd || i >= tlen;
+        if (done) {
+            if (gl == 0) {
+                bsb_ext_out_t o;
+                o.score = best; o.qle = best_j + 1; o.tle = best_i + 1;
+                o.gtle = max_ie + 1; o.gscore = gscore; o.max_off = max_off;
+                out[job] = o;
+                if (cells) cells[job] = ncell;
+            }
+            have = false;
+        }
+    }
+}

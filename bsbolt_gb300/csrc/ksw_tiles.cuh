@@ -45,16 +45,18 @@ struct KswTileMap {
 };
 
 // 4 lanes up to 64 columns, 8 lanes up to 144, 16 up to 256, then 32; the
-// narrowest C that holds the query within each group size.
+// narrowest even C that holds the query within each group size (even C runs
+// on 16-bit cells, two per register: cheaper than the next-narrower odd C).
+constexpr int even_up(int c) { return c + (c & 1); }
 constexpr KswTileMap make_default_tile_map()
 {
     KswTileMap m{};
     for (int need = 1; need <= kMaxNeed; ++need) {
         int t = 0;
-        if (need <= 64) t = tile_index(4, (need + 3) / 4);
-        else if (need <= 144) t = tile_index(8, (need + 7) / 8 < 9 ? 9 : (need + 7) / 8);
-        else if (need <= 256) t = tile_index(16, (need + 15) / 16 < 10 ? 10 : (need + 15) / 16);
-        else if (need <= 512) t = tile_index(32, (need + 31) / 32 < 9 ? 9 : (need + 31) / 32);
+        if (need <= 64) t = tile_index(4, even_up((need + 3) / 4));
+        else if (need <= 144) t = tile_index(8, even_up((need + 7) / 8 < 9 ? 9 : (need + 7) / 8));
+        else if (need <= 256) t = tile_index(16, even_up((need + 15) / 16 < 10 ? 10 : (need + 15) / 16));
+        else if (need <= 512) t = tile_index(32, even_up((need + 31) / 32 < 9 ? 9 : (need + 31) / 32));
         else if (need <= 640) t = tile_index(32, 20);
         else if (need <= 768) t = tile_index(32, 24);
         else if (need <= 896) t = tile_index(32, 28);
@@ -66,17 +68,22 @@ constexpr KswTileMap make_default_tile_map()
 
 constexpr KswTileMap kDefaultTileMap = make_default_tile_map();
 
-// Launches the persistent kernel of one tile shape over bin `bin` of the
-// scheduled order (jobs order[bin_start[bin] .. bin_start[bin+1]) ).
+// Launches the persistent kernel of one tile shape over a range of the scheduled
+// order: the jobs order[range[0] .. range[1]), drawn through *counter.
 typedef cudaError_t (*KswTileLaunch)(const KswParams &P, const bsb_ext_job_t *jobs, const uint8_t *seq,
-                                     const int32_t *order, const int32_t *bin_start, int bin, int *counter,
+                                     const int32_t *order, const int32_t *range, int *counter,
                                      bsb_ext_out_t *out, int64_t *cells, int n_sm, cudaStream_t st);
 
 KswTileLaunch ksw_tiles_g4(int C);
 KswTileLaunch ksw_tiles_g8(int C);
 KswTileLaunch ksw_tiles_g16(int C);
 KswTileLaunch ksw_tiles_g32(int C);
+KswTileLaunch ksw_tiles16_g4(int C);
+KswTileLaunch ksw_tiles16_g8(int C);
+KswTileLaunch ksw_tiles16_g16(int C);
+KswTileLaunch ksw_tiles16_g32(int C);
 
+// The 32-bit cell kernel of tile t (every shape has one).
 inline KswTileLaunch ksw_tile_launcher(int t)
 {
     if (t < 0 || t >= kNumTiles) return nullptr;
@@ -86,6 +93,20 @@ inline KswTileLaunch ksw_tile_launcher(int t)
     case 8: return ksw_tiles_g8(s.C);
     case 16: return ksw_tiles_g16(s.C);
     case 32: return ksw_tiles_g32(s.C);
+    default: return nullptr;
+    }
+}
+
+// The 16-bit two-columns-per-register kernel of tile t (shapes with an even C), or NULL.
+inline KswTileLaunch ksw_tile16_launcher(int t)
+{
+    if (t < 0 || t >= kNumTiles || kTileList[t].C % 2) return nullptr;
+    const KswTile s = kTileList[t];
+    switch (s.G) {
+    case 4: return ksw_tiles16_g4(s.C);
+    case 8: return ksw_tiles16_g8(s.C);
+    case 16: return ksw_tiles16_g16(s.C);
+    case 32: return ksw_tiles16_g32(s.C);
     default: return nullptr;
     }
 }

@@ -1,4 +1,4 @@
-// ksw_tiles_g32.cu -- extension kernels with 32 lanes per job (see ksw_tiles.cuh).
+// ksw_tiles_g32.cu -- extension kernels with 32 lanes (a warp) per job, 32-bit cells (see ksw_tiles.cuh).
 #include "ksw_tiles_impl.cuh"
 
 KswTileLaunch ksw_tiles_g32(int C)

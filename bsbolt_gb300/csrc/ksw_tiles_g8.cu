@@ -1,4 +1,4 @@
-// ksw_tiles_g8.cu -- extension kernels with 8 lanes per job (see ksw_tiles.cuh).
+// ksw_tiles_g8.cu -- extension kernels with 8 lanes per job, 32-bit cells (see ksw_tiles.cuh).
 #include "ksw_tiles_impl.cuh"
 
 KswTileLaunch ksw_tiles_g8(int C)

@@ -365,6 +365,9 @@ int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_ext_job_t *
  * operations per second, counting each add and each max as one operation.
  * The roofline denominator for the integer-bound extension kernels. */
 int bsb_probe_int_peak(bsb_ctx *ctx, double *tops, double *ms);
+/* The same on two 16-bit values per register (__viaddmax_s16x2): the peak of the
+ * 16-bit cell kernels, four operations per instruction. */
+int bsb_probe_int16x2_peak(bsb_ctx *ctx, double *tops, double *ms);
 
 #ifdef __cplusplus
 }
