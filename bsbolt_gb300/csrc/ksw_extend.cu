@@ -220,9 +220,11 @@ cudaError_t ksw_launch(const KswParams &P, const bsb_ext_job_t *d_jobs, int64_t 
     int32_t *key = (int32_t *)(p + fixed_bytes());
     int32_t *order = key + n;
     // 16-bit cells need every value of the packed arithmetic inside 16 bits: penalties
-    // and their multiples by a lane's column count stay small (scores are checked per job)
+    // and their multiples by a lane's column count stay small, and scores at most
+    // kPack16MaxScore (h0 + qlen * max score is checked per job)
     KswParams Q = P;
-    Q.pack16 = P.o_del + P.e_del <= 8000 && P.o_ins + P.e_ins <= 8000 && P.e_del <= 500 && P.e_ins <= 500;
+    Q.pack16 = P.o_del + P.e_del <= 8000 && P.o_ins + P.e_ins <= 8000 && P.e_del <= 500 && P.e_ins <= 500 &&
+               P.mat_max <= kPack16MaxScore;
     cudaError_t e;
     if (ev0) cudaEventRecord(ev0, st);
     e = cudaMemsetAsync(scratch, 0, sizeof(int) * (3 * kNumTiles + 1 + kHistSlots), st);

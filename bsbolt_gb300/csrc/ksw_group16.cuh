@@ -9,21 +9,24 @@
 // halves are two runs of the row's F recurrence, over columns [0, C2) and
 // [C2, C); the high run's carry-in is max(carry - e_ins*C2, F at the low run's
 // end), so the group scan is unchanged.  The row maximum and its last column
-// (ties keep the later column, ksw.c:437) are tracked per half with
-// __vibmax_s16x2 and combined with the high half winning ties.
+// (ties keep the later column, ksw.c:437) are one maximum per half over the key
+// H*16 + u, combined with the high half winning ties.
 //
-// Values stay below 2^15 when h0 + qlen * max(mat) <= kPack16MaxH (scores are at
-// most that; E, F <= H; every subtraction is by a penalty or a column count); the
-// scheduler sends any other job of the shape to the 32-bit kernel.
+// Bounds: every H is at most h0 + qlen * max(mat) <= kPack16MaxH = 2047 (E, F <= H),
+// so H*16 + u stays below 2^15; every subtraction is by a penalty or a column count
+// (the launcher checks the penalties); with max(mat) <= 15, min(H + score, H*16) is
+// H + score when H > 0 and at most 0 when H == 0, the reference's M (ksw.c:431) in
+// every use.  The scheduler sends any other job of the shape to the 32-bit kernel.
 #pragma once
 
 #include "ksw_group.cuh"
 
-constexpr int kPack16MaxH = 30000;
+constexpr int kPack16MaxH = 2047;
+constexpr int kPack16MaxScore = 15;
 
 __device__ __forceinline__ uint32_t pk16(int lo, int hi)
 {
-    return ((uint32_t)lo & 0xffffu) | ((uint32_t)hi << 16);
+    return __byte_perm((uint32_t)lo, (uint32_t)hi, 0x5410);     // low halves of lo and hi
 }
 __device__ __forceinline__ int lo16(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
 __device__ __forceinline__ int hi16(uint32_t x) { return (int)x >> 16; }
@@ -47,8 +50,6 @@ __device__ __forceinline__ uint32_t below16(uint32_t t, int u)
     return __viaddmin_s16x2_relu(t, pk16(-u, -u), 0x00010001u);
 }
 
-// Clamp to a small range that keeps the packed thresholds exact.
-__device__ __forceinline__ int clamp64(int x) { return x < -64 ? -64 : x > 64 ? 64 : x; }
 
 template <int C2, int G>
 __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ext_job_t *__restrict__ jobs,
@@ -149,7 +150,8 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         const bool bump = beg < i - w;         // band edge (ksw.c:416-419)
         beg = bump ? i - w : beg;
         if (__any_sync(act, bump)) {           // cells left of the band are kept at zero
-            const uint32_t tb = pk16(clamp64(beg - base), clamp64(beg - base - C2));
+            // |beg - base| <= 1023 and u < C2: the 16-bit differences below are exact
+            const uint32_t tb = pk16(beg - base, beg - base - C2);
 #pragma unroll
             for (int u = 0; u < C2; ++u) {
                 const uint32_t keep = ~(below16(tb, u) * 0xffffu);
@@ -163,7 +165,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
 
         // pass 1: M, next-row E, and the two halves' F runs from a zero carry-in.
         // M = H(i-1,j-1) + score, or at most 0 when H(i-1,j-1) == 0 (ksw.c:431): the
-        // minimum with 0x7fff where H > 0 and with 0 where H == 0.
+        // minimum with H*16, which is >= H + score when H > 0 (scores <= 15).
         uint32_t Mv[C2], En[C2], Pf[C2];
         uint32_t local = 0;
         if (!__any_sync(act, tc >= 4)) {
@@ -172,7 +174,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
             for (int u = 0; u < C2; ++u) {
                 const uint32_t sc = prmt2(prof[u], prof[u + C2], sel);
                 const uint32_t Hp = Hs[u];
-                const uint32_t M = __viaddmin_s16x2(Hp, sc, __vimin_s16x2_relu(Hp, 0x00010001u) * 0x7fffu);
+                const uint32_t M = __viaddmin_s16x2(Hp, sc, Hp * 16u);   // Hp <= 2047: no carry between halves
                 En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
                 Pf[u] = local;
                 local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
@@ -186,7 +188,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                                            : prmt2(profN[u >> 2], profN[(u + C2) >> 2],
                                                    sext2_selector(u & 3, (u + C2) & 3));
                 const uint32_t Hp = Hs[u];
-                const uint32_t M = __viaddmin_s16x2(Hp, sc, __vimin_s16x2_relu(Hp, 0x00010001u) * 0x7fffu);
+                const uint32_t M = __viaddmin_s16x2(Hp, sc, Hp * 16u);   // Hp <= 2047: no carry between halves
                 En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
                 Pf[u] = local;
                 local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
@@ -204,44 +206,46 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         const int carry = gl == 0 ? 0 : excl;
         const uint32_t carry2 = pk16(carry, max(carry - e_ins * C2, f_lo_end));
 
-        // pass 2a: F, H, and the row maximum with its last column, per half
-        const int rend = end - base;
-        const uint32_t t_lt = pk16(clamp64(rend), clamp64(rend - C2));
-        uint32_t Hv[C2];
-        uint32_t mx = 0xffffffffu;             // -1 in both halves: the first column always sets
-        int arg_lo = 0, arg_hi = 0;
+        // pass 2: F, H, the row maximum key, and the new eh[] -- E(i+1, j) inside the
+        // band, 0 at end, kept beyond; H shifted one column up to end, kept beyond --
+        // and the non-zero cells.  Column 0's shifted H needs the left lane's last column
+        // and column C2-1 of this lane, so it is finished after the loop.
+        const int rend = end - base;               // |rend| <= 1023: exact in 16 bits
+        const uint32_t t_lt = pk16(rend, rend - C2), t_le = pk16(rend + 1, rend + 1 - C2);
+        uint32_t kmx = 0;                          // per half: max of H*16 + u over band columns
+        uint32_t cF = carry2;                      // per half: the carry minus e_ins per column
+        uint32_t Hprev = 0, nE0 = 0, lem0 = 0, nzw = 0;
 #pragma unroll
         for (int u = 0; u < C2; ++u) {
-            const uint32_t F = __viaddmax_s16x2(carry2, pk16(-e_ins * u, -e_ins * u), Pf[u]);
+            const uint32_t F = __vimax_s16x2_relu(cF, Pf[u]);            // F >= 0 (ksw.c:446-447)
+            cF = __viaddmax_s16x2(cF, ne_ins, 0x80008000u);
             const uint32_t H = __vimax3_s16x2(Mv[u], Es[u], F);
-            Hv[u] = H;
-            const uint32_t Hm = H & (below16(t_lt, u) * 0xffffu);   // columns past the band count as 0
-            bool p_hi, p_lo;
-            mx = __vibmax_s16x2(Hm, mx, &p_hi, &p_lo);             // ties: the later column
-            arg_lo = p_lo ? u : arg_lo;
-            arg_hi = p_hi ? u : arg_hi;
-        }
-        // pass 2b: the new eh[] -- E(i+1, j) inside the band, 0 at end, kept beyond;
-        // H shifted one column up to end, kept beyond -- and the non-zero cells
-        const uint32_t t_le = pk16(clamp64(rend + 1), clamp64(rend + 1 - C2));
-        int Hleft = __shfl_up_sync(act, hi16(Hv[C2 - 1]), 1, G);
-        if (gl == 0) Hleft = h1_init;
-        uint32_t nzw = 0;
-#pragma unroll
-        for (int u = 0; u < C2; ++u) {
             const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = below16(t_le, u) * 0xffffu;
+            kmx = __vimax_s16x2_relu(kmx, (H & ltm) * 16u + pk16(u, u));   // ties: the later column
             const uint32_t nE = (En[u] & ltm) | (Es[u] & ~lem);
             Es[u] = nE;
-            const uint32_t prevH = u == 0 ? pk16(Hleft, lo16(Hv[C2 - 1])) : Hv[u - 1];
-            const uint32_t nH = (prevH & lem) | (Hs[u] & ~lem);
-            Hs[u] = nH;
-            nzw |= __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;
+            if (u > 0) {
+                const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);
+                Hs[u] = nH;
+                nzw |= __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;
+            } else {
+                nE0 = nE, lem0 = lem;
+            }
+            Hprev = H;
+        }
+        int Hleft = __shfl_up_sync(act, hi16(Hprev), 1, G);
+        if (gl == 0) Hleft = h1_init;
+        {
+            const uint32_t nH = (pk16(Hleft, lo16(Hprev)) & lem0) | (Hs[0] & ~lem0);
+            Hs[0] = nH;
+            nzw |= __vimin_s16x2_relu(nH | nE0, 0x00010001u);
         }
         uint32_t nzb = (nzw & 0xffffu) | (nzw >> 16) << C2;
         nzb &= rend < 0 ? 0u : rend >= C - 1 ? 0xffffffffu : (2u << rend) - 1u;   // columns s <= rend
         // the lane's maximum: the high half (later columns) wins ties
-        const int m_lo = lo16(mx), m_hi = hi16(mx);
-        const int kmax = m_hi >= m_lo ? m_hi * 1024 + arg_hi + C2 : m_lo * 1024 + arg_lo;
+        const int k_lo = lo16(kmx), k_hi = hi16(kmx);
+        const int kmax = (k_hi >> 4) >= (k_lo >> 4) ? (k_hi >> 4) * 1024 + (k_hi & 15) + C2
+                                                    : (k_lo >> 4) * 1024 + (k_lo & 15);
         const int kw = group_max<G>(act, kmax + base);
         const int m = kw >> 10, mj = kw & 1023;
         if (!empty) ncell += end - beg;
@@ -249,12 +253,11 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         // query end reached: eh[qlen].h == H(i, qlen-1), or h1 for an empty band at qlen (ksw.c:450-453)
         int hq = h1_init;
         if (__any_sync(act, !empty && end == qlen)) {
-            int hsel = 0;
+            const int qu = q_slot < C2 ? q_slot : q_slot - C2;
+            uint32_t wsel = 0;
 #pragma unroll
-            for (int u = 0; u < C2; ++u) {
-                hsel = u == q_slot ? lo16(Hs[u]) : hsel;
-                hsel = u + C2 == q_slot ? hi16(Hs[u]) : hsel;
-            }
+            for (int u = 0; u < C2; ++u) wsel = u == qu ? Hs[u] : wsel;
+            const int hsel = q_slot < C2 ? lo16(wsel) : hi16(wsel);
             const int h1 = __shfl_sync(act, hsel, q_lane, G);
             hq = empty ? hq : h1;
         }

@@ -69,13 +69,14 @@ def test_ksw_long_queries_all_tiles(gpu_ctx):
     assert_same(out, ref, "long queries")
 
 
-@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1), (2, 5, 5, 3, 7, 2), (1, 4, 400, 300, 450, 400)],
-                         ids=["bwa", "asym", "wide-penalties"])
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1), (2, 5, 5, 3, 7, 2), (1, 4, 400, 300, 450, 600),
+                                     (20, 30, 6, 1, 6, 1)],
+                         ids=["bwa", "asym", "wide-penalties", "large-scores"])
 def test_ksw_16bit_cell_boundary(gpu_ctx, scoring):
-    """Jobs on both sides of the 16-bit cell limit (h0 + qlen * max score around 30000) in
+    """Jobs on both sides of the 16-bit cell limit (h0 + qlen * max score around 2047) in
     one batch: the ones below run on 16-bit cells, the ones above on the 32-bit kernel of
-    the same shape, and penalties too large for 16-bit arithmetic send the whole batch to
-    32 bits; every tuple and cell count must equal the reference loop's."""
+    the same shape; penalties or scores too large for the 16-bit arithmetic send the whole
+    batch to 32 bits.  Every tuple and cell count must equal the reference loop's."""
     a, b, o_del, e_del, o_ins, e_ins = scoring
     rng = np.random.Generator(np.random.PCG64(17))
     parts, rows, base = [], [], 0
@@ -85,7 +86,7 @@ def test_ksw_16bit_cell_boundary(gpu_ctx, scoring):
         t = np.concatenate([q, rng.integers(0, 4, int(rng.integers(0, 120))).astype(np.uint8)])
         flip = rng.random(len(t)) < 0.03
         t[flip] = rng.integers(0, 5, int(flip.sum()))
-        limit = 30000 - qlen * a
+        limit = max(2047 - qlen * a, 10)
         h0 = int(rng.choice([rng.integers(1, 200), limit + int(rng.integers(-3, 4)),
                              int(rng.integers(limit - 2000, limit + 2000))]))
         parts += [q, t]
@@ -98,7 +99,7 @@ def test_ksw_16bit_cell_boundary(gpu_ctx, scoring):
     ref, rcells = oracle.ksw_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, 100, n_threads=8)
     assert_same(out, ref, f"16-bit boundary, scoring {scoring}")
     assert np.array_equal(cells, rcells)
-    assert (jobs["h0"] + jobs["qlen"] * a > 30000).sum() > 300       # both sides are exercised
+    assert (jobs["h0"] + jobs["qlen"] * a > 2047).sum() > 300        # both sides are exercised
 
 
 def test_ksw_order_invariance_device(gpu_ctx):
