@@ -56,6 +56,24 @@ def dist_env():
     return ws, rank, local
 
 
+def rank_seed(rank):
+    """Each replica extends its own batch: the 4M-job workload's generator seed, offset by rank."""
+    return 20261203 + 1 + rank
+
+
+def replica_totals(elapsed, cells, dist=None, device="cpu"):
+    """Whole-job figures of a replicas run (no data-path collective): the slowest rank's
+    time and the cells of every rank.  Without a process group, this rank's own figures."""
+    if dist is None:
+        return float(elapsed), float(cells)
+    import torch
+    t = torch.tensor([float(elapsed)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(cells)], device=device, dtype=torch.float64)
+    dist.all_reduce(c)
+    return float(t.item()), float(c.item())
+
+
 def cached_jobs(n, seed):
     from bsbolt_gb300 import synth
     d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache")
@@ -486,7 +504,7 @@ def run_reference(args, ws, rank):
     from bsbolt_gb300 import synth
     if rank != 0:
         return
-    jobs, seq = cached_jobs(args.jobs, 20261203 + 1)
+    jobs, seq = cached_jobs(args.jobs, rank_seed(0))
     mat = synth.fill_scmat(1, 4)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -524,8 +542,7 @@ def run_ours(args, ws, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    seed = 20261203 + 1 + rank
-    jobs, seq = cached_jobs(args.jobs, seed)
+    jobs, seq = cached_jobs(args.jobs, rank_seed(rank))
     n = len(jobs)
     mat = synth.fill_scmat(1, 4)
     ctx = extend.Context(local)
@@ -593,15 +610,7 @@ def run_ours(args, ws, rank, local):
             dist.barrier()
     clocks = clk.summary()
     elapsed_ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([elapsed_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        c = torch.tensor([float(total_cells)], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(c)
-        all_cells = float(c.item())
-    else:
-        all_cells = float(total_cells)
+    elapsed_ms, all_cells = replica_totals(elapsed_ms, total_cells, dist, f"cuda:{local}")
     ms_step = elapsed_ms / args.steps
     value = all_cells / (ms_step * 1e-3) / 1e9
     kernel_ms = float(np.mean(kms))
@@ -645,10 +654,7 @@ def run_ours(args, ws, rank, local):
     for _ in range(e2e_steps):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s, _ = replica_totals(e2e_s, 0, dist, f"cuda:{local}")
     e2e_val = all_cells / e2e_s / 1e9
     e2e_match = bool(np.array_equal(ho.numpy(), out_host))
 
