@@ -21,8 +21,8 @@ _SO = os.path.join(_HERE, "_build", "liborc.so")
 _lib = None
 
 
-_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c", "bsb_oracle_cigar.c")
-_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h", "bsb_oracle_cigar.h")
+_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c", "bsb_oracle_cigar.c", "bsb_oracle_sw.c")
+_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h", "bsb_oracle_cigar.h", "bsb_oracle_sw.h")
 
 
 def build(force: bool = False) -> str:
@@ -55,6 +55,9 @@ def lib():
         L.orc_collect_intv_batch.argtypes = [P, P, ctypes.c_int, P, P, P, ctypes.c_int64, P,
                                              ctypes.c_int]
         L.orc_bwt_sa_batch.restype = None
+        L.orc_align2_batch.restype = None
+        L.orc_align2_batch.argtypes = [ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, P, ctypes.c_int]
         L.orc_gen_cigar_batch.restype = ctypes.c_int64
         L.orc_gen_cigar_batch.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int64, P, P, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P,
@@ -238,3 +241,20 @@ def gen_cigar_batch(mat, o_del, e_del, o_ins, e_ins, l_pac, pac, opac, crick_l, 
     if used < 0:
         raise RuntimeError("oracle CIGAR blob too small")
     return out, blob[:used].copy()
+
+
+SW_JOB_DTYPE = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"), ("xtra", "<i4"),
+                         ("pad", "<i4")])
+KSWR_DTYPE = np.dtype([("score", "<i4"), ("te", "<i4"), ("qe", "<i4"), ("score2", "<i4"), ("te2", "<i4"),
+                       ("tb", "<i4"), ("qb", "<i4")])
+KSW_XBYTE, KSW_XSTOP, KSW_XSUBO, KSW_XSTART = 0x10000, 0x20000, 0x40000, 0x80000
+
+
+def align2_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, n_threads: int = 1):
+    """Reference ksw_align2 (ksw.c:336-360) over a job table (SW_JOB_DTYPE).  Returns kswr_t records."""
+    jobs = np.ascontiguousarray(jobs, dtype=SW_JOB_DTYPE)
+    seq = np.ascontiguousarray(seq, dtype=np.uint8)
+    mat = np.ascontiguousarray(mat, dtype=np.int8)
+    out = np.zeros(len(jobs), KSWR_DTYPE)
+    lib().orc_align2_batch(len(jobs), _p(jobs), _p(seq), _p(mat), o_del, e_del, o_ins, e_ins, _p(out), n_threads)
+    return out

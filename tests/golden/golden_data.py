@@ -240,3 +240,76 @@ def golden_cigar_jobs(pac, opac, l_pac, crick_l, n_random=500, seed=20261203 + 1
     add(5000, 5100, doubled_seq(pac, l_pac, 5000, 5100), doubled_seq(opac, l_pac, 5000, 5100), 0, "perfect_w0")
     jobs = np.array(jobs, CIGAR_JOB_DTYPE)
     return jobs, np.concatenate(qparts), np.concatenate(oparts), np.array(tags)
+
+
+# ------------------------------------------------- mate-rescue Smith-Waterman jobs
+
+SW_JOB_DTYPE = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"), ("xtra", "<i4"),
+                         ("pad", "<i4")])
+KSW_XBYTE, KSW_XSTOP, KSW_XSUBO, KSW_XSTART = 0x10000, 0x20000, 0x40000, 0x80000
+
+
+def golden_sw_jobs(a=1, n=1200, seed=20261203 + 21):
+    """ksw_align2 jobs shaped like mem_matesw's (bwamem_pair.c:135-160): a mate read of 30-250
+    bases against a reference window of a few hundred bases that holds a mutated copy of it
+    (or does not), with the flags mem_matesw passes -- XSUBO | XSTART | min_seed_len*a, plus
+    XBYTE when qlen*a < 250 -- and the other flag combinations of the interface: none, XSTART
+    alone, XSTOP, XSUBO thresholds, byte lanes on long queries (saturation, without XSTART:
+    the reference's start pass is undefined there), tiny queries and targets.
+    Returns (jobs[SW_JOB_DTYPE], seq, tags)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    jobs, parts, tags = [], [], []
+    off = 0
+
+    def add(q, t, xtra, tag):
+        nonlocal off
+        q = np.asarray(q, np.uint8)
+        t = np.asarray(t, np.uint8)
+        jobs.append((off, off + len(q), len(q), len(t), int(xtra), 0))
+        parts.extend([q, t])
+        off += len(q) + len(t)
+        tags.append(tag)
+
+    for k in range(n):
+        L = int(rng.integers(30, 251))
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        q[rng.random(L) < 0.01] = 4
+        wl = int(rng.integers(L + 20, L + 700))
+        t = rng.integers(0, 4, wl).astype(np.uint8)
+        kind = k % 5
+        if kind < 4:                                       # the mate inside the window
+            m = q.copy()
+            sub = rng.random(L) < float(rng.choice([0.0, 0.01, 0.05, 0.15]))
+            m[sub] = rng.integers(0, 4, int(sub.sum()))
+            for _ in range(int(rng.choice([0, 0, 1, 2]))):
+                at = int(rng.integers(1, len(m) - 1))
+                ln = int(rng.integers(1, 6))
+                m = np.concatenate([m[:at], rng.integers(0, 4, ln).astype(np.uint8), m[at:]]) if rng.random() < .5 \
+                    else np.concatenate([m[:at], m[at + ln:]])
+            m = m[: wl]
+            at = int(rng.integers(0, wl - len(m) + 1))
+            t[at:at + len(m)] = m
+            if kind == 3:                                  # a second, weaker copy: a suboptimal hit
+                at2 = int(rng.integers(0, max(1, wl - len(m) + 1)))
+                if abs(at2 - at) > L:
+                    m2 = m.copy()
+                    s2 = rng.random(len(m2)) < 0.2
+                    m2[s2] = rng.integers(0, 4, int(s2.sum()))
+                    t[at2:at2 + len(m2)] = m2[: wl - at2]
+        flags = [KSW_XSUBO | KSW_XSTART | (KSW_XBYTE if L * a < 250 else 0) | (19 * a),   # mem_matesw
+                 0, KSW_XSTART, KSW_XSTART | (KSW_XBYTE if L * a < 250 else 0),
+                 KSW_XSUBO | int(rng.integers(1, 60)), KSW_XSTOP | int(rng.integers(10, 120))]
+        add(q, t, flags[k % len(flags)], ["matesw", "plain", "start", "start-byte", "subo", "stop"][k % len(flags)])
+    for L in (1, 2, 3, 7, 15, 16, 17, 31, 32, 33, 48):     # lane and segment boundaries
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        t = np.concatenate([rng.integers(0, 4, 20), q, rng.integers(0, 4, 20)]).astype(np.uint8)
+        for xtra in (KSW_XSTART, KSW_XSTART | KSW_XBYTE, KSW_XSUBO | KSW_XSTART | 5):
+            add(q, t, xtra, "short")
+    add(rng.integers(0, 4, 40), np.zeros(0, np.uint8), KSW_XSTART, "empty-target")
+    add(rng.integers(0, 4, 40), rng.integers(0, 4, 1), KSW_XSTART, "one-row")
+    for L in (300, 400, 600):                               # byte lanes that saturate (no start pass)
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        t = np.concatenate([rng.integers(0, 4, 50), q, rng.integers(0, 4, 50)]).astype(np.uint8)
+        add(q, t, KSW_XBYTE | KSW_XSUBO | 19, "byte-saturated")
+        add(q, t, KSW_XSTART, "long-i16")
+    return np.array(jobs, SW_JOB_DTYPE), np.concatenate(parts), np.array(tags)

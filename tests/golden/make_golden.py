@@ -8,6 +8,7 @@ sources (this script, and only this script, reads them):
     python tests/golden/make_golden.py index   # reference `bwa index` checksums
     python tests/golden/make_golden.py reads   # seeds / chains / regions / job stream
     python tests/golden/make_golden.py cigar   # bwa_gen_cigar2 records (CIGAR, MD, XB)
+    python tests/golden/make_golden.py sw      # ksw_align2 results (mate-rescue Smith-Waterman)
 
 Every output value in the fixtures comes from the reference code compiled
 from BSBolt's bsbolt/External/BWA sources (oracle/_ref/golden_dump,
@@ -30,7 +31,7 @@ from bsbolt_gb300 import synth  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 from golden_data import (GENOME, GENOME_REP, OPTS, golden_cigar_jobs, golden_genome,  # noqa: E402
-                         golden_genome_rep, golden_reads, golden_reads_rep)
+                         golden_genome_rep, golden_reads, golden_reads_rep, golden_sw_jobs)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
@@ -316,10 +317,44 @@ def make_cigar(td):
               "status", np.bincount(recs[:, 7], minlength=3))
 
 
+# ------------------------------------------------------------------ sw
+
+SW_SCORINGS = [("default", 1, 4, 6, 1, 6, 1), ("asym", 2, 5, 5, 3, 7, 2), ("wide", 1, 3, 250, 10, 200, 60)]
+
+
+def make_sw():
+    """The reference ksw_align2 (ksw.c:336-360), one call per job."""
+    import ctypes
+    L = ctypes.CDLL(os.path.join(REF, "libbwaref.so"))
+
+    class Kswr(ctypes.Structure):
+        _fields_ = [(f, ctypes.c_int) for f in ("score", "te", "qe", "score2", "te2", "tb", "qb")]
+    f = L.ksw_align2
+    f.restype = Kswr
+    I, P = ctypes.c_int, ctypes.c_void_p
+    f.argtypes = [I, P, I, P, I, P, I, I, I, I, I, P]
+    for name, a, b, o_del, e_del, o_ins, e_ins in SW_SCORINGS:
+        jobs, seq, tags = golden_sw_jobs(a)
+        mat = np.ascontiguousarray(synth.fill_scmat(a, b))
+        recs = []
+        for j in jobs:
+            q = np.ascontiguousarray(seq[j["qoff"]:j["qoff"] + j["qlen"]].copy())
+            t = np.ascontiguousarray(seq[j["toff"]:j["toff"] + j["tlen"]].copy())
+            r = f(int(j["qlen"]), q.ctypes.data if len(q) else None, int(j["tlen"]), t.ctypes.data if len(t) else None,
+                  5, mat.ctypes.data, o_del, e_del, o_ins, e_ins, int(j["xtra"]), None)
+            recs.append([r.score, r.te, r.qe, r.score2, r.te2, r.tb, r.qb])
+        fn = os.path.join(HERE, f"sw_{name}.npz")
+        np.savez_compressed(fn, scoring=np.array([a, b, o_del, e_del, o_ins, e_ins], np.int32),
+                            recs=np.array(recs, np.int32))
+        print(fn, os.path.getsize(fn), "jobs", len(jobs))
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["ksw"]
     if "ksw" in what:
         make_ksw()
+    if "sw" in what:
+        make_sw()
     if "cigar" in what:
         with tempfile.TemporaryDirectory() as td:
             make_cigar(td)
