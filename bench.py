@@ -216,6 +216,42 @@ def cigar_jobs_from_regions(regs, roff, offs, opt):
     return jobs, n
 
 
+def matesw_block(ctx, steps, n_jobs=40000):
+    """Mate-rescue Smith-Waterman (ksw_align2 as mem_matesw calls it): GPU batch through
+    the C ABI (host buffers, copies included) against the CPU oracle on all host threads."""
+    import oracle
+    from bsbolt_gb300 import matesw, synth
+    jobs, seq = synth.matesw_jobs(n_jobs)
+    mat = synth.fill_scmat(1, 4)
+    out = matesw.align2_batch(ctx, jobs, seq, mat, 6, 1, 6, 1)                # warm-up
+    k = max(3, min(steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        out = matesw.align2_batch(ctx, jobs, seq, mat, 6, 1, 6, 1)
+    gpu_s = (time.perf_counter() - t0) / k
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = oracle.align2_batch(jobs, seq, mat, 6, 1, 6, 1, n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    same = bool(all(np.array_equal(out[f], ref[f]) for f in ref.dtype.names))
+    # cells of the forward pass as the reference computes them: padded query columns x target rows
+    p = np.where(jobs["xtra"] & matesw.KSW_XBYTE, 16, 8)
+    cells = float(((jobs["qlen"] + p - 1) // p * p).astype(np.float64) @ jobs["tlen"].astype(np.float64))
+    return {
+        "workload": f"{n_jobs} ksw_align2 jobs shaped like mem_matesw's: mate of 30-250 bases vs a window of "
+                    "read length + 20-700 bases (4 in 5 holding a mutated copy), KSW_XSUBO|KSW_XSTART|19, "
+                    "byte lanes when qlen < 250, BWA scoring",
+        "jobs": n_jobs, "forward_pass_cells": int(cells),
+        "gpu_jobs_per_s": round(n_jobs / gpu_s, 1), "gpu_ms_per_batch": round(gpu_s * 1e3, 3),
+        "gpu_forward_gcups": round(cells / gpu_s / 1e9, 2),
+        "h2d_bytes_per_batch": int(jobs.nbytes + len(seq)), "d2h_bytes_per_batch": int(out.nbytes),
+        "cpu_oracle_jobs_per_s": round(n_jobs / cpu_s, 1), "cpu_oracle_threads": threads,
+        "cpu_oracle_note": "scalar restatement of the striped SSE2 code (oracle/bsb_oracle_sw.c), slower than "
+                           "the reference's own SIMD build, which does not run on this Arm host",
+        "results_bit_exact_vs_oracle": same,
+    }
+
+
 def cigar_block(ctx, steps):
     """bwa_gen_cigar2 for the best region of every read of the 2 Mb workload: GPU batch
     (host buffers, copies included) against the CPU oracle on all host threads."""
@@ -707,6 +743,13 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             cig = {"error": f"{type(e).__name__}: {e}"}
 
+    msw = None
+    if rank == 0 and not args.no_matesw:
+        try:
+            msw = matesw_block(ctx, args.steps)
+        except Exception as e:   # reported, never hidden
+            msw = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
@@ -746,6 +789,7 @@ def run_ours(args, ws, rank, local):
             "autotune": tuned,
             "pipeline_100mb_ref": big,
             "gen_cigar": cig,
+            "mate_rescue_sw": msw,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -766,6 +810,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule block")
     ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
     ap.add_argument("--no-cigar", action="store_true", help="skip the bwa_gen_cigar2 block")
+    ap.add_argument("--no-matesw", action="store_true", help="skip the mate-rescue Smith-Waterman block")
     ap.add_argument("--ref100mb", action="store_true",
                     help="add the 100 Mb-reference seed->region block (builds a 100 Mb index: ~2 min the first time)")
     args = ap.parse_args()

@@ -34,7 +34,7 @@ EXPORTS = (
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
     "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
-    "bsb_index_upload_opac", "bsb_gen_cigar_batch",
+    "bsb_index_upload_opac", "bsb_gen_cigar_batch", "bsb_align2_batch",
 )
 
 
@@ -165,6 +165,8 @@ def load(path: str = LIB_PATH):
     L.bsb_index_upload_opac.restype = I32
     L.bsb_gen_cigar_batch.argtypes = [P, P, I64, I32, P, P, I64, P, I64, P, P, I64, ctypes.POINTER(I64)]
     L.bsb_gen_cigar_batch.restype = I32
+    L.bsb_align2_batch.argtypes = [P, P, P, I64, P, I64, P]
+    L.bsb_align2_batch.restype = I32
     _lib = L
     return L
 

@@ -262,3 +262,40 @@ def bs_convert(read: np.ndarray, g2a: bool) -> np.ndarray:
     else:
         r[r == 1] = 3
     return r
+
+
+def matesw_jobs(n_jobs: int, seed: int = 20261203 + 5, a: int = 1, min_seed_len: int = 19):
+    """Jobs shaped like mem_matesw's ksw_align2 calls (bwamem_pair.c:135-151): a mate read of
+    30-250 bases (1 % N) against a reference window of the read length plus 20-700 bases,
+    which in 4 of 5 jobs holds a copy of the read with 0-15 % substitutions and up to two
+    1-5-base indels; the flags mem_matesw passes (KSW_XSUBO | KSW_XSTART | min_seed_len*a,
+    plus KSW_XBYTE when qlen*a < 250).  Returns (jobs with qoff, toff, qlen, tlen, xtra,
+    pad as int64, int64, int32 x 4; seq)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dt = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"), ("xtra", "<i4"),
+                   ("pad", "<i4")])
+    jobs = np.zeros(n_jobs, dt)
+    parts, off = [], 0
+    for k in range(n_jobs):
+        L = int(rng.integers(30, 251))
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        q[rng.random(L) < 0.01] = 4
+        wl = int(rng.integers(L + 20, L + 700))
+        t = rng.integers(0, 4, wl).astype(np.uint8)
+        if k % 5:
+            m = q.copy()
+            sub = rng.random(L) < float(rng.choice([0.0, 0.01, 0.05, 0.15]))
+            m[sub] = rng.integers(0, 4, int(sub.sum()))
+            for _ in range(int(rng.choice([0, 0, 1, 2]))):
+                at = int(rng.integers(1, len(m) - 1))
+                ln = int(rng.integers(1, 6))
+                m = (np.concatenate([m[:at], rng.integers(0, 4, ln).astype(np.uint8), m[at:]]) if rng.random() < .5
+                     else np.concatenate([m[:at], m[at + ln:]]))
+            m = m[:wl]
+            at = int(rng.integers(0, wl - len(m) + 1))
+            t[at:at + len(m)] = m
+        xtra = 0x40000 | 0x80000 | (0x10000 if L * a < 250 else 0) | (min_seed_len * a)
+        jobs[k] = (off, off + L, L, wl, xtra, 0)
+        parts += [q, t]
+        off += L + wl
+    return jobs, np.concatenate(parts)

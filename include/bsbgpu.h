@@ -297,6 +297,31 @@ int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int64_t crick_
                         const uint8_t *obuf, int64_t o_bytes, bsb_cigar_out_t *out,
                         uint8_t *blob, int64_t blob_cap, int64_t *blob_used);
 
+/* ---- mate-rescue Smith-Waterman: ksw_align2 ----------------------------- */
+
+/* Replaces a loop of ksw_align2 calls (ksw.c:336-360, declared ksw.h:59-60), as
+ * mem_matesw makes them (bwamem_pair.c:150-151): local alignment of a query
+ * against a target (codes 0..4 in one buffer) with the 5x5 matrix and gap
+ * penalties of param (zdrop unused) and the KSW_X* flags and threshold in xtra
+ * (KSW_XBYTE 0x10000, KSW_XSTOP 0x20000, KSW_XSUBO 0x40000, KSW_XSTART 0x80000).
+ * out[i] = the reference's kswr_t, including its striped-SSE2 specifics: byte
+ * lanes (16) with KSW_XBYTE, else 16-bit lanes (8), penalties broadcast at that
+ * width, the lazy-F loop, padded query columns.  One case differs by design: a
+ * byte-lane pass that saturates (score 255) with KSW_XSTART leaves tb = qb = -1,
+ * where the reference profiles a zero-length query.  Needs a positive matrix
+ * entry.  Host buffers; synchronous. */
+#define BSB_SW_MAX_QLEN 1024
+typedef struct {
+    int64_t qoff, toff;
+    int32_t qlen, tlen;
+    int32_t xtra, pad_;
+} bsb_sw_job_t;
+typedef struct {
+    int32_t score, te, qe, score2, te2, tb, qb;
+} bsb_kswr_t;
+int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_sw_job_t *jobs, int64_t n_jobs,
+                     const uint8_t *seq, int64_t seq_bytes, bsb_kswr_t *out);
+
 /* ---- learned cost model for the extension scheduler ---------------------- */
 
 /* No reference counterpart: BWA runs extensions in call order on CPU threads.

@@ -1,0 +1,71 @@
+"""bsb_align2_batch (ksw_align2 on the GPU) against the reference and the oracle.
+
+Every kswr_t field must be identical: to the reference's own results
+(tests/golden/sw_*.npz, three scoring sets, byte and word lanes, every flag
+combination), and to the oracle on a larger seeded set of mate-rescue-shaped jobs."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from bsbolt_gb300 import _lib, matesw, synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
+import golden_data  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("score", "te", "qe", "score2", "te2", "tb", "qb")
+
+
+def assert_same(got, want, tags, what):
+    for f in FIELDS:
+        w = want[f] if want.dtype.names else want[:, FIELDS.index(f)]
+        bad = np.nonzero(got[f] != w)[0]
+        assert len(bad) == 0, f"{what}: {f} differs at jobs {bad[:6]} ({tags[bad[:6]] if tags is not None else ''}): " \
+                              f"{got[f][bad[:6]]} vs {w[bad[:6]]}"
+
+
+@pytest.mark.parametrize("name", ["default", "asym", "wide"])
+def test_align2_matches_reference(gpu_ctx, name):
+    g = np.load(os.path.join(GOLDEN, f"sw_{name}.npz"))
+    a, b, o_del, e_del, o_ins, e_ins = (int(v) for v in g["scoring"])
+    jobs, seq, tags = golden_data.golden_sw_jobs(a)
+    out = matesw.align2_batch(gpu_ctx, jobs.view(matesw.JOB_DTYPE), seq, synth.fill_scmat(a, b), o_del, e_del,
+                              o_ins, e_ins)
+    assert_same(out, g["recs"], tags, name)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_align2_matches_oracle_random(gpu_ctx, seed):
+    jobs, seq, tags = golden_data.golden_sw_jobs(1, n=6000, seed=20261203 + 40 + seed)
+    mat = synth.fill_scmat(1, 4)
+    out = matesw.align2_batch(gpu_ctx, jobs.view(matesw.JOB_DTYPE), seq, mat, 6, 1, 6, 1)
+    ref = oracle.align2_batch(jobs, seq, mat, 6, 1, 6, 1, n_threads=8)
+    assert_same(out, ref, tags, f"seed {seed}")
+    assert (out["score2"] > 0).sum() > 300 and (out["tb"] >= 0).sum() > 2000
+
+
+def test_align2_errors(gpu_ctx):
+    jobs, seq, _ = golden_data.golden_sw_jobs(1, n=20)
+    jobs = jobs.view(matesw.JOB_DTYPE)
+    mat = synth.fill_scmat(1, 4)
+    assert len(matesw.align2_batch(gpu_ctx, jobs[:0], seq, mat, 6, 1, 6, 1)) == 0
+    bad = jobs.copy()
+    bad["toff"][2] = len(seq)
+    with pytest.raises(_lib.BsbError) as e:
+        matesw.align2_batch(gpu_ctx, bad, seq, mat, 6, 1, 6, 1)
+    assert e.value.code == _lib.BSB_EINVAL
+    long_q = np.zeros(1100, np.uint8)
+    lj = np.array([(0, 0, 1100, 100, matesw.KSW_XSTART, 0)], matesw.JOB_DTYPE)
+    with pytest.raises(_lib.BsbError) as e:
+        matesw.align2_batch(gpu_ctx, lj, long_q, mat, 6, 1, 6, 1)
+    assert e.value.code == _lib.BSB_ETOOLONG
+    with pytest.raises(_lib.BsbError) as e:
+        matesw.align2_batch(gpu_ctx, jobs, seq, -np.abs(mat), 6, 1, 6, 1)
+    assert e.value.code == _lib.BSB_EINVAL
+    out = matesw.align2_batch(gpu_ctx, jobs, seq, mat, 6, 1, 6, 1)
+    ref = oracle.align2_batch(jobs, seq, mat, 6, 1, 6, 1)
+    assert_same(out, ref, None, "after errors")
