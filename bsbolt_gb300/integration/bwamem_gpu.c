@@ -9,7 +9,10 @@
  *   if (mem_align_batch_gpu(g_bsb, opt, bns, pac, n, seqs, w.regs) ||
  *       mem_gen_cigar_prepass_gpu(g_bsb, opt, bns, n, seqs, w.regs))
  *       err_fatal(__func__, "%s", bsb_last_error(g_bsb));
- * and link with -Wl,--wrap=bwa_gen_cigar2.
+ * after mem_pestat (bwamem.c:1342) add
+ *   if (mem_matesw_prepass_gpu(g_bsb, opt, bns, pac, pes, n, seqs, w.regs))
+ *       err_fatal(__func__, "%s", bsb_last_error(g_bsb));
+ * and link with -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -17,6 +20,7 @@
 
 #include "bntseq.h"
 #include "bwa.h"
+#include "ksw.h"
 #include "bwamem_gpu.h"
 
 /* defined in bwamem.c (bwamem.c:441), not declared in bwamem.h */
@@ -248,4 +252,231 @@ uint32_t *__wrap_bwa_gen_cigar2(const int8_t mat[25], int o_del, int e_del, int 
     }
     return __real_bwa_gen_cigar2(mat, o_del, e_del, o_ins, e_ins, w_, l_pac, pac, opac, l_query, query, rb, re, score,
                                  n_cigar, NM, crick_l, oquery, cg_meth, cg_unmeth, ch_meth, ch_unmeth);
+}
+
+/* ---- mate-rescue pre-pass and the ksw_align2 wrapper ----------------------- */
+
+typedef struct {
+    int32_t qlen, tlen, xtra, pad_;
+    const uint8_t *q, *t;
+    bsb_kswr_t r;
+} sw_entry_t;
+
+static struct {
+    int64_t n, mask;
+    sw_entry_t *e;
+    int64_t *slot;                 /* open addressing: entry index + 1, 0 = empty */
+    uint8_t *seq;
+    int8_t mat[25];
+    int o_del, e_del, o_ins, e_ins;
+    int64_t served;
+} g_sw;
+
+/* content hash of one ksw_align2 call: lengths, flags and both sequences */
+static uint64_t sw_hash(int qlen, const uint8_t *q, int tlen, const uint8_t *t, int xtra)
+{
+    uint64_t h = ((uint64_t)(uint32_t)qlen << 32 | (uint32_t)tlen) * 0x9e3779b97f4a7c15ULL ^ (uint32_t)xtra;
+    const uint8_t *p[2] = {q, t};
+    int l[2] = {qlen, tlen}, s, i;
+    for (s = 0; s < 2; ++s) {
+        for (i = 0; i + 8 <= l[s]; i += 8) {
+            uint64_t w;
+            memcpy(&w, p[s] + i, 8);
+            h = (h ^ w) * 0xc2b2ae3d27d4eb4fULL;
+            h ^= h >> 29;
+        }
+        for (; i < l[s]; ++i) h = (h ^ p[s][i]) * 0x165667b19e3779f9ULL;
+    }
+    return h ^ (h >> 32);
+}
+
+static void sw_clear(void)
+{
+    free(g_sw.e); free(g_sw.slot); free(g_sw.seq);
+    memset(&g_sw, 0, sizeof g_sw);
+}
+
+void mem_matesw_stats(int64_t *kept, int64_t *served)
+{
+    if (kept) *kept = g_sw.n;
+    if (served) *served = __atomic_load_n(&g_sw.served, __ATOMIC_RELAXED);
+}
+
+/* mem_infer_dir (bwamem_pair.c:23-30) */
+static int glue_infer_dir(int64_t l_pac, int64_t b1, int64_t b2, int64_t *dist)
+{
+    int64_t p2;
+    int r1 = (b1 >= l_pac), r2 = (b2 >= l_pac);
+    p2 = r1 == r2 ? b2 : (l_pac << 1) - 1 - b2;
+    *dist = p2 > b1 ? p2 - b1 : b1 - p2;
+    return (r1 == r2 ? 0 : 1) ^ (p2 > b1 ? 0 : 3);
+}
+
+typedef struct {
+    bsb_sw_job_t *jobs;
+    int64_t n, m;
+    uint8_t *seq;
+    int64_t len, cap;
+} sw_batch_t;
+
+static int64_t sw_put(sw_batch_t *b, const uint8_t *s, int64_t l)
+{
+    int64_t off = b->len;
+    if (b->len + l > b->cap) {
+        b->cap = (b->len + l) * 2 + 4096;
+        b->seq = (uint8_t *)realloc(b->seq, b->cap);
+    }
+    memcpy(b->seq + off, s, l);
+    b->len += l;
+    return off;
+}
+
+/* The ksw_align2 calls mem_matesw would make for the region a against the mate
+ * ms whose regions are ma (bwamem_pair.c:111-154), with ma as it stands before
+ * any rescue of the pair. */
+static void matesw_jobs(const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac, const mem_pestat_t pes[4],
+                        const mem_alnreg_t *a, int l_ms, const uint8_t *ms, const mem_alnreg_v *ma, uint8_t *rev,
+                        sw_batch_t *b)
+{
+    int64_t l_pac = bns->l_pac;
+    int i, r, skip[4];
+    for (r = 0; r < 4; ++r) skip[r] = pes[r].failed ? 1 : 0;
+    for (i = 0; i < (int)ma->n; ++i) {
+        int64_t dist;
+        r = glue_infer_dir(l_pac, a->rb, ma->a[i].rb, &dist);
+        if (dist >= pes[r].low && dist <= pes[r].high) skip[r] = 1;
+    }
+    if (skip[0] + skip[1] + skip[2] + skip[3] == 4) return;
+    for (r = 0; r < 4; ++r) {
+        int is_rev, is_larger, rid = -1;
+        const uint8_t *seq;
+        uint8_t *ref;
+        int64_t rb, re;
+        if (skip[r]) continue;
+        is_rev = (r >> 1 != (r & 1));
+        is_larger = !(r >> 1);
+        if (is_rev) {
+            for (i = 0; i < l_ms; ++i) rev[l_ms - 1 - i] = ms[i] < 4 ? 3 - ms[i] : 4;
+            seq = rev;
+        } else
+            seq = ms;
+        if (!is_rev) {
+            rb = is_larger ? a->rb + pes[r].low : a->rb - pes[r].high;
+            re = (is_larger ? a->rb + pes[r].high : a->rb - pes[r].low) + l_ms;
+        } else {
+            rb = (is_larger ? a->rb + pes[r].low : a->rb - pes[r].high) - l_ms;
+            re = is_larger ? a->rb + pes[r].high : a->rb - pes[r].low;
+        }
+        if (rb < 0) rb = 0;
+        if (re > l_pac << 1) re = l_pac << 1;
+        /* rb >= re leaves the reference's rid unset: that call is left to the reference */
+        if (rb >= re) continue;
+        ref = bns_fetch_seq(bns, pac, &rb, (rb + re) >> 1, &re, &rid);
+        if (a->rid == rid && re - rb >= opt->min_seed_len) {
+            bsb_sw_job_t *j;
+            if (b->n == b->m) {
+                b->m = b->m ? b->m * 2 : 1024;
+                b->jobs = (bsb_sw_job_t *)realloc(b->jobs, sizeof(bsb_sw_job_t) * b->m);
+            }
+            j = &b->jobs[b->n++];
+            memset(j, 0, sizeof *j);
+            j->qlen = l_ms, j->tlen = (int32_t)(re - rb);
+            j->xtra = KSW_XSUBO | KSW_XSTART | (l_ms * opt->a < 250 ? KSW_XBYTE : 0) | (opt->min_seed_len * opt->a);
+            j->qoff = sw_put(b, seq, l_ms);
+            j->toff = sw_put(b, ref, re - rb);
+        }
+        free(ref);
+    }
+}
+
+int mem_matesw_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
+                           const mem_pestat_t pes[4], int n, const bseq1_t *seqs, const mem_alnreg_v *regs)
+{
+    sw_batch_t b;
+    bsb_ext_param_t p;
+    bsb_kswr_t *out;
+    uint8_t *rev;
+    int64_t k, t;
+    int id, i, j, max_l = 1, rc;
+    sw_clear();
+    if (!(opt->flag & MEM_F_PE) || (opt->flag & MEM_F_NO_RESCUE)) return 0;
+    memset(&b, 0, sizeof b);
+    for (i = 0; i < n; ++i) max_l = seqs[i].l_seq > max_l ? seqs[i].l_seq : max_l;
+    rev = (uint8_t *)malloc(max_l);
+    /* mem_sam_pe's choice of regions to rescue from (bwamem_pair.c:265-274) */
+    for (id = 0; id + 1 < n; id += 2) {
+        const mem_alnreg_v *a = &regs[id];
+        for (i = 0; i < 2; ++i) {
+            const bseq1_t *m = &seqs[id + !i];
+            int taken = 0;
+            if (m->l_seq > BSB_SW_MAX_QLEN) continue;
+            for (j = 0; j < (int)a[i].n && taken < opt->max_matesw; ++j) {
+                if (a[i].a[j].score < a[i].a[0].score - opt->pen_unpaired) continue;
+                ++taken;
+                matesw_jobs(opt, bns, pac, pes, &a[i].a[j], m->l_seq, (const uint8_t *)m->seq, &a[!i], rev, &b);
+            }
+        }
+    }
+    free(rev);
+    if (b.n == 0) {
+        free(b.jobs); free(b.seq);
+        return 0;
+    }
+    memset(&p, 0, sizeof p);
+    memcpy(p.mat, opt->mat, 25);
+    p.o_del = opt->o_del, p.e_del = opt->e_del, p.o_ins = opt->o_ins, p.e_ins = opt->e_ins, p.zdrop = opt->zdrop;
+    out = (bsb_kswr_t *)malloc(sizeof(bsb_kswr_t) * b.n);
+    rc = bsb_align2_batch(ctx, &p, b.jobs, b.n, b.seq, b.len, out);
+    if (rc) {
+        free(b.jobs); free(b.seq); free(out);
+        return rc;
+    }
+    g_sw.seq = b.seq;
+    g_sw.e = (sw_entry_t *)malloc(sizeof(sw_entry_t) * b.n);
+    for (t = 1; t < 2 * b.n; t <<= 1) {}
+    g_sw.mask = t - 1;
+    g_sw.slot = (int64_t *)calloc(t, sizeof(int64_t));
+    for (k = 0; k < b.n; ++k) {
+        const bsb_sw_job_t *jb = &b.jobs[k];
+        sw_entry_t *e;
+        uint64_t h;
+        /* a saturated byte-lane pass is defined differently by the library: the
+         * reference answers that call itself */
+        if ((jb->xtra & KSW_XBYTE) && out[k].score >= 255) continue;
+        e = &g_sw.e[g_sw.n];
+        e->qlen = jb->qlen, e->tlen = jb->tlen, e->xtra = jb->xtra;
+        e->q = g_sw.seq + jb->qoff, e->t = g_sw.seq + jb->toff;
+        e->r = out[k];
+        for (h = sw_hash(e->qlen, e->q, e->tlen, e->t, e->xtra) & g_sw.mask; g_sw.slot[h]; h = (h + 1) & g_sw.mask) {}
+        g_sw.slot[h] = ++g_sw.n;
+    }
+    memcpy(g_sw.mat, opt->mat, 25);
+    g_sw.o_del = opt->o_del, g_sw.e_del = opt->e_del, g_sw.o_ins = opt->o_ins, g_sw.e_ins = opt->e_ins;
+    free(b.jobs); free(out);
+    return 0;
+}
+
+kswr_t __real_ksw_align2(int qlen, uint8_t *query, int tlen, uint8_t *target, int m, const int8_t *mat, int o_del,
+                         int e_del, int o_ins, int e_ins, int xtra, kswq_t **qry);
+
+kswr_t __wrap_ksw_align2(int qlen, uint8_t *query, int tlen, uint8_t *target, int m, const int8_t *mat, int o_del,
+                         int e_del, int o_ins, int e_ins, int xtra, kswq_t **qry)
+{
+    /* only a call without a query profile to keep, on the pre-pass's scoring */
+    if (g_sw.n && !qry && m == 5 && o_del == g_sw.o_del && e_del == g_sw.e_del && o_ins == g_sw.o_ins &&
+        e_ins == g_sw.e_ins && !memcmp(mat, g_sw.mat, 25)) {
+        uint64_t h;
+        for (h = sw_hash(qlen, query, tlen, target, xtra) & g_sw.mask; g_sw.slot[h]; h = (h + 1) & g_sw.mask) {
+            const sw_entry_t *e = &g_sw.e[g_sw.slot[h] - 1];
+            if (e->qlen == qlen && e->tlen == tlen && e->xtra == xtra && !memcmp(e->q, query, qlen) &&
+                !memcmp(e->t, target, tlen)) {
+                kswr_t r;
+                r.score = e->r.score, r.te = e->r.te, r.qe = e->r.qe, r.score2 = e->r.score2, r.te2 = e->r.te2;
+                r.tb = e->r.tb, r.qb = e->r.qb;
+                __atomic_add_fetch(&g_sw.served, 1, __ATOMIC_RELAXED);
+                return r;
+            }
+        }
+    }
+    return __real_ksw_align2(qlen, query, tlen, target, m, mat, o_del, e_del, o_ins, e_ins, xtra, qry);
 }

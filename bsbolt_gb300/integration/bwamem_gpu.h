@@ -43,6 +43,22 @@ int mem_gen_cigar_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t
 /* Records kept by the last pre-pass, and calls answered from them since. */
 void mem_gen_cigar_stats(int64_t *kept, int64_t *served);
 
+/* Mate-rescue pre-pass (ksw_align2 on the GPU).  Called after mem_pestat and
+ * before worker2 of a paired-end batch: for every pair it lists the ksw_align2
+ * calls mem_sam_pe's rescue loop would make (bwamem_pair.c:265-274 choosing the
+ * regions, mem_matesw bwamem_pair.c:111-154 the orientations, windows and
+ * flags), with each mate's regions as they stand before any rescue, runs them
+ * through bsb_align2_batch and keeps the results.  The glue's __wrap_ksw_align2
+ * (link with -Wl,--wrap=ksw_align2) answers a call whose query, target, flags and
+ * scoring equal a kept job's, and passes every other call (orientations that an
+ * earlier rescue of the same pair reopened, mem_seed_sw's calls, mates over
+ * BSB_SW_MAX_QLEN) to the reference's own function.  Nothing is kept for
+ * single-end batches or with MEM_F_NO_RESCUE.  Returns 0 or a BSB_E* code. */
+int mem_matesw_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
+                           const mem_pestat_t pes[4], int n, const bseq1_t *seqs, const mem_alnreg_v *regs);
+/* Jobs kept by the last mate-rescue pre-pass, and calls answered from them since. */
+void mem_matesw_stats(int64_t *kept, int64_t *served);
+
 #ifdef __cplusplus
 }
 #endif

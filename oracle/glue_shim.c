@@ -5,9 +5,11 @@
  * machine without a GPU: bsb_align_regs_batch and bsb_gen_cigar_batch are
  * answered by the CPU oracle (whose results equal the GPU's, by the GPU tests),
  * and the worker1 call of the reference's mem_process_seqs is redirected to
- * mem_align_batch_gpu + mem_gen_cigar_prepass_gpu by a link-time wrap of kt_for
- * (-Wl,--wrap=kt_for); bwa_gen_cigar2 is wrapped by the glue itself
- * (-Wl,--wrap=bwa_gen_cigar2).  The reference sources stay untouched.  The
+ * mem_align_batch_gpu + mem_gen_cigar_prepass_gpu, and the worker2 call is
+ * preceded by mem_matesw_prepass_gpu, by a link-time wrap of kt_for
+ * (-Wl,--wrap=kt_for); bsb_align2_batch is answered by the oracle too;
+ * bwa_gen_cigar2 and ksw_align2 are wrapped by the glue itself
+ * (-Wl,--wrap=bwa_gen_cigar2, -Wl,--wrap=ksw_align2).  The reference sources stay untouched.  The
  * resulting `bwa_glue mem` must write the same SAM as the reference `bwa mem`.
  */
 #include <stdlib.h>
@@ -18,6 +20,7 @@
 #include "bsb_oracle.h"
 #include "bsb_oracle_chain.h"
 #include "bsb_oracle_cigar.h"
+#include "bsb_oracle_sw.h"
 #include <stdio.h>
 
 struct bsb_ctx {
@@ -87,11 +90,38 @@ int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int64_t crick_l,
     return 0;
 }
 
+int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *param, const bsb_sw_job_t *jobs, int64_t n_jobs,
+                     const uint8_t *seq, int64_t seq_bytes, bsb_kswr_t *out)
+{
+    int64_t i;
+    (void)ctx, (void)seq_bytes;
+    orc_align2_batch(n_jobs, (const orc_sw_job_t *)jobs, seq, param->mat, param->o_del, param->e_del, param->o_ins,
+                     param->e_ins, (orc_kswr_t *)out, 4);
+    /* self-check of the test: with BSB_SHIM_PERTURB_SW set, move the start of every
+     * rescued hit one base right, so the SAM must change if results are served */
+    if (getenv("BSB_SHIM_PERTURB_SW"))
+        for (i = 0; i < n_jobs; ++i)
+            if (out[i].tb >= 0 && out[i].tb < out[i].te) ++out[i].tb;
+    return 0;
+}
+
+/* matesw statistics accumulated over batches (each pre-pass starts afresh) */
+static int64_t g_sw_kept, g_sw_served;
+
+static void take_sw_stats(void)
+{
+    int64_t kept, served;
+    mem_matesw_stats(&kept, &served);
+    g_sw_kept += kept, g_sw_served += served;
+}
+
 static void print_stats(void)
 {
     int64_t kept, served;
+    take_sw_stats();
     mem_gen_cigar_stats(&kept, &served);
     fprintf(stderr, "[bsb_glue] cigar records kept %lld served %lld\n", (long long)kept, (long long)served);
+    fprintf(stderr, "[bsb_glue] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
 }
 
 /* worker_t of bwamem.c:1274-1285 */
@@ -137,6 +167,12 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
             mem_gen_cigar_prepass_gpu(&g_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs) != 0)
             abort();
         return;
+    }
+    {                                  /* worker2: pes is set (mem_pestat or pes0) */
+        worker_view_t *w = (worker_view_t *)data;
+        int n_reads = (w->opt->flag & MEM_F_PE) ? (int)(n << 1) : (int)n;
+        take_sw_stats();
+        if (mem_matesw_prepass_gpu(&g_ctx, w->opt, w->bns, w->pac, w->pes, n_reads, w->seqs, w->regs) != 0) abort();
     }
     __real_kt_for(n_threads, func, data, n);
 }

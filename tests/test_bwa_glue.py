@@ -42,6 +42,14 @@ def data(tmp_path_factory):
     synth.write_fasta(fa, contigs)
     subprocess.check_call([BWA, "index", "-a", "bwtsw", fa], stderr=subprocess.DEVNULL)
     r1, r2 = synth.bs_reads_pe(contigs, 3000, 100, 300, 30, seed=4243)
+    # pairs with one end mutated at every 10th base (by +1, which neither conversion
+    # undoes): no exact 19-mer, so that end has no seed and only mate rescue places it
+    m1, m2 = synth.bs_reads_pe(contigs, 60, 100, 300, 30, seed=4245)
+    for k, (a, b) in enumerate(zip(m1, m2)):
+        x = b if k % 2 == 0 else a
+        x[5::10] = (x[5::10] + 1) % 4
+    r1 += m1
+    r2 += m2
     # a few adapter-like / random / short reads
     rng = np.random.Generator(np.random.PCG64(4244))
     for _ in range(20):
@@ -88,4 +96,19 @@ def test_glue_cigar_records_are_served(data):
     kept, served = int(line.split()[4]), int(line.split()[6])
     assert kept > 5000 and served > 0.9 * 6000, line
     env = dict(os.environ, BSB_SHIM_PERTURB_CIGAR="1")
+    assert run_mem(GLUE, fa, r1, r2, extra, env) != run_mem(BWA, fa, r1, r2, extra)
+
+
+def test_glue_matesw_results_are_served(data):
+    """The mate-rescue pre-pass answers worker2's ksw_align2 calls from mem_matesw (the
+    SAM of the identity test above is produced with them), and a perturbed result reaches
+    the SAM."""
+    fa, r1, r2 = data
+    extra = ["-L", "5,5"]
+    cmd = [GLUE, "mem", "-Y", "-t", "4", "-K", "10000000"] + extra + [fa, r1, r2]
+    res = subprocess.run(cmd, capture_output=True, check=True, env=dict(os.environ, BSB_SHIM_STATS="1"))
+    line = [x for x in res.stderr.decode().splitlines() if x.startswith("[bsb_glue] matesw jobs")][-1]
+    kept, served = int(line.split()[4]), int(line.split()[6])
+    assert kept > 0 and served > 0, line
+    env = dict(os.environ, BSB_SHIM_PERTURB_SW="1")
     assert run_mem(GLUE, fa, r1, r2, extra, env) != run_mem(BWA, fa, r1, r2, extra)
