@@ -36,3 +36,32 @@ def align2_batch(ctx: Context, jobs: np.ndarray, seq: np.ndarray, mat, o_del: in
                                 _ptr(seq) if len(seq) else None, len(seq), _ptr(out) if len(jobs) else None)
     _lib.check(ctx.handle, rc)
     return out
+
+
+def _main(argv=None) -> None:
+    """Times align2_batch on seeded mem_matesw-shaped jobs (synth.matesw_jobs): one line
+    per repetition with the wall time of the call (copies included) and its forward-pass
+    cells per second (padded query columns x target rows, as the striped code computes)."""
+    import argparse
+    import time
+
+    from . import synth
+    ap = argparse.ArgumentParser(prog="python -m bsbolt_gb300.matesw")
+    ap.add_argument("--jobs", type=int, default=40000)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    jobs, seq = synth.matesw_jobs(args.jobs)
+    mat = synth.fill_scmat(1, 4)
+    ctx = Context(args.device)
+    p = np.where(jobs["xtra"] & KSW_XBYTE, 16, 8)
+    cells = float(((jobs["qlen"] + p - 1) // p * p).astype(np.float64) @ jobs["tlen"].astype(np.float64))
+    for r in range(args.reps):
+        t0 = time.perf_counter()
+        align2_batch(ctx, jobs, seq, mat, 6, 1, 6, 1)
+        dt = time.perf_counter() - t0
+        print(f"rep {r}: {args.jobs} jobs {dt * 1e3:.3f} ms {args.jobs / dt:.0f} jobs/s {cells / dt / 1e9:.2f} GCUPS")
+
+
+if __name__ == "__main__":
+    _main()
