@@ -12,22 +12,32 @@
 // and its all-lanes exit tests (__any_sync over the group).  The group's H0/H1/E/Hmax vectors
 // live in its slice of shared memory, segment-major like the reference's.
 //
-//   sw_partition    byte-lane and word-lane jobs into two lists
-//   sw_kernel<16>   byte-lane jobs (ksw_u8), two jobs per warp
-//   sw_kernel<8>    word-lane jobs (ksw_i16), four jobs per warp
-// Each job: the forward pass with the suboptimal-score rows (KSW_XSUBO) kept in global
-// scratch, then, with KSW_XSTART, the same pass over the reversed query and target prefixes.
+//   sw_pack_kernel<16, ..> byte-lane jobs of 1..16 segments (every mate of < 250 bases with
+//                          BWA's scoring), two SIMD lanes per thread (sw_pack.cuh): forward
+//                          passes in the order of a host counting sort by segments and length,
+//                          sw_rev_scatter grouping the jobs that want start positions by the
+//                          segment count of their reversed query, then their reverse passes
+//   sw_pack_kernel<8, ..>  the same for word-lane jobs of 1..32 segments whose scores stay
+//                          clear of 16-bit saturation (sw_pack16a.cu, sw_pack16b.cu), on a
+//                          second stream
+//   sw_kernel<16>, <8>     every other job (longer queries, extreme scores or penalties, empty
+//                          queries): one SIMD lane per thread, shared-memory vectors, both
+//                          passes, on the second stream
+// A forward pass keeps the suboptimal-score rows (KSW_XSUBO) in global scratch; with
+// KSW_XSTART the same pass then runs over the reversed query and target prefixes.
 
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "bsb_internal.cuh"
+#include "sw_pack.cuh"
 
 namespace {
 
+using namespace bsbsw;
+
 constexpr int kSwBlock = 64;
-constexpr int kXByte = 0x10000, kXStop = 0x20000, kXSubo = 0x40000, kXStart = 0x80000;
 
 struct SwParams {
     int8_t mat[25];
@@ -65,10 +75,6 @@ __device__ __forceinline__ int subs16(int a, int b)          // _mm_subs_epu16 o
     const int d = (int)(uint16_t)a - (int)(uint16_t)b;
     return (int16_t)(uint16_t)(d < 0 ? 0 : d);
 }
-
-struct PassOut {
-    int score, te, qe, score2, te2;
-};
 
 // One ksw_u8 (P = 16) or ksw_i16 (P = 8) pass (ksw.c:98-327) of the group.  q(c) and t(i)
 // give query column c (< qlen) and target row i.  The caller's vectors hold slen*P entries.
@@ -124,20 +130,53 @@ __device__ PassOut sw_pass(const SwParams &S, const int8_t *smat, int qlen, int 
             }
             h = H0[x];
         }
-        // lazy F (ksw.c:166-177, 284-295): each round shifts f up one lane
-        for (int k = 0; k < 16; ++k) {
+        // lazy F (ksw.c:166-177, 284-295).  The reference shifts f up one lane per round and
+        // sweeps the segments until no lane can raise an H any more.  The sweep raises H(l, j)
+        // to relu(G(l) - j*e_ins) at most, where G(l) is the F arriving at lane l's first column,
+        //   G(0) = 0,  G(l) = max(x(l), relu(G(l-1) - slen*e_ins)),  x(l) = the f leaving lane l-1,
+        // and its early exit (Farrar's) leaves out only updates that change nothing.  So: the
+        // reference's own first test, and where a lane fails it, G as a max-plus scan over the
+        // lanes and one max per segment, with no per-segment vote.
+        // That bound needs oe_ins >= e_ins as the lanes hold them; byte lanes wrap o_ins + e_ins
+        // modulo 256, and there the reference's loop runs as it is.
+        if (poe_ins < pe_ins) {
+            for (int k = 0; k < 16; ++k) {
+                f = __shfl_up_sync(gm, f, 1, P);
+                if (l == 0) f = 0;
+                bool go = true;
+                for (int j = 0; j < slen && go; ++j) {
+                    const int x = j * P + l;
+                    int hv = max((int)H1[x], f);
+                    H1[x] = (int16_t)hv;
+                    if (U8) hv = sat8(hv - poe_ins), f = sat8(f - pe_ins);
+                    else hv = subs16(hv, poe_ins), f = subs16(f, pe_ins);
+                    go = __any_sync(gm, f > hv);
+                }
+                if (!go) break;
+            }
+        } else {
             f = __shfl_up_sync(gm, f, 1, P);
             if (l == 0) f = 0;
-            bool go = true;
-            for (int j = 0; j < slen && go; ++j) {
-                const int x = j * P + l;
-                int hv = max((int)H1[x], f);
-                H1[x] = (int16_t)hv;
-                if (U8) hv = sat8(hv - poe_ins), f = sat8(f - pe_ins);
-                else hv = subs16(hv, poe_ins), f = subs16(f, pe_ins);
-                go = __any_sync(gm, f > hv);
+            if (slen) {
+                const int h0 = max((int)H1[l], f);
+                const int hh = U8 ? sat8(h0 - poe_ins) : subs16(h0, poe_ins);
+                const int fn = U8 ? sat8(f - pe_ins) : subs16(f, pe_ins);
+                if (__any_sync(gm, fn > hh)) {
+                    const int d = pe_ins * slen;
+                    int g = f;
+#pragma unroll
+                    for (int o = 1; o < P; o <<= 1) {
+                        const int v = __shfl_up_sync(gm, g, o, P);
+                        if (l >= o) g = max(g, v - o * d);
+                    }
+                    for (int j = 0; j < slen; ++j, g = max(g - pe_ins, 0)) {
+                        const int x = j * P + l;
+                        H1[x] = (int16_t)max((int)H1[x], g);
+                    }
+                } else {
+                    H1[l] = (int16_t)h0;
+                }
             }
-            if (!go) break;
         }
         __syncwarp(gm);
         const int imax = grp_max<P>(gm, mx);
@@ -206,19 +245,10 @@ struct RevT {                    // target[0..te] reversed, the rest as is (ksw.
     __device__ int operator()(int i) const { return t[i <= te ? te - i : i]; }
 };
 
-__global__ void sw_partition(const bsb_sw_job_t *__restrict__ jobs, int64_t n, int *__restrict__ cnt,
-                             int32_t *__restrict__ list8, int32_t *__restrict__ list16)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (jobs[i].xtra & kXByte) list8[atomicAdd(&cnt[0], 1)] = (int32_t)i;
-        else list16[atomicAdd(&cnt[1], 1)] = (int32_t)i;
-    }
-}
-
 template <int P>
 __global__ void __launch_bounds__(kSwBlock)
 sw_kernel(SwParams S, const bsb_sw_job_t *__restrict__ jobs, const uint8_t *__restrict__ seq,
-          const int32_t *__restrict__ list, const int *__restrict__ n_list, int *__restrict__ next,
+          const int32_t *__restrict__ list, int total, int *__restrict__ next,
           const int64_t *__restrict__ boff, int2 *__restrict__ bscratch, bsb_kswr_t *__restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -232,7 +262,6 @@ sw_kernel(SwParams S, const bsb_sw_job_t *__restrict__ jobs, const uint8_t *__re
     unsigned char *g = sm + (size_t)(threadIdx.x / P) * (size_t)(nv * 9 + 16);
     int16_t *H0 = (int16_t *)g, *H1 = H0 + nv, *E = H1 + nv, *Hmax = E + nv;
     uint8_t *qs = (uint8_t *)(Hmax + nv);
-    const int total = *n_list;
     for (;;) {
         int k = 0;
         if (l == 0) k = atomicAdd(next, 1);
@@ -283,9 +312,20 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
     }
     if (S.qmax < 1) return bsb_fail(ctx, BSB_EINVAL, "the scoring matrix needs a positive entry");
     if (n == 0) return 0;
-    int max8 = 0, max16 = 0;
+    // Four job lists: packed byte lanes (1..16 segments), packed word lanes (1..32 segments, when
+    // 16-bit arithmetic without saturation is exact: qlen * max score <= 32640 and penalties
+    // below 32768), then the one-lane byte and word jobs.  The packed lists are in counting-sort
+    // order by segment count and then target length, both descending.
+    constexpr int kLenBins = 64, kKeys8 = kPackMaxSeg8 * kLenBins, kKeys16 = kPackMaxSeg16 * kLenBins;
+    const bool w16_ok = S.o_del + S.e_del <= 32767 && S.o_ins + S.e_ins <= 32767;
+    // the packed passes read F in closed form, which needs oe_ins >= e_ins as the lanes hold them
+    const bool b8_ok = (uint8_t)(S.o_ins + S.e_ins) >= (uint8_t)S.e_ins;
     std::vector<int64_t> boff((size_t)n);
-    int64_t nb = 0;
+    std::vector<int32_t> key((size_t)n);
+    std::vector<int32_t> lists((size_t)n);
+    std::vector<int64_t> kcnt((size_t)(kKeys8 + kKeys16) + 1, 0);
+    int64_t nb = 0, n_fb8 = 0, n_fb16 = 0, n_p8 = 0, n_p16 = 0;
+    int max8 = 0, max16 = 0;
     for (int64_t i = 0; i < n; ++i) {
         const bsb_sw_job_t &j = jobs[i];
         if (j.qlen < 0 || j.tlen < 0 || j.qoff < 0 || j.toff < 0 || j.qoff > seq_bytes - j.qlen ||
@@ -293,28 +333,81 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
             return bsb_fail(ctx, BSB_EINVAL, "job %lld: bytes outside seq", (long long)i);
         if (j.qlen > BSB_SW_MAX_QLEN)
             return bsb_fail(ctx, BSB_ETOOLONG, "job %lld: qlen %d > %d", (long long)i, j.qlen, BSB_SW_MAX_QLEN);
-        if (j.xtra & kXByte) max8 = std::max(max8, j.qlen);
-        else max16 = std::max(max16, j.qlen);
         boff[(size_t)i] = nb;
         if (j.xtra & kXSubo) nb += j.tlen;
+        const int bin = kLenBins - 1 - std::min(j.tlen >> 4, kLenBins - 1);
+        const bool byte = j.xtra & kXByte;
+        const int sl = byte ? (j.qlen + 15) >> 4 : (j.qlen + 7) >> 3;
+        int k = -1;
+        if (byte && b8_ok && sl >= 1 && sl <= kPackMaxSeg8)
+            k = (kPackMaxSeg8 - sl) * kLenBins + bin, ++n_p8;
+        else if (!byte && w16_ok && sl >= 1 && sl <= kPackMaxSeg16 && (int64_t)j.qlen * S.qmax <= 32640)
+            k = kKeys8 + (kPackMaxSeg16 - sl) * kLenBins + bin, ++n_p16;
+        else if (byte)
+            ++n_fb8, max8 = std::max(max8, j.qlen);
+        else
+            ++n_fb16, max16 = std::max(max16, j.qlen);
+        key[(size_t)i] = k;
+        if (k >= 0) ++kcnt[(size_t)k + 1];
+    }
+    for (int k = 0; k < kKeys8 + kKeys16; ++k) kcnt[(size_t)k + 1] += kcnt[(size_t)k];
+    {   // lists: [packed byte | packed word | one-lane byte | one-lane word]
+        int64_t p8 = n_p8 + n_p16, p16 = n_p8 + n_p16 + n_fb8;
+        for (int64_t i = 0; i < n; ++i) {
+            const int k = key[(size_t)i];
+            if (k >= 0) lists[(size_t)kcnt[(size_t)k]++] = (int32_t)i;
+            else if (jobs[i].xtra & kXByte) lists[(size_t)p8++] = (int32_t)i;
+            else lists[(size_t)p16++] = (int32_t)i;
+        }
     }
     S.slen8 = std::max(1, (max8 + 15) / 16), S.slen16 = std::max(1, (max16 + 7) / 8);
+    PackParams P8, P16;
+    {
+        const uint8_t sh = (uint8_t)S.shift;
+        for (int tc = 0; tc < 5; ++tc) {
+            uint8_t b[8], w[8];
+            for (int qc = 0; qc < 5; ++qc) {               // ksw_qinit (ksw.c:80-95)
+                b[qc] = (uint8_t)(p->mat[tc * 5 + qc] + sh);
+                w[qc] = (uint8_t)p->mat[tc * 5 + qc];
+            }
+            b[5] = sh, w[5] = 0;                           // the padding column: score 0
+            P8.plo[tc] = (uint32_t)b[0] | (uint32_t)b[1] << 8 | (uint32_t)b[2] << 16 | (uint32_t)b[3] << 24;
+            P8.phi[tc] = (uint32_t)b[4] | (uint32_t)b[5] << 8;
+            P16.plo[tc] = (uint32_t)w[0] | (uint32_t)w[1] << 8 | (uint32_t)w[2] << 16 | (uint32_t)w[3] << 24;
+            P16.phi[tc] = (uint32_t)w[4];
+        }
+        // the penalties as _mm_set1_epi8 / _mm_set1_epi16 broadcast them, negated in both halves
+        P8.nshift = neg2(S.shift);
+        P8.npe_del = neg2((uint8_t)S.e_del), P8.npoe_del = neg2((uint8_t)(S.o_del + S.e_del));
+        P8.npe_ins = neg2((uint8_t)S.e_ins), P8.npoe_ins = neg2((uint8_t)(S.o_ins + S.e_ins));
+        P8.shift = S.shift, P8.qmax = S.qmax, P8.pe_ins = (uint8_t)S.e_ins;
+        P16.nshift = 0;
+        P16.npe_del = neg2(std::min(S.e_del, 32767)), P16.npoe_del = neg2(std::min(S.o_del + S.e_del, 32767));
+        P16.npe_ins = neg2(std::min(S.e_ins, 32767)), P16.npoe_ins = neg2(std::min(S.o_ins + S.e_ins, 32767));
+        P16.shift = 0, P16.qmax = S.qmax, P16.pe_ins = std::min(S.e_ins, 32767);
+    }
     int rc;
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     cudaStream_t st = ctx->stream;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t jb = al(sizeof(bsb_sw_job_t) * (size_t)n), sb = al((size_t)seq_bytes), ob = al(8 * (size_t)n);
-    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, jb + sb + ob + 256, "SW input staging"))) return rc;
+    const size_t lb = al(sizeof(int32_t) * (size_t)n);
+    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, jb + sb + ob + lb + 256, "SW input staging"))) return rc;
     char *in = (char *)ctx->d_in;
     bsb_sw_job_t *d_jobs = (bsb_sw_job_t *)in;
     uint8_t *d_seq = (uint8_t *)(in + jb);
     int64_t *d_boff = (int64_t *)(in + jb + sb);
-    const size_t lb = al(sizeof(int32_t) * (size_t)n), bb = al(sizeof(int2) * (size_t)(nb > 0 ? nb : 1));
-    if ((rc = bsb_ensure(ctx, &ctx->arena2, &ctx->arena2_bytes, 2 * lb + 256 + bb, "SW scratch"))) return rc;
+    int32_t *d_list = (int32_t *)(in + jb + sb + ob);
+    const size_t bb = al(sizeof(int2) * (size_t)(nb > 0 ? nb : 1)), rb = al((size_t)n);
+    constexpr size_t kCtrBytes = 4096;
+    if ((rc = bsb_ensure(ctx, &ctx->arena2, &ctx->arena2_bytes, lb + rb + kCtrBytes + bb, "SW scratch"))) return rc;
     char *a2 = (char *)ctx->arena2;
-    int32_t *list8 = (int32_t *)a2, *list16 = (int32_t *)(a2 + lb);
-    int *cnt = (int *)(a2 + 2 * lb);                    // [0..1] list sizes, [2..3] queue heads
-    int2 *d_b = (int2 *)(a2 + 2 * lb + 256);
+    int32_t *d_rlist = (int32_t *)a2;                   // reverse lists: byte jobs, then word jobs
+    uint8_t *d_rsl = (uint8_t *)(a2 + lb);
+    // counters: [0..1] one-lane queues, then one block of kCtrInts per packed lane width
+    int *cnt = (int *)(a2 + lb + rb);
+    int *ctr8 = cnt + 64, *ctr16 = cnt + 64 + kCtrInts;
+    int2 *d_b = (int2 *)(a2 + lb + rb + kCtrBytes);
     if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, sizeof(bsb_kswr_t) * (size_t)n + 256, "SW output")))
         return rc;
     bsb_kswr_t *d_out = (bsb_kswr_t *)ctx->d_out;
@@ -322,25 +415,68 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
                        "H2D jobs")) ||
         (seq_bytes && (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seq, seq, seq_bytes, cudaMemcpyHostToDevice, st), "H2D seq"))) ||
         (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_boff, boff.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D offsets")) ||
-        (rc = bsb_cuda(ctx, cudaMemsetAsync(cnt, 0, 4 * sizeof(int), st), "SW counters")))
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_list, lists.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D lists")) ||
+        (rc = bsb_cuda(ctx, cudaMemsetAsync(cnt, 0, kCtrBytes, st), "SW counters")))
         return rc;
-    const int pb = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->n_sm * 8);
-    sw_partition<<<pb, 256, 0, st>>>(d_jobs, n, cnt, list8, list16);
-    // shared memory per group: 4 int16 vectors + the striped query, slen*P entries each
-    const size_t sm8 = (size_t)(kSwBlock / 16) * (size_t)(S.slen8 * 16 * 9 + 16);
-    const size_t sm16 = (size_t)(kSwBlock / 8) * (size_t)(S.slen16 * 8 * 9 + 16);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(sw_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(sw_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        attr_set = true;
+    // the word-lane and one-lane jobs on a second stream, beside the packed byte-lane jobs
+    const bool side = n_p16 + n_fb8 + n_fb16 > 0;
+    cudaStream_t st2 = ctx->ms.aux[0];
+    if (side) {
+        if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->ms.fork, st), "SW fork")) ||
+            (rc = bsb_cuda(ctx, cudaStreamWaitEvent(st2, ctx->ms.fork, 0), "SW fork")))
+            return rc;
+        if (n_p16) {   // word lanes: the 17..32-segment part of the list, then the 1..16 part
+            const int32_t *l16 = d_list + n_p8;
+            int32_t *r16 = d_rlist + n_p8;
+            const int n_hi = (int)(kcnt[(size_t)(kKeys8 + 16 * kLenBins - 1)] - n_p8), n16 = (int)n_p16;
+            if ((rc = bsb_cuda(ctx, sw_pack16_run_hi(false, P16, d_jobs, d_seq, l16, n_hi, d_boff, d_b, d_out, d_rsl,
+                                                     ctr16, 0, ctx->n_sm, st2), "SW word-lane kernels")) ||
+                (rc = bsb_cuda(ctx, sw_pack16_run_lo(false, P16, d_jobs, d_seq, l16 + n_hi, n16 - n_hi, d_boff, d_b,
+                                                     d_out, d_rsl, ctr16, 1, ctx->n_sm, st2), "SW word-lane kernels")))
+                return rc;
+            sw_rev_scatter<kPackMaxSeg16><<<(int)std::min<int64_t>((n16 + 255) / 256, (int64_t)ctx->n_sm * 4), 256,
+                                            0, st2>>>(l16, n16, d_rsl, ctr16, r16);
+            if ((rc = bsb_cuda(ctx, sw_pack16_run_hi(true, P16, d_jobs, d_seq, r16, n16, d_boff, d_b, d_out, d_rsl,
+                                                     ctr16, 2, ctx->n_sm, st2), "SW word-lane kernels")) ||
+                (rc = bsb_cuda(ctx, sw_pack16_run_lo(true, P16, d_jobs, d_seq, r16, n16, d_boff, d_b, d_out, d_rsl,
+                                                     ctr16, 3, ctx->n_sm, st2), "SW word-lane kernels")))
+                return rc;
+        }
+        // shared memory per group: 4 int16 vectors + the striped query, slen*P entries each
+        const size_t sm8 = (size_t)(kSwBlock / 16) * (size_t)(S.slen8 * 16 * 9 + 16);
+        const size_t sm16 = (size_t)(kSwBlock / 8) * (size_t)(S.slen16 * 8 * 9 + 16);
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(sw_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(sw_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            attr_set = true;
+        }
+        const int blocks = ctx->n_sm * 16;
+        const int32_t *fb = d_list + n_p8 + n_p16;
+        if (n_fb8)
+            sw_kernel<16><<<(int)std::min<int64_t>(blocks, (n_fb8 + 3) / 4), kSwBlock, sm8, st2>>>(
+                S, d_jobs, d_seq, fb, (int)n_fb8, cnt + 0, d_boff, d_b, d_out);
+        if (n_fb16)
+            sw_kernel<8><<<(int)std::min<int64_t>(blocks, (n_fb16 + 7) / 8), kSwBlock, sm16, st2>>>(
+                S, d_jobs, d_seq, fb + n_fb8, (int)n_fb16, cnt + 1, d_boff, d_b, d_out);
+        if ((rc = bsb_cuda(ctx, cudaGetLastError(), "SW one-lane kernels")) ||
+            (rc = bsb_cuda(ctx, cudaEventRecord(ctx->ms.join[0], st2), "SW join")))
+            return rc;
     }
-    const int blocks = ctx->n_sm * 16;
-    if (max8 > 0)
-        sw_kernel<16><<<blocks, kSwBlock, sm8, st>>>(S, d_jobs, d_seq, list8, cnt + 0, cnt + 2, d_boff, d_b, d_out);
-    if (max16 > 0)
-        sw_kernel<8><<<blocks, kSwBlock, sm16, st>>>(S, d_jobs, d_seq, list16, cnt + 1, cnt + 3, d_boff, d_b, d_out);
-    if ((rc = bsb_cuda(ctx, cudaGetLastError(), "SW kernels"))) return rc;
+    if (n_p8) {        // byte lanes: forward passes, grouping by reversed segment count, reverse passes
+        const int n8 = (int)n_p8;
+        if ((rc = bsb_cuda(ctx, sw_pack_run<16, 1, kPackMaxSeg8, kPackMaxSeg8>(false, P8, d_jobs, d_seq, d_list, n8,
+                                                                               d_boff, d_b, d_out, d_rsl, ctr8, 0,
+                                                                               ctx->n_sm, st), "SW byte-lane kernels")))
+            return rc;
+        sw_rev_scatter<kPackMaxSeg8><<<(int)std::min<int64_t>((n8 + 255) / 256, (int64_t)ctx->n_sm * 4), 256, 0,
+                                       st>>>(d_list, n8, d_rsl, ctr8, d_rlist);
+        if ((rc = bsb_cuda(ctx, sw_pack_run<16, 1, kPackMaxSeg8, kPackMaxSeg8>(true, P8, d_jobs, d_seq, d_rlist, n8,
+                                                                               d_boff, d_b, d_out, d_rsl, ctr8, 1,
+                                                                               ctx->n_sm, st), "SW byte-lane kernels")))
+            return rc;
+    }
+    if (side && (rc = bsb_cuda(ctx, cudaStreamWaitEvent(st, ctx->ms.join[0], 0), "SW join"))) return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out, d_out, sizeof(bsb_kswr_t) * n, cudaMemcpyDeviceToHost, st), "D2H")))
         return rc;
     return bsb_cuda(ctx, cudaStreamSynchronize(st), "SW batch");

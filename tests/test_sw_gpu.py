@@ -69,3 +69,18 @@ def test_align2_errors(gpu_ctx):
     out = matesw.align2_batch(gpu_ctx, jobs, seq, mat, 6, 1, 6, 1)
     ref = oracle.align2_batch(jobs, seq, mat, 6, 1, 6, 1)
     assert_same(out, ref, None, "after errors")
+
+
+@pytest.mark.parametrize("scoring", [(2, 3, 5, 2, 7, 1), (1, 4, 0, 1, 0, 1), (1, 4, 6, 0, 6, 0),
+                                     (1, 4, 6, 1, 250, 10), (2, 3, 255, 255, 255, 255), (5, 3, 100, 50, 120, 60),
+                                     (1, 4, 20000, 9000, 30000, 3000)])
+def test_align2_scorings_match_oracle(gpu_ctx, scoring):
+    """Other scorings: asymmetric, zero open or extension penalties, byte-lane penalties that
+    wrap (o + e >= 256: the one-lane kernels keep the reference's lazy-F loop), penalties that
+    keep word lanes off the 16-bit path."""
+    a, b, o_del, e_del, o_ins, e_ins = scoring
+    jobs, seq, tags = golden_data.golden_sw_jobs(a, n=2500, seed=20261203 + 60 + a + o_ins)
+    mat = synth.fill_scmat(a, b)
+    out = matesw.align2_batch(gpu_ctx, jobs.view(matesw.JOB_DTYPE), seq, mat, o_del, e_del, o_ins, e_ins)
+    ref = oracle.align2_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, n_threads=8)
+    assert_same(out, ref, tags, f"scoring {scoring}")
