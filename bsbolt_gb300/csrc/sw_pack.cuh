@@ -11,8 +11,8 @@
 //   P = 8, word lanes (ksw_i16): the same instructions with signed scores, for jobs whose scores
 //     cannot reach the reference's 16-bit saturation (qlen * max score <= 32640) and whose
 //     penalties stay below 32768, so that 16-bit arithmetic without saturation is exact.
-// A job's H and E vectors and its query-profile selectors are register arrays of its exact
-// segment count SL (a template argument); the row's scores come from two profile words of its
+// A job's H and E vectors and its query-profile selectors are register arrays sized by its
+// segment count's bucket (below); the row's scores come from two profile words of its
 // target base by one byte permute per pair of cells.  The lazy-F loop runs in closed form (see
 // pack_pass).  The groups of a warp take consecutive jobs of a list sorted by segment count, so
 // they run the same code for about as many rows.
@@ -74,23 +74,33 @@ __device__ __forceinline__ uint32_t lane_up(uint32_t x, int tid, unsigned gm)   
 __device__ __forceinline__ int grp_max(unsigned gm, int v) { return (int)__reduce_max_sync(gm, (unsigned)v); }
 __device__ __forceinline__ int grp_min(unsigned gm, int v) { return (int)__reduce_min_sync(gm, (unsigned)v); }
 
-// One ksw_u8 (P = 16) or ksw_i16 (P = 8) pass of a group of P/2 threads on SL segments.
-// hm: the thread's Hmax slots (stride kPackBlock); bbuf: the suboptimal rows (KSW_XSUBO only).
-template <int P, int SL>
-__device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *plo, const uint32_t *phi, int qlen,
-                                          int tlen, const SwSeq &a, int xtra, uint32_t *hm, int2 *bbuf, int tid,
-                                          unsigned gm)
+// Segment counts per pass instance: a bucket of B consecutive counts (SLMAX - B, SLMAX] shares
+// one instance, the exact count sl a runtime value: the striping uses sl, segments at and past
+// sl are skipped (only the last B - 1 of the instance's segments test it).  Eight byte-lane and
+// four word-lane instances keep the code the SMs run at one time small: with one instance per
+// count, instruction fetch was the kernel's main stall.
+template <int P>
+constexpr int kSegBucket = P == 16 ? 2 : 8;
+
+// One ksw_u8 (P = 16) or ksw_i16 (P = 8) pass of a group of P/2 threads on sl segments,
+// SLMAX - kSegBucket < sl <= SLMAX.  hm: the thread's Hmax slots (stride kPackBlock); bbuf: the
+// suboptimal rows (KSW_XSUBO only).
+template <int P, int SLMAX>
+__device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *plo, const uint32_t *phi, int sl,
+                                          int qlen, int tlen, const SwSeq &a, int xtra, uint32_t *hm, int2 *bbuf,
+                                          int tid, unsigned gm)
 {
     constexpr bool U8 = P == 16;
-    constexpr int G = P / 2;
+    constexpr int G = P / 2, SLMIN = SLMAX - kSegBucket<P> + 1;    // segments below SLMIN always exist
     const uint32_t nshift = S.nshift, npe_del = S.npe_del, npoe_del = S.npoe_del, npe_ins = S.npe_ins,
                    npoe_ins = S.npoe_ins;
     const int shift = S.shift, pe_ins = S.pe_ins;
-    uint32_t sel[SL], H[SL], E[SL];
+    uint32_t sel[SLMAX], H[SLMAX], E[SLMAX];
 #pragma unroll
-    for (int j = 0; j < SL; ++j) {                 // ksw_qinit's striping; the vectors start at zero
-        const int c0 = j + tid * SL, c1 = j + (tid + G) * SL;
-        const uint32_t x = c0 < qlen ? (uint32_t)a.qc(c0) : 5u, y = c1 < qlen ? (uint32_t)a.qc(c1) : 5u;
+    for (int j = 0; j < SLMAX; ++j) {              // ksw_qinit's striping; the vectors start at zero
+        const int c0 = j + tid * sl, c1 = j + (tid + G) * sl;
+        const bool in = j < sl;
+        const uint32_t x = in && c0 < qlen ? (uint32_t)a.qc(c0) : 5u, y = in && c1 < qlen ? (uint32_t)a.qc(c1) : 5u;
         // bytes: score(x), 0 or its sign, score(y), 0 or its sign
         sel[j] = U8 ? (x | 0x60u | y << 8 | 0x6000u) : (x | (x | 8u) << 4 | y << 8 | (y | 8u) << 12);
         H[j] = 0, E[j] = 0;
@@ -100,39 +110,41 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
     const int endsc = (xtra & kXStop) ? xtra & 0xffff : 0x10000;
     int gmax = 0, te = -1, n_b = 0, last_row = -2, last_sc = 0;
     int tc = tlen > 0 ? a.tc(0) : 0;
+    uint32_t hlast = 0;                            // H of segment sl - 1 in the previous row
     for (int i = 0; i < tlen; ++i) {
         const int tn = i + 1 < tlen ? a.tc(i + 1) : 0;
         const uint32_t xlo = plo[tc], xhi = phi[tc];
-        uint32_t h = lane_up<G>(H[SL - 1], tid, gm), f = 0, mx = 0;      // H(i-1, -1), ksw.c:141-142
+        uint32_t h = lane_up<G>(hlast, tid, gm), f = 0, mx = 0;          // H(i-1, -1), ksw.c:141-142
         // H = max(a, E, f), a = the diagonal plus the score (ksw.c:149-153); the next f is
         // max(relu(f - e_ins), relu(H - oe_ins)) = max(relu(f - e_ins), relu(max(a, E) - oe_ins)), as
         // relu(f - oe_ins) <= relu(f - e_ins): one instruction per segment on the f chain
 #pragma unroll
-        for (int j = 0; j < SL; ++j) {
-            const uint32_t s = prmt(xlo, xhi, sel[j]);
-            const uint32_t ae = U8 ? __viaddmax_s16x2(__viaddmin_s16x2(h, s, 0x00ff00ffu), nshift, E[j])
-                                   : __viaddmax_s16x2(h, s, E[j]);
-            const uint32_t fo = __viaddmax_s16x2(ae, npoe_ins, 0u);
-            const uint32_t hv = __vimax_s16x2_relu(ae, f);
-            f = __viaddmax_s16x2(f, npe_ins, fo);
-            mx = __vimax_s16x2_relu(mx, hv);
-            E[j] = __viaddmax_s16x2(E[j], npe_del, __viaddmax_s16x2(hv, npoe_del, 0u));
-            h = H[j];
-            H[j] = hv;
-        }
+        for (int j = 0; j < SLMAX; ++j)
+            if (j < SLMIN || j < sl) {
+                const uint32_t s = prmt(xlo, xhi, sel[j]);
+                const uint32_t ae = U8 ? __viaddmax_s16x2(__viaddmin_s16x2(h, s, 0x00ff00ffu), nshift, E[j])
+                                       : __viaddmax_s16x2(h, s, E[j]);
+                const uint32_t fo = __viaddmax_s16x2(ae, npoe_ins, 0u);
+                const uint32_t hv = __vimax_s16x2_relu(ae, f);
+                f = __viaddmax_s16x2(f, npe_ins, fo);
+                mx = __vimax_s16x2_relu(mx, hv);
+                E[j] = __viaddmax_s16x2(E[j], npe_del, __viaddmax_s16x2(hv, npoe_del, 0u));
+                h = H[j];
+                H[j] = hv;
+            }
         {   // lazy F (ksw.c:166-177, 284-295).  The reference shifts f up one lane per round and
             // sweeps the segments until no lane can raise an H any more.  The sweep raises H(l, j)
             // to relu(G(l) - j*e_ins) at most, where G(l) is the F arriving at lane l's first
-            // column: G(0) = 0, G(l) = max(x(l), relu(G(l-1) - SL*e_ins)), x(l) the f leaving lane
+            // column: G(0) = 0, G(l) = max(x(l), relu(G(l-1) - sl*e_ins)), x(l) the f leaving lane
             // l-1; its early exit (Farrar's) leaves out only updates that change nothing.  So: the
             // reference's own first test, and where a lane fails it, G as a max-plus scan over the
             // lanes (the group's threads, then the low lanes into the high ones) and one max per
-            // segment, without a vote per segment.
+            // segment, without a vote per segment.  (Segments past sl take values nothing reads.)
             const uint32_t x = lane_up<G>(f, tid, gm);
             const uint32_t h0 = __vimax_s16x2_relu(H[0], x);
             const uint32_t hh = __viaddmax_s16x2(h0, npoe_ins, 0u), fn = __viaddmax_s16x2(x, npe_ins, 0u);
             if (__any_sync(gm, __vimax_s16x2_relu(fn, hh) != hh)) {
-                const int d = pe_ins * SL;
+                const int d = pe_ins * sl;
                 uint32_t g = x;
 #pragma unroll
                 for (int o = 1; o < G; o <<= 1) {
@@ -142,7 +154,7 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
                 const int gl = (int)(__shfl_sync(gm, g, G - 1, G) & 0xffffu);
                 g = __vimax_s16x2_relu(g, (uint32_t)max(gl - d * (tid + 1), 0) << 16);
 #pragma unroll
-                for (int j = 0; j < SL; ++j) {
+                for (int j = 0; j < SLMAX; ++j) {
                     H[j] = __vimax_s16x2_relu(H[j], g);
                     g = __viaddmax_s16x2(g, npe_ins, 0u);
                 }
@@ -150,6 +162,10 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
                 H[0] = h0;
             }
         }
+        hlast = H[SLMIN - 1];
+#pragma unroll
+        for (int j = SLMIN; j < SLMAX; ++j)
+            if (j == sl - 1) hlast = H[j];
         const int imax = grp_max(gm, max((int)(mx & 0xffffu), (int)(mx >> 16)));
         if (imax > gmax || imax >= minsc) {
             if (imax >= minsc) {                  // the rows of the suboptimal score (ksw.c:182-189)
@@ -164,7 +180,7 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
             if (imax > gmax) {
                 gmax = imax, te = i;
 #pragma unroll
-                for (int j = 0; j < SL; ++j) hm[j * kPackBlock] = H[j];
+                for (int j = 0; j < SLMAX; ++j) hm[j * kPackBlock] = H[j];
                 if ((U8 && gmax + shift >= 255) || gmax >= endsc) break;
             }
         }
@@ -176,10 +192,10 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
     r.te = te, r.qe = -1, r.score2 = -1, r.te2 = -1;
     if (!U8 || r.score != 255) {
         int best = -1, col = 0x7fffffff;          // the smallest column holding the best Hmax value
-#pragma unroll
-        for (int j = 0; j < SL; ++j) {
+#pragma unroll 1
+        for (int j = 0; j < sl; ++j) {
             const uint32_t v = hm[j * kPackBlock];
-            const int v0 = (int)(v & 0xffffu), v1 = (int)(v >> 16), c0 = j + tid * SL, c1 = j + (tid + G) * SL;
+            const int v0 = (int)(v & 0xffffu), v1 = (int)(v >> 16), c0 = j + tid * sl, c1 = j + (tid + G) * sl;
             if (v0 > best || (v0 == best && c0 < col)) best = v0, col = c0;
             if (v1 > best || (v1 == best && c1 < col)) best = v1, col = c1;
         }
@@ -188,6 +204,7 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
         if (n_b) {                                 // ksw.c:218-225: the best row outside te +- d
             const int d = (r.score + S.qmax - 1) / S.qmax, low = te - d, high = te + d;
             int bs = -1, bk = 0x7fffffff;
+#pragma unroll 1
             for (int k = tid; k < n_b; k += G) {
                 const int2 e = bbuf[k];
                 if ((e.y < low || e.y > high) && e.x > bs) bs = e.x, bk = k;
@@ -200,18 +217,18 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
     return r;
 }
 
-// pack_pass<P, sl> for SL <= sl <= HI.  Each instance is a function of its own, so a kernel's
-// registers are those of its largest instance.
-template <int P, int SL, int HI>
+// pack_pass of the bucket holding sl, for buckets ending at SLMAX..HI (step kSegBucket<P>).
+// Each instance is a function of its own, so a kernel's registers are those of its largest.
+template <int P, int SLMAX, int HI>
 __device__ __forceinline__ PassOut pack_range(int sl, const PackParams &S, const uint32_t *plo, const uint32_t *phi,
                                               int qlen, int tlen, const SwSeq &a, int xtra, uint32_t *hm, int2 *bbuf,
                                               int tid, unsigned gm)
 {
-    if constexpr (SL >= HI) {
-        return pack_pass<P, HI>(S, plo, phi, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
+    if constexpr (SLMAX >= HI) {
+        return pack_pass<P, HI>(S, plo, phi, sl, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
     } else {
-        if (sl == SL) return pack_pass<P, SL>(S, plo, phi, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
-        return pack_range<P, SL + 1, HI>(sl, S, plo, phi, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
+        if (sl <= SLMAX) return pack_pass<P, SLMAX>(S, plo, phi, sl, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
+        return pack_range<P, SLMAX + kSegBucket<P>, HI>(sl, S, plo, phi, qlen, tlen, a, xtra, hm, bbuf, tid, gm);
     }
 }
 
@@ -259,7 +276,8 @@ sw_pack_kernel(PackParams S, const bsb_sw_job_t *__restrict__ jobs, const uint8_
             const uint8_t *qp = seq + jb.qoff, *tp = seq + jb.toff;
             if (!REV) {
                 const SwSeq a{qp, tp, -1, -1};
-                const PassOut r = pack_range<P, LO, HI>((jb.qlen + P - 1) / P, S, plo, phi, jb.qlen, jb.tlen, a,
+                constexpr int B0 = LO + kSegBucket<P> - 1;
+                const PassOut r = pack_range<P, B0, HI>((jb.qlen + P - 1) / P, S, plo, phi, jb.qlen, jb.tlen, a,
                                                         jb.xtra, hm, bscratch + boff[id], tid, gm);
                 const bool start = (jb.xtra & kXStart) && !((jb.xtra & kXSubo) && r.score < (jb.xtra & 0xffff));
                 if (tid == 0) {
@@ -275,7 +293,8 @@ sw_pack_kernel(PackParams S, const bsb_sw_job_t *__restrict__ jobs, const uint8_
             } else {
                 const bsb_kswr_t o = out[id];
                 const SwSeq a{qp, tp, o.qe, o.te};
-                const PassOut rr = pack_range<P, LO, HI>((o.qe + P) / P, S, plo, phi, o.qe + 1, jb.tlen, a,
+                constexpr int B0 = LO + kSegBucket<P> - 1;
+                const PassOut rr = pack_range<P, B0, HI>((o.qe + P) / P, S, plo, phi, o.qe + 1, jb.tlen, a,
                                                          kXStop | o.score, hm, nullptr, tid, gm);
                 if (tid == 0 && rr.score == o.score) out[id].tb = o.te - rr.te, out[id].qb = o.qe - rr.qe;
             }
