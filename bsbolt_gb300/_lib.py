@@ -32,6 +32,7 @@ EXPORTS = (
     "bsb_probe_int_peak", "bsb_probe_int16x2_peak",
     "bsb_index_upload", "bsb_index_load", "bsb_seed_batch", "bsb_seed_batch_device",
     "bsb_sa_batch", "bsb_sa_batch_device", "bsb_extend_batch_noalloc", "bsb_align_regs_batch",
+    "bsb_mem_align1_batch",
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
     "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
     "bsb_index_upload_opac", "bsb_gen_cigar_batch", "bsb_align2_batch",
@@ -76,7 +77,7 @@ class AlignOpt(ctypes.Structure):
                                                "max_chain_gap", "min_chain_weight", "max_chain_extend")] + \
                [("mask_level", ctypes.c_float), ("drop_ratio", ctypes.c_float), ("split_factor", ctypes.c_float),
                 ("split_width", ctypes.c_int32), ("max_mem_intv", ctypes.c_int32),
-                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3)]
+                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3), ("mask_level_redun", ctypes.c_float)]
 
     @classmethod
     def bwa_defaults(cls, a=1, b=4, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, zdrop=100, pen_clip5=5,
@@ -85,7 +86,8 @@ class AlignOpt(ctypes.Structure):
         o = cls(a=a, b=b, o_del=o_del, e_del=e_del, o_ins=o_ins, e_ins=e_ins, w=w, zdrop=zdrop,
                 pen_clip5=pen_clip5, pen_clip3=pen_clip3, min_seed_len=min_seed_len, max_occ=max_occ,
                 max_chain_gap=max_chain_gap, min_chain_weight=0, max_chain_extend=1 << 30, mask_level=0.5,
-                drop_ratio=0.5, split_factor=1.5, split_width=split_width, max_mem_intv=max_mem_intv)
+                drop_ratio=0.5, split_factor=1.5, split_width=split_width, max_mem_intv=max_mem_intv,
+                mask_level_redun=0.95)
         for i in range(5):
             for j in range(5):
                 o.mat[i * 5 + j] = -1 if (i == 4 or j == 4) else (a if i == j else -b)
@@ -141,6 +143,8 @@ def load(path: str = LIB_PATH):
     L.bsb_extend_batch_noalloc.restype = I32
     L.bsb_align_regs_batch.argtypes = [P, P, ctypes.c_int32, P, P, P, I64, P]
     L.bsb_align_regs_batch.restype = I32
+    L.bsb_mem_align1_batch.argtypes = [P, P, ctypes.c_int32, P, P, P, I64, P]
+    L.bsb_mem_align1_batch.restype = I32
     L.bsb_cost_features.argtypes = [P, P, I64, P, I64, P]
     L.bsb_cost_features.restype = I32
     L.bsb_mlp_forward.argtypes = [P, P, P, I64, P, P]

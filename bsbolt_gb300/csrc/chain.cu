@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "bsb_internal.cuh"
+#include "ksw_global.cuh"
 #include "fm_index.cuh"
 #include "ksw_core.cuh"
 #include "scan.cuh"
@@ -225,12 +226,12 @@ struct Bt {
     }
 };
 
-// ks_introsort over chain indices with the comparison w[a] > w[b] (ksort.h:146-226):
-// restated step for step, since chains of equal weight keep the order it leaves.
-struct FltSort {
+// ks_introsort (ksort.h:146-226) over an index array with the comparison lt(x, y):
+// restated step for step, since records that compare equal keep the order it leaves.
+template <class Lt>
+struct KsSort {
     int *a;
-    const int *w;
-    __device__ bool lt(int x, int y) const { return w[x] > w[y]; }
+    Lt lt;
     __device__ void insertsort(int s, int t)
     {
         for (int i = s + 1; i < t; ++i)
@@ -302,6 +303,12 @@ struct FltSort {
             }
         }
     }
+};
+
+// mem_chain_flt's order: chain weight, descending (bwamem.c:328-329)
+struct FltLt {
+    const int *w;
+    __device__ bool operator()(int x, int y) const { return w[x] > w[y]; }
 };
 
 // One thread per read.  Per-read scratch is carved from arrays sized by the
@@ -466,7 +473,7 @@ chain_kernel(AlnOpt opt, DevBns B, int n_reads, const int64_t *__restrict__ read
         if (n == 0) continue;
         {
             int stk_l[64], stk_r[64], stk_d[64];
-            FltSort fs{order, wgt};
+            KsSort<FltLt> fs{order, FltLt{wgt}};
             fs.sort(n, stk_l, stk_r, stk_d);
         }
         DevChain *oc = out_chains + R0;              // working copy, compacted at the end
@@ -768,6 +775,219 @@ __global__ void compact_regs(const bsb_reg_t *__restrict__ regs, const int64_t *
     }
 }
 
+// ---------------------------------------------------------------- mem_sort_dedup_patch
+
+struct RegReLt {                      // alnreg_slt2 (bwamem.c:395): by end
+    const bsb_reg_t *r;
+    __device__ bool operator()(int x, int y) const { return r[x].re < r[y].re; }
+};
+
+struct RegScoreLt {                   // alnreg_slt (bwamem.c:398): score down, then rb, qb up
+    const bsb_reg_t *r;
+    __device__ bool operator()(int x, int y) const
+    {
+        const bsb_reg_t &a = r[x], &b = r[y];
+        return a.score > b.score || (a.score == b.score && (a.rb < b.rb || (a.rb == b.rb && a.qb < b.qb)));
+    }
+};
+
+struct DedupOpt {
+    int w, max_chain_gap;
+    float mask_level_redun;
+    GlobalPen pen;
+    int8_t mat[25];
+};
+
+constexpr int kDedupWarps = 4;
+
+struct DedupSmem {                    // one warp's global alignment of mem_patch_reg
+    int32_t H[BSB_ALIGN_MAX_LEN + 1], E[BSB_ALIGN_MAX_LEN + 1];
+    uint8_t q[BSB_ALIGN_MAX_LEN];
+};
+
+// Target base i of [rb, re) after bwa_gen_cigar2's flip (bwa.c:216-221): read backwards on the
+// reverse strand.
+struct PatchText {
+    DevBns B;
+    int64_t rb, re;
+    bool rev;
+    __device__ __forceinline__ int operator[](int i) const { return text_base(B, rev ? re - 1 - i : rb + i); }
+};
+
+// mem_patch_reg (bwamem.c:410-439) on the warp: every lane takes the same steps; the global
+// alignment of its bwa_gen_cigar2 call (score only, bwa.c:211-244) runs on the whole warp.  The
+// reference's double expressions are evaluated as written (no fused multiply-adds).
+__device__ int patch_reg_warp(const DedupOpt &O, const int8_t *smat, const DevBns &B, const uint8_t *read,
+                              const bsb_reg_t &a, const bsb_reg_t &b, int *w_out, DedupSmem &S, int lane)
+{
+    const int64_t l_pac = B.l_pac;
+    if (a.rb < l_pac && b.rb >= l_pac) return 0;                       // different strands
+    if (a.qb >= b.qb || a.qe >= b.qe || a.re >= b.re) return 0;       // not colinear
+    int w = (int)((a.re - b.rb) - (a.qe - b.qb));
+    w = w > 0 ? w : -w;
+    double r = __dsub_rn(__ddiv_rn((double)(a.re - b.rb), (double)(b.re - a.rb)),
+                         __ddiv_rn((double)(a.qe - b.qb), (double)(b.qe - a.qb)));
+    r = r > 0. ? r : -r;
+    if (a.re < b.rb || a.qe < b.qb) {
+        if (w > O.w << 1 || r >= (double)0.05f) return 0;              // PATCH_MAX_R_BW
+    } else if (w > O.w << 2 || r >= (double)(0.05f * 2)) return 0;
+    w += a.w + b.w;
+    w = w < O.w << 2 ? w : O.w << 2;
+    // bwa_gen_cigar2(..., w, l_pac, pac, pac, b.qe - a.qb, query + a.qb, a.rb, b.re, &score, 0, ...)
+    const int lq = b.qe - a.qb;
+    const int64_t rb = a.rb, re = b.re;
+    int score = 0;
+    if (!(lq <= 0 || rb >= re || (rb < l_pac && re > l_pac)) && rb >= 0 && re <= l_pac << 1) {
+        const bool rev = rb >= l_pac;
+        const int rlen = (int)(re - rb);
+        for (int j = lane; j < lq; j += 32) S.q[j] = read[rev ? b.qe - 1 - j : a.qb + j];
+        __syncwarp();
+        const PatchText T{B, rb, re, rev};
+        if (lq == rlen && w == 0) {                                    // ungapped (bwa.c:222-230)
+            int part = 0;
+            for (int j = lane; j < lq; j += 32) part += smat[T[j] * 5 + S.q[j]];
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(BSB_FULL_MASK, part, d);
+            score = part;
+        } else {                                                       // the band of bwa.c:232-240
+            const int half = ((lq + 1) >> 1) * smat[0];
+            const int max_ins = (int)__dadd_rn(__ddiv_rn((double)(half - O.pen.o_ins), (double)O.pen.e_ins), 1.);
+            const int max_del = (int)__dadd_rn(__ddiv_rn((double)(half - O.pen.o_del), (double)O.pen.e_del), 1.);
+            int max_gap = max_ins > max_del ? max_ins : max_del;
+            max_gap = max_gap > 1 ? max_gap : 1;
+            const int dl = rlen > lq ? rlen - lq : lq - rlen;
+            int bw = (max_gap + dl + 1) >> 1;
+            bw = bw < w ? bw : w;
+            bw = bw > dl + 3 ? bw : dl + 3;
+            score = global_rows_warp(O.pen, smat, S.q, lq, T, rlen, bw, 0, S.H, S.E, nullptr, lane);
+        }
+        __syncwarp();
+    }
+    const int sc2 = b.score + a.score;
+    const int q_s = (int)__dadd_rn(__dmul_rn(__ddiv_rn((double)(b.qe - a.qb), (double)((b.qe - b.qb) + (a.qe - a.qb))),
+                                             (double)sc2), .499);
+    const int r_s = (int)__dadd_rn(__dmul_rn(__ddiv_rn((double)(b.re - a.rb), (double)((b.re - b.rb) + (a.re - a.rb))),
+                                             (double)sc2), .499);
+    if (__ddiv_rn((double)score, (double)(q_s > r_s ? q_s : r_s)) < (double)0.90f) return 0;   // PATCH_MIN_SC_RATIO
+    *w_out = w;
+    return score;
+}
+
+// mem_sort_dedup_patch (bwamem.c:441-493) per read, one warp per read.  in: the read's
+// pre-dedup regions at reg_off[r]; a: scratch of the same size (the sorted copy that the scan
+// edits); ix: index scratch; out: the kept regions at reg_off[r], n_out[r] of them.  Lane 0 runs
+// the two ks_introsort orders; the redundancy and merge scan is taken by every lane in step
+// (lane 0 writes), so that the warp can run a merge's global alignment.
+__global__ void __launch_bounds__(kDedupWarps * 32)
+dedup_kernel(DedupOpt O, DevBns B, int n_reads, const uint8_t *__restrict__ reads,
+             const int64_t *__restrict__ read_off, const int64_t *__restrict__ reg_off,
+             const bsb_reg_t *__restrict__ in, bsb_reg_t *a_all, int *ix_all, bsb_reg_t *__restrict__ out,
+             int *__restrict__ n_out)
+{
+    __shared__ DedupSmem sm[kDedupWarps];
+    __shared__ int8_t smat[25];
+    if (threadIdx.x < 25) smat[threadIdx.x] = O.mat[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    for (int r = blockIdx.x * kDedupWarps + wb; r < n_reads; r += gridDim.x * kDedupWarps) {
+        const int64_t o0 = reg_off[r];
+        const int n = (int)(reg_off[r + 1] - o0);
+        const bsb_reg_t *a_in = in + o0;
+        bsb_reg_t *a = a_all + o0, *dst = out + o0;
+        int *ix = ix_all + o0;
+        if (n <= 1) {                                    // bwamem.c:444: returned as they are
+            if (lane == 0) {
+                if (n == 1) dst[0] = a_in[0];
+                n_out[r] = n;
+            }
+            continue;
+        }
+        if (lane == 0) {                                 // sort by end (bwamem.c:445)
+            int stk_l[64], stk_r[64], stk_d[64];
+            for (int k = 0; k < n; ++k) ix[k] = k;
+            KsSort<RegReLt>{ix, RegReLt{a_in}}.sort(n, stk_l, stk_r, stk_d);
+        }
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) {
+            a[k] = a_in[ix[k]];
+            a[k].n_comp = 1;
+        }
+        __syncwarp();
+        const uint8_t *read = reads + read_off[r];
+        for (int i = 1; i < n; ++i) {                    // bwamem.c:447-474
+            bsb_reg_t p = a[i];
+            if (p.rid != a[i - 1].rid || p.rb >= a[i - 1].re + O.max_chain_gap) continue;
+            for (int j = i - 1; j >= 0 && p.rid == a[j].rid && p.rb < a[j].re + O.max_chain_gap; --j) {
+                const bsb_reg_t q = a[j];
+                if (q.qe == q.qb) continue;                      // a[j] has been excluded
+                const int64_t or_ = q.re - p.rb;
+                const int64_t oq = q.qb < p.qb ? q.qe - p.qb : p.qe - q.qb;
+                const int64_t mr = q.re - q.rb < p.re - p.rb ? q.re - q.rb : p.re - p.rb;
+                const int64_t mq = q.qe - q.qb < p.qe - p.qb ? q.qe - q.qb : p.qe - p.qb;
+                // float, as the reference's float option times an int64
+                if ((float)or_ > __fmul_rn(O.mask_level_redun, (float)mr) &&
+                    (float)oq > __fmul_rn(O.mask_level_redun, (float)mq)) {
+                    if (p.score < q.score) {
+                        if (lane == 0) a[i].qe = p.qb;
+                        __syncwarp();
+                        break;
+                    }
+                    if (lane == 0) a[j].qe = q.qb;
+                    __syncwarp();
+                } else if (q.rb < p.rb) {
+                    int w = 0;
+                    const int score = patch_reg_warp(O, smat, B, read, q, p, &w, sm[wb], lane);
+                    if (score > 0) {                             // merge q into p
+                        if (lane == 0) {
+                            p.n_comp += q.n_comp + 1;
+                            p.seedcov = p.seedcov > q.seedcov ? p.seedcov : q.seedcov;
+                            p.qb = q.qb, p.rb = q.rb;
+                            p.truesc = p.score = score;
+                            p.w = w;
+                            a[i] = p;
+                            a[j].qb = q.qe;
+                        }
+                        __syncwarp();
+                        p = a[i];
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {                                 // bwamem.c:475-492
+            int m = 0;
+            for (int k = 0; k < n; ++k)
+                if (a[k].qe > a[k].qb) ix[m++] = k;
+            int cnt;
+            if (m == 0) {                                // the reference then returns its first region
+                dst[0] = a[0];
+                cnt = 1;
+            } else {
+                int stk_l[64], stk_r[64], stk_d[64];
+                KsSort<RegScoreLt>{ix, RegScoreLt{a}}.sort(m, stk_l, stk_r, stk_d);
+                dst[0] = a[ix[0]];
+                cnt = 1;
+                for (int k = 1; k < m; ++k) {
+                    const bsb_reg_t &x = a[ix[k]], &y = a[ix[k - 1]];
+                    if (!(x.score == y.score && x.rb == y.rb && x.qb == y.qb)) dst[cnt++] = x;
+                }
+            }
+            n_out[r] = cnt;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void compact_kept(const bsb_reg_t *__restrict__ regs, const int64_t *__restrict__ in_off, int n_reads,
+                             const int *__restrict__ n_kept, const int64_t *__restrict__ out_off,
+                             bsb_reg_t *__restrict__ out)
+{
+    for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
+        const bsb_reg_t *src = regs + in_off[r];
+        for (int i = threadIdx.x; i < n_kept[r]; i += blockDim.x) out[out_off[r] + i] = src[i];
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host driver
@@ -789,9 +1009,10 @@ struct AlignScratch {
 
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// dedup: also run mem_sort_dedup_patch per read (the regions mem_align1_core returns).
 static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_reads, const uint8_t *d_reads,
                        const int64_t *d_read_off, const bsb_intv_t *d_seeds, const int64_t *d_seed_off,
-                       int64_t n_seeds, int max_len, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out,
+                       int64_t n_seeds, int max_len, bool dedup, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out,
                        int64_t *n_regs_total)
 {
     int rc;
@@ -830,6 +1051,9 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     const size_t o_ctrl = off; off += al(sizeof(int) * 4);
     const size_t o_regoff = off; off += al(sizeof(int64_t) * (n_reads + 1));
     const size_t o_out = off; off += al(sizeof(bsb_reg_t) * Rb);
+    const size_t o_dtmp = off; off += dedup ? al(sizeof(bsb_reg_t) * Rb) : 0;
+    const size_t o_dn = off; off += dedup ? al(sizeof(int) * (n_reads + 1)) : 0;
+    const size_t o_doff = off; off += dedup ? al(sizeof(int64_t) * (n_reads + 1)) : 0;
     if ((rc = bsb_ensure(ctx, &ctx->arena1, &ctx->arena1_bytes, off, "chain scratch"))) return rc;
     char *A = (char *)ctx->arena1;
     uint64_t *rows = (uint64_t *)(A + o_rows), *pos = (uint64_t *)(A + o_pos);
@@ -884,6 +1108,23 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
                                                              cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
     if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
     compact_regs<<<ctx->n_sm * 4, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
+    if (dedup) {
+        // mem_sort_dedup_patch: regs_out (pre-dedup, at reg_off) -> regs (kept, at reg_off,
+        // n_kept per read) -> regs_out again, compacted at the new offsets
+        DedupOpt D;
+        D.w = o->w, D.max_chain_gap = o->max_chain_gap, D.mask_level_redun = o->mask_level_redun;
+        D.pen = GlobalPen{o->o_del, o->e_del, o->o_ins, o->e_ins};
+        memcpy(D.mat, o->mat, 25);
+        bsb_reg_t *dtmp = (bsb_reg_t *)(A + o_dtmp);
+        int *n_kept = (int *)(A + o_dn);
+        int64_t *kept_off = (int64_t *)(A + o_doff);
+        const int db = (int)((n_reads + kDedupWarps - 1) / kDedupWarps);
+        dedup_kernel<<<db < ctx->n_sm * 8 ? db : ctx->n_sm * 8, kDedupWarps * 32, 0, st>>>(
+            D, B, n_reads, d_reads, d_read_off, reg_off, regs_out, dtmp, iwork, regs, n_kept);
+        if ((rc = bsb_cuda(ctx, scan_i32_i64(n_kept, n_reads, kept_off, scan_tmp, st), "kept offsets"))) return rc;
+        compact_kept<<<ctx->n_sm * 4, 128, 0, st>>>(regs, reg_off, n_reads, n_kept, kept_off, regs_out);
+        reg_off = kept_off;
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return bsb_cuda(ctx, e, "chain/extension launch");
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(n_regs_total, reg_off + n_reads, 8, cudaMemcpyDeviceToHost, st), "reg total")))
@@ -894,8 +1135,8 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     return 0;
 }
 
-extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
-                                    const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                       const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off, bool dedup)
 {
     if (!ctx) return BSB_EINVAL;
     if (!ctx->has_index || !ctx->idx_pac || !ctx->idx_ann_off)
@@ -959,8 +1200,8 @@ extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
     if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
     bsb_reg_t *d_regs = nullptr;
     int64_t *d_reg_off = nullptr, n_regs = 0;
-    if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, &d_regs, &d_reg_off,
-                                 &n_regs)))
+    if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, dedup, &d_regs,
+                                 &d_reg_off, &n_regs)))
         return rc;
     if (n_regs > max_regs)
         return bsb_fail(ctx, BSB_EINVAL, "%lld regions do not fit max_regs %lld", (long long)n_regs, (long long)max_regs);
@@ -971,4 +1212,19 @@ extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
                        "D2H regions")))
         return rc;
     return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "align batch");
+}
+
+extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                                    const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    return align_batch(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, false);
+}
+
+extern "C" int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                                    const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (o && !(o->mask_level_redun >= 0.f && o->mask_level_redun <= 1.f))
+        return bsb_fail(ctx, BSB_EINVAL, "mask_level_redun must lie in [0, 1]");
+    return align_batch(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, true);
 }

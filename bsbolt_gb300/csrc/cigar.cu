@@ -24,11 +24,11 @@
 #include <vector>
 
 #include "bsb_internal.cuh"
+#include "ksw_global.cuh"
 #include "scan.cuh"
 
 namespace {
 
-constexpr int kNegInf = -0x40000000;        // MINUS_INF, ksw.c:490
 constexpr int kCigarBlock = 128;
 constexpr int kCigarWarps = kCigarBlock / 32;
 constexpr int kUnit = 16;                   // scratch and slot sizes are counted in 16-byte units
@@ -123,75 +123,6 @@ __global__ void plan_kernel(CigarParams P, const bsb_cigar_job_t *__restrict__ j
         scratch_units[i] = p.reject ? 0 : (int)(p.scratch / kUnit);
         slot_units[i] = p.reject ? 0 : p.slot_units;
     }
-}
-
-// The DP rows of ksw_global2 (ksw.c:519-582) on staged sequences (qs, ts after the strand
-// flip), one warp: row i is processed 32 columns at a time, one column per lane.  At the
-// start of cell j the reference holds eh[j] = {H(i-1, j-1), E(i, j)} and f = F(i, j); F
-// depends only on the row's M values (F(i, j+1) = max(M(i, j) - oe_ins, F(i, j) - e_ins),
-// F(i, beg) = -inf), so the lanes get it from a max-plus prefix scan -- max commutes with
-// subtracting a constant, so the values are the reference's exactly -- and everything
-// else in a cell is local.  H / E: qlen + 1 entries each (the reference's eh); Z: tlen
-// rows of `stride` direction bytes.  Returns the score on every lane.
-__device__ __forceinline__ int global_rows_warp(const CigarParams &P, const int8_t *smat, const uint8_t *qs, int qlen,
-                                const uint8_t *ts, int tlen, int w, int stride, int32_t *H, int32_t *E, uint8_t *Z,
-                                int lane)
-{
-    const int oe_del = P.o_del + P.e_del, oe_ins = P.o_ins + P.e_ins, e_ins = P.e_ins;
-    for (int j = lane; j <= qlen; j += 32) {
-        H[j] = j == 0 ? 0 : j <= w ? -(P.o_ins + e_ins * j) : kNegInf;
-        E[j] = kNegInf;
-    }
-    __syncwarp();
-    for (int i = 0; i < tlen; ++i) {
-        const int8_t *srow = smat + ts[i] * 5;
-        const int beg = i > w ? i - w : 0, end = i + w + 1 < qlen ? i + w + 1 : qlen;
-        int32_t f_carry = kNegInf;                                        // F(i, j0)
-        int32_t h_carry = beg == 0 ? -(P.o_del + P.e_del * (i + 1)) : kNegInf;   // H(i, j0 - 1)
-        uint8_t *zrow = Z + (size_t)i * stride;
-        if (beg >= end && lane == 0) H[end] = h_carry, E[end] = kNegInf;     // an empty row (not reached: w > |tlen - qlen|)
-        for (int j0 = beg; j0 < end; j0 += 32) {
-            const int j = j0 + lane;
-            const bool on = j < end;
-            int32_t m = kNegInf, e = kNegInf;
-            if (on) m = H[j] + srow[qs[j]], e = E[j];
-            // out_L = F(i, j0+L+1) = max(m_L - oe_ins, out_{L-1} - e_ins), out_{-1} = f_carry;
-            // with b_L = m_L - oe_ins + L*e_ins it is an inclusive max-scan shifted back
-            int32_t sc = on ? m - oe_ins + lane * e_ins : INT32_MIN / 2;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const int32_t v = __shfl_up_sync(BSB_FULL_MASK, sc, d);
-                if (lane >= d) sc = sc > v ? sc : v;
-            }
-            const int32_t c0 = f_carry - e_ins;                          // out_{-1}, normalised at L = -1
-            const int32_t out = (sc > c0 ? sc : c0) - lane * e_ins;      // F(i, j + 1)
-            int32_t f = __shfl_up_sync(BSB_FULL_MASK, out, 1);          // F(i, j)
-            if (lane == 0) f = f_carry;
-            int32_t h, t;
-            uint32_t dir;
-            if (m >= e) h = m, dir = 0;
-            else h = e, dir = 1;
-            if (h < f) h = f, dir = 2;
-            t = m - oe_del;
-            e -= P.e_del;
-            if (e > t) dir |= 1 << 2;
-            else e = t;
-            t = m - oe_ins;
-            if (f - e_ins > t) dir |= 2 << 4;
-            int32_t hprev = __shfl_up_sync(BSB_FULL_MASK, h, 1);        // H(i, j - 1)
-            if (lane == 0) hprev = h_carry;
-            if (on) {
-                H[j] = hprev;
-                E[j] = e;
-                zrow[j - beg] = (uint8_t)dir;
-                if (j == end - 1) H[end] = h, E[end] = kNegInf;
-            }
-            f_carry = __shfl_sync(BSB_FULL_MASK, out, 31);
-            h_carry = __shfl_sync(BSB_FULL_MASK, h, 31);
-        }
-        __syncwarp();
-    }
-    return H[qlen];
 }
 
 // The traceback of ksw_global2 (ksw.c:584-600), one thread: ops come out last-first, then
@@ -300,7 +231,8 @@ cigar_kernel(CigarParams P, const bsb_cigar_job_t *__restrict__ jobs, int n, con
             n_cigar = 1;
             if (lane == 0) cig[0] = (uint32_t)l << 4;
         } else {                              // ksw_global2: rows on the warp, traceback on lane 0
-            score = global_rows_warp(P, smat, qs, l, ts, rlen, p.w, p.stride, H, E, Z, lane);
+            score = global_rows_warp(GlobalPen{P.o_del, P.e_del, P.o_ins, P.e_ins}, smat, qs, l, ts, rlen, p.w, p.stride,
+                                     H, E, Z, lane);
             if (lane == 0) band_exit = !global_traceback(Z, l, rlen, p.w, p.stride, cig, n_cigar);
         }
         score = __shfl_sync(BSB_FULL_MASK, score, 0);

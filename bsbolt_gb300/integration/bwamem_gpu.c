@@ -23,10 +23,6 @@
 #include "ksw.h"
 #include "bwamem_gpu.h"
 
-/* defined in bwamem.c (bwamem.c:441), not declared in bwamem.h */
-int mem_sort_dedup_patch(const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac, uint8_t *query, int n,
-                         mem_alnreg_t *a);
-
 void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o)
 {
     memset(o, 0, sizeof(*o));
@@ -37,6 +33,7 @@ void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o)
     o->min_chain_weight = opt->min_chain_weight; o->max_chain_extend = opt->max_chain_extend;
     o->mask_level = opt->mask_level; o->drop_ratio = opt->drop_ratio; o->split_factor = opt->split_factor;
     o->split_width = opt->split_width; o->max_mem_intv = (int32_t)opt->max_mem_intv;
+    o->mask_level_redun = opt->mask_level_redun;
     memcpy(o->mat, opt->mat, 25);
 }
 
@@ -63,7 +60,7 @@ int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns,
     }
     /* every region comes from one extended seed, so 4 per base is a safe bound */
     out = (bsb_reg_t *)malloc(sizeof(bsb_reg_t) * (4 * total + 64 * (int64_t)n + 1));
-    rc = bsb_align_regs_batch(ctx, &o, n, buf, offs, out, 4 * total + 64 * (int64_t)n, roff);
+    rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, 4 * total + 64 * (int64_t)n, roff);
     if (rc == 0) {
         for (i = 0; i < n; ++i) {
             mem_alnreg_v *v = &regs[i];
@@ -77,9 +74,9 @@ int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns,
                 a->rb = r->rb; a->re = r->re; a->qb = r->qb; a->qe = r->qe;
                 a->rid = r->rid; a->score = r->score; a->truesc = r->truesc; a->w = r->w;
                 a->seedcov = r->seedcov; a->seedlen0 = r->seedlen0; a->frac_rep = r->frac_rep;
+                a->n_comp = r->n_comp;
             }
-            /* the host-side tail of mem_align1_core (bwamem.c:1181-1194) */
-            v->n = mem_sort_dedup_patch(opt, bns, pac, (uint8_t *)seqs[i].seq, (int)v->n, v->a);
+            /* the ALT marking of mem_align1_core (bwamem.c:1189-1193) */
             for (j = 0; j < (int)v->n; ++j)
                 if (v->a[j].rid >= 0 && bns->anns[v->a[j].rid].is_alt) v->a[j].is_alt = 1;
         }

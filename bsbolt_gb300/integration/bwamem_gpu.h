@@ -21,10 +21,10 @@ extern "C" {
 /* bsb_align_opt_t from the reference's options. */
 void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o);
 
-/* Seeds, chains and extends n reads (seqs[i].seq is the converted ASCII read,
- * encoded to nt4 in place as mem_align1_core does), then runs the reference's
- * own mem_sort_dedup_patch and ALT marking per read.  regs[i].a is malloc()ed
- * (worker2 frees it).  Returns 0 or a BSB_E* code. */
+/* Seeds, chains, extends and dedups n reads on the GPU (bsb_mem_align1_batch;
+ * seqs[i].seq is the converted ASCII read, encoded to nt4 in place as
+ * mem_align1_core does), then marks ALT regions per read.  regs[i].a is
+ * malloc()ed (worker2 frees it).  Returns 0 or a BSB_E* code. */
 int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
                         int n, bseq1_t *seqs, mem_alnreg_v *regs);
 

@@ -52,12 +52,14 @@ def sa_batch(ctx: Context, rows: np.ndarray) -> np.ndarray:
 # bsb_reg_t: the mem_alnreg_t fields mem_chain2aln sets (bwamem.h:64-82)
 REG_DTYPE = np.dtype([("rb", "<i8"), ("re", "<i8"), ("qb", "<i4"), ("qe", "<i4"), ("rid", "<i4"),
                       ("score", "<i4"), ("truesc", "<i4"), ("w", "<i4"), ("seedcov", "<i4"),
-                      ("seedlen0", "<i4"), ("frac_rep", "<f4"), ("pad", "<i4")])
+                      ("seedlen0", "<i4"), ("frac_rep", "<f4"), ("n_comp", "<i4")])
 
 
-def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.AlignOpt" = None):
+def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.AlignOpt" = None, dedup: bool = False):
     """Seeds -> chains -> chain filter -> mem_chain2aln for every read (the pre-dedup part of
-    mem_align1_core, bwamem.c:1157-1180) on the GPU.  Returns (regs[REG_DTYPE], regs_off[n+1])."""
+    mem_align1_core, bwamem.c:1157-1180) on the GPU; with dedup, mem_sort_dedup_patch too
+    (bsb_mem_align1_batch: the regions mem_align1_core returns, bwamem.c:1157-1188).
+    Returns (regs[REG_DTYPE], regs_off[n+1])."""
     seqs = np.ascontiguousarray(seqs, dtype=np.uint8)
     offs = np.ascontiguousarray(offs, dtype=np.int64)
     opt = opt or _lib.AlignOpt.bwa_defaults()
@@ -70,7 +72,8 @@ def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.Alig
         regs = np.empty(cap, REG_DTYPE)
         ctx._regs_buf = regs
     regs_off = np.empty(n + 1, np.int64)
-    rc = ctx.L.bsb_align_regs_batch(ctx.handle, ctypes.byref(opt), n, _ptr(seqs) if len(seqs) else None,
-                                    _ptr(offs), _ptr(regs), cap, _ptr(regs_off))
+    fn = ctx.L.bsb_mem_align1_batch if dedup else ctx.L.bsb_align_regs_batch
+    rc = fn(ctx.handle, ctypes.byref(opt), n, _ptr(seqs) if len(seqs) else None, _ptr(offs), _ptr(regs), cap,
+            _ptr(regs_off))
     _lib.check(ctx.handle, rc)
     return regs[: regs_off[-1]].copy(), regs_off

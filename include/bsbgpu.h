@@ -227,15 +227,17 @@ typedef struct {
     int32_t split_width, max_mem_intv;
     int8_t  mat[25];
     int8_t  pad_[3];
+    float   mask_level_redun;    /* mem_sort_dedup_patch (bwa default 0.95) */
 } bsb_align_opt_t;
 
 /* The fields of mem_alnreg_t (bwamem.h:64-82) that mem_chain2aln sets; every
- * other field of the reference's struct is zero at that point. */
+ * other field of the reference's struct is zero at that point.  n_comp is set
+ * by mem_sort_dedup_patch (bsb_mem_align1_batch) and 0 before it. */
 typedef struct {
     int64_t rb, re;
     int32_t qb, qe, rid, score, truesc, w, seedcov, seedlen0;
     float   frac_rep;
-    int32_t pad_;
+    int32_t n_comp;
 } bsb_reg_t;
 
 /* Replaces, for a batch of reads, the part of mem_align1_core
@@ -248,6 +250,19 @@ typedef struct {
  * mem_flt_chained_seeds a no-op (bwamem.c:606), indexes without ALT contigs
  * (BSBolt writes none).  Host buffers; synchronous. */
 int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
+                         const uint8_t *seqs, const int64_t *offs,
+                         bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
+
+/* Replaces mem_align1_core (bwamem.c:1157-1195) for a batch of reads up to its
+ * ALT marking: bsb_align_regs_batch followed by mem_sort_dedup_patch
+ * (bwamem.c:441-493) per read -- the sort by end, the redundant regions
+ * dropped (opt->mask_level_redun), colinear regions merged by mem_patch_reg
+ * (bwamem.c:410-439, with its banded global alignment), the sort by score and
+ * identical regions dropped.  Read r's regions, in the order mem_align1_core
+ * returns them, are regs[regs_off[r] .. regs_off[r+1]); n_comp as the reference
+ * sets it.  Marking regions on ALT contigs (bwamem.c:1189-1193) stays with the
+ * caller (BSBolt's indexes have none).  Same limits as bsb_align_regs_batch. */
+int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
 

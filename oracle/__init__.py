@@ -21,8 +21,8 @@ _SO = os.path.join(_HERE, "_build", "liborc.so")
 _lib = None
 
 
-_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c", "bsb_oracle_cigar.c", "bsb_oracle_sw.c")
-_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h", "bsb_oracle_cigar.h", "bsb_oracle_sw.h")
+_SRC = ("bsb_oracle.c", "bsb_oracle_chain.c", "bsb_oracle_cigar.c", "bsb_oracle_sw.c", "bsb_oracle_dedup.c")
+_HDR = ("bsb_oracle.h", "bsb_oracle_chain.h", "bsb_oracle_cigar.h", "bsb_oracle_sw.h", "bsb_oracle_dedup.h")
 
 
 def build(force: bool = False) -> str:
@@ -32,7 +32,7 @@ def build(force: bool = False) -> str:
         return _SO
     os.makedirs(os.path.dirname(_SO), exist_ok=True)
     tmp = _SO + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-o", tmp]
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-o", tmp]
                           + [os.path.join(_HERE, f) for f in _SRC] + ["-lm"])
     os.replace(tmp, _SO)
     return _SO
@@ -137,7 +137,7 @@ CHAIN_DTYPE = np.dtype([("n", "<i4"), ("rid", "<i4"), ("first", "<i4"), ("kept",
 SEED_DTYPE = np.dtype([("rbeg", "<i8"), ("qbeg", "<i4"), ("len", "<i4"), ("score", "<i4"), ("pad", "<i4")])
 REG_DTYPE = np.dtype([("rb", "<i8"), ("re", "<i8"), ("qb", "<i4"), ("qe", "<i4"), ("rid", "<i4"),
                       ("score", "<i4"), ("truesc", "<i4"), ("w", "<i4"), ("seedcov", "<i4"),
-                      ("seedlen0", "<i4"), ("frac_rep", "<f4"), ("pad", "<i4")])
+                      ("seedlen0", "<i4"), ("frac_rep", "<f4"), ("n_comp", "<i4")])
 ANN_DTYPE = np.dtype([("offset", "<i8"), ("len", "<i4"), ("is_alt", "<i4")])
 
 
@@ -148,7 +148,7 @@ class Opt(ctypes.Structure):
                                                "max_chain_gap", "min_chain_weight", "max_chain_extend")] + \
                [("mask_level", ctypes.c_float), ("drop_ratio", ctypes.c_float), ("split_factor", ctypes.c_float),
                 ("split_width", ctypes.c_int32), ("max_mem_intv", ctypes.c_int32),
-                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3)]
+                ("mat", ctypes.c_int8 * 25), ("pad_", ctypes.c_int8 * 3), ("mask_level_redun", ctypes.c_float)]
 
     @classmethod
     def from_list(cls, o):
@@ -158,7 +158,7 @@ class Opt(ctypes.Structure):
         opt = cls(a=o[0], b=o[1], o_del=o[2], e_del=o[3], o_ins=o[4], e_ins=o[5], w=o[6], zdrop=o[7],
                   pen_clip5=o[8], pen_clip3=o[9], min_seed_len=o[10], max_occ=o[11], max_chain_gap=o[14],
                   min_chain_weight=0, max_chain_extend=1 << 30, mask_level=0.5, drop_ratio=0.5,
-                  split_factor=1.5, split_width=o[12], max_mem_intv=o[13])
+                  split_factor=1.5, split_width=o[12], max_mem_intv=o[13], mask_level_redun=0.95)
         for i in range(4):
             for j in range(4):
                 opt.mat[i * 5 + j] = o[0] if i == j else -o[1]
@@ -258,3 +258,37 @@ def align2_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, n_threads: int = 1)
     out = np.zeros(len(jobs), KSWR_DTYPE)
     lib().orc_align2_batch(len(jobs), _p(jobs), _p(seq), _p(mat), o_del, e_del, o_ins, e_ins, _p(out), n_threads)
     return out
+
+
+def sort_dedup_batch(opt, l_pac, pac, seqs, offs, regs, regs_off):
+    """mem_sort_dedup_patch (bwamem.c:441-493) per read on pre-dedup regions (REG_DTYPE, per
+    read regs[regs_off[r]:regs_off[r+1]]); reads are nt4 seqs[offs[r]:offs[r+1]].
+    Returns (regions after dedup, their offsets)."""
+    L = lib()
+    L.orc_sort_dedup_batch.restype = None
+    L.orc_sort_dedup_batch.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int] + \
+        [ctypes.c_void_p] * 6
+    pac = np.ascontiguousarray(pac, dtype=np.uint8)
+    seqs = np.ascontiguousarray(seqs, dtype=np.uint8)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    regs = np.ascontiguousarray(regs, dtype=REG_DTYPE)
+    regs_off = np.ascontiguousarray(regs_off, dtype=np.int64)
+    n = len(offs) - 1
+    out = np.zeros(max(len(regs), 1), REG_DTYPE)
+    out_off = np.zeros(n + 1, np.int64)
+    L.orc_sort_dedup_batch(ctypes.byref(opt), l_pac, _p(pac), n, _p(seqs), _p(offs), _p(regs), _p(regs_off), _p(out),
+                           _p(out_off))
+    return out[:int(out_off[-1])].copy(), out_off
+
+
+def regs_from_golden(rows):
+    """REG_DTYPE records from the fixtures' region rows (rb, re, qb, qe, rid, score, truesc,
+    w, seedcov, seedlen0, [n_comp,] frac_rep bits)."""
+    rows = np.asarray(rows, np.int64)
+    r = np.zeros(len(rows), REG_DTYPE)
+    for i, f in enumerate(["rb", "re", "qb", "qe", "rid", "score", "truesc", "w", "seedcov", "seedlen0"]):
+        r[f] = rows[:, i]
+    if rows.shape[1] == 12:
+        r["n_comp"] = rows[:, 10]
+    r["frac_rep"] = rows[:, -1].astype(np.int32).view(np.float32)
+    return r

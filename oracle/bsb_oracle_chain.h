@@ -30,6 +30,7 @@ typedef struct {
     int32_t split_width, max_mem_intv;
     int8_t mat[25];
     int8_t pad_[3];
+    float mask_level_redun;      /* mem_sort_dedup_patch */
 } orc_opt_t;
 
 typedef struct { int64_t rbeg; int32_t qbeg, len, score, pad_; } orc_seed_t;   /* mem_seed_t */
@@ -45,7 +46,7 @@ typedef struct {                 /* the mem_alnreg_t fields mem_chain2aln sets (
     int64_t rb, re;
     int32_t qb, qe, rid, score, truesc, w, seedcov, seedlen0;
     float frac_rep;
-    int32_t pad_;
+    int32_t n_comp;              /* set by mem_sort_dedup_patch; 0 before */
 } orc_reg_t;
 
 int orc_mem_chain(const orc_bwt_t *bwt, const orc_bns_t *bns, const orc_opt_t *opt, int len,

@@ -362,3 +362,39 @@ int64_t orc_gen_cigar_batch(const int8_t mat[25], int o_del, int e_del, int o_in
     free(rs), free(th);
     return used <= blob_cap ? used : -1;
 }
+
+/* bwa_gen_cigar2 (bwa.c:199-244, 343-346) as mem_patch_reg calls it (bwamem.c:432): only
+ * the score is wanted (n_cigar, NM, oquery NULL).  Returns 0 where the reference returns
+ * before setting *score (bwa.c:211, 215), else 1. */
+int orc_gen_cigar2_score(const int8_t mat[25], int o_del, int e_del, int o_ins, int e_ins, int w_, int64_t l_pac,
+                         const uint8_t *pac, int l_query, const uint8_t *query_in, int64_t rb, int64_t re, int *score)
+{
+    if (l_query <= 0 || rb >= re || (rb < l_pac && re > l_pac)) return 0;
+    int64_t rlen;
+    int clamped;
+    uint8_t *rseq = get_seq(l_pac, pac, rb, re, &rlen, &clamped);
+    if (re - rb != rlen) {
+        free(rseq);
+        return 0;
+    }
+    uint8_t *query = malloc(l_query);
+    memcpy(query, query_in, l_query);
+    if (rb >= l_pac) reverse_bytes(query, l_query), reverse_bytes(rseq, rlen);
+    if (l_query == re - rb && w_ == 0) {
+        *score = 0;
+        for (int i = 0; i < l_query; ++i) *score += mat[rseq[i] * 5 + query[i]];
+    } else {
+        const int max_ins = (int)((double)(((l_query + 1) >> 1) * mat[0] - o_ins) / e_ins + 1.);
+        const int max_del = (int)((double)(((l_query + 1) >> 1) * mat[0] - o_del) / e_del + 1.);
+        int max_gap = max_ins > max_del ? max_ins : max_del;
+        max_gap = max_gap > 1 ? max_gap : 1;
+        const int dl = abs((int)rlen - l_query);
+        int w = (max_gap + dl + 1) >> 1;
+        w = w < w_ ? w : w_;
+        w = w > dl + 3 ? w : dl + 3;
+        *score = orc_ksw_global2(l_query, query, (int)rlen, rseq, mat, o_del, e_del, o_ins, e_ins, w, 0, 0, 0);
+    }
+    free(query);
+    free(rseq);
+    return 1;
+}

@@ -63,6 +63,11 @@ int64_t orc_gen_cigar_batch(const int8_t mat[25], int o_del, int e_del, int o_in
                             const uint8_t *obuf, orc_cigar_out_t *out, uint8_t *blob,
                             int64_t blob_cap, int n_threads);
 
+/* bwa_gen_cigar2's score alone (bwa.c:199-244), as mem_patch_reg calls it (bwamem.c:432):
+ * returns 0 where the reference leaves *score unset, else 1. */
+int orc_gen_cigar2_score(const int8_t mat[25], int o_del, int e_del, int o_ins, int e_ins, int w_, int64_t l_pac,
+                         const uint8_t *pac, int l_query, const uint8_t *query, int64_t rb, int64_t re, int *score);
+
 #ifdef __cplusplus
 }
 #endif

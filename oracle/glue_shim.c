@@ -2,8 +2,8 @@
  * glue_shim.c -- TEST INFRASTRUCTURE ONLY.
  *
  * Lets the BWA glue (bsbolt_gb300/integration/bwamem_gpu.c) be tested on a
- * machine without a GPU: bsb_align_regs_batch and bsb_gen_cigar_batch are
- * answered by the CPU oracle (whose results equal the GPU's, by the GPU tests),
+ * machine without a GPU: bsb_mem_align1_batch, bsb_gen_cigar_batch and
+ * bsb_align2_batch are answered by the CPU oracle (whose results equal the GPU's, by the GPU tests),
  * and the worker1 call of the reference's mem_process_seqs is redirected to
  * mem_align_batch_gpu + mem_gen_cigar_prepass_gpu, and the worker2 call is
  * preceded by mem_matesw_prepass_gpu, by a link-time wrap of kt_for
@@ -21,6 +21,7 @@
 #include "bsb_oracle_chain.h"
 #include "bsb_oracle_cigar.h"
 #include "bsb_oracle_sw.h"
+#include "bsb_oracle_dedup.h"
 #include <stdio.h>
 
 struct bsb_ctx {
@@ -34,8 +35,8 @@ static struct bsb_ctx g_ctx;
 
 const char *bsb_last_error(const bsb_ctx *ctx) { (void)ctx; return "oracle shim failure"; }
 
-int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
-                         const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+static int shim_align(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                      const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off, int dedup)
 {
     orc_opt_t oo;
     orc_align_out_t out;
@@ -47,8 +48,18 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads
     oo.min_chain_weight = o->min_chain_weight; oo.max_chain_extend = o->max_chain_extend;
     oo.mask_level = o->mask_level; oo.drop_ratio = o->drop_ratio; oo.split_factor = o->split_factor;
     oo.split_width = o->split_width; oo.max_mem_intv = o->max_mem_intv;
+    oo.mask_level_redun = o->mask_level_redun;
     memcpy(oo.mat, o->mat, 25);
     rc = orc_align_regs_batch(&ctx->bwt, &ctx->bns, &oo, n_reads, seqs, offs, &out, 4);
+    if (rc == 0 && dedup) {            /* mem_sort_dedup_patch per read, in place of the pre-dedup list */
+        orc_reg_t *kept = (orc_reg_t *)malloc(sizeof(orc_reg_t) * (out.regs_off[n_reads] + 1));
+        int64_t *kept_off = (int64_t *)malloc(sizeof(int64_t) * (n_reads + 1));
+        orc_sort_dedup_batch(&oo, ctx->bns.l_pac, ctx->bns.pac, n_reads, seqs, offs, out.regs, out.regs_off, kept,
+                             kept_off);
+        free(out.regs);
+        free(out.regs_off);
+        out.regs = kept, out.regs_off = kept_off;
+    }
     if (rc == 0 && out.regs_off[n_reads] > max_regs) rc = BSB_EINVAL;
     if (rc == 0) {
         for (r = 0; r <= n_reads; ++r) regs_off[r] = out.regs_off[r];
@@ -58,7 +69,7 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads
             memset(d, 0, sizeof(*d));
             d->rb = s->rb; d->re = s->re; d->qb = s->qb; d->qe = s->qe; d->rid = s->rid; d->score = s->score;
             d->truesc = s->truesc; d->w = s->w; d->seedcov = s->seedcov; d->seedlen0 = s->seedlen0;
-            d->frac_rep = s->frac_rep;
+            d->frac_rep = s->frac_rep; d->n_comp = s->n_comp;
         }
         /* self-check of the test: with BSB_SHIM_PERTURB set, shift the first
          * region by one base so the SAM must change if this path is live */
@@ -66,6 +77,18 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads
     }
     orc_align_out_free(&out);
     return rc ? BSB_EINVAL : 0;
+}
+
+int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                         const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    return shim_align(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, 0);
+}
+
+int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
+                         const int64_t *offs, bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off)
+{
+    return shim_align(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, 1);
 }
 
 int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int64_t crick_l, int32_t n,

@@ -18,7 +18,8 @@
  *       already-converted reads.  For each read: the sorted seed intervals
  *       of mem_collect_intv (taken from mem_chain's smem buffer), the chains
  *       of mem_chain + mem_chain_flt + mem_flt_chained_seeds, the pre-dedup
- *       regions of mem_chain2aln, and every ksw_extend2 call (inputs and
+ *       regions of mem_chain2aln, the regions after mem_sort_dedup_patch, and
+ *       every ksw_extend2 call (inputs and
  *       tuple) made while building them.
  */
 #include <stdint.h>
@@ -31,6 +32,10 @@
 #include "bwt.h"
 #include "ksw.h"
 #include "kvec.h"
+
+/* defined in bwamem.c (bwamem.c:441), not declared in bwamem.h */
+int mem_sort_dedup_patch(const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac, uint8_t *query, int n,
+                         mem_alnreg_t *a);
 
 typedef struct {
     int64_t qoff, toff;
@@ -140,7 +145,7 @@ static int mode_reads(const char *prefix, const char *readsfn, const char *outp,
     mem_opt_t *opt = mem_opt_init();
     smem_buf_t sb;
     char fn[4096];
-    FILE *f_smem, *f_chain, *f_reg;
+    FILE *f_smem, *f_chain, *f_reg, *f_dedup;
     int64_t r;
 
     /* option overrides: a, b, o_del, e_del, o_ins, e_ins, w, zdrop, pen_clip5, pen_clip3,
@@ -162,6 +167,7 @@ static int mode_reads(const char *prefix, const char *readsfn, const char *outp,
     snprintf(fn, sizeof fn, "%s.chain.bin", outp); f_chain = fopen(fn, "wb");
     snprintf(fn, sizeof fn, "%s.reg.bin", outp); f_reg = fopen(fn, "wb");
     snprintf(fn, sizeof fn, "%s.ksw.bin", outp); g_kswlog = fopen(fn, "wb");
+    snprintf(fn, sizeof fn, "%s.dedup.bin", outp); f_dedup = fopen(fn, "wb");
 
     for (r = 0; r < n; ++r) {
         int l = (int)(offs[r + 1] - offs[r]), i, j;
@@ -217,10 +223,24 @@ static int mode_reads(const char *prefix, const char *readsfn, const char *outp,
             fwrite(v, 4, 9, f_reg);
             fwrite(&p->frac_rep, 4, 1, f_reg);
         }
+        /* the reference's own mem_sort_dedup_patch on them (bwamem.c:1181), as mem_align1_core
+         * calls it: the regions mem_align1_core returns */
+        regs.n = mem_sort_dedup_patch(opt, idx->bns, idx->pac, q, (int)regs.n, regs.a);
+        hdr[1] = (int32_t)regs.n;
+        fwrite(hdr, 4, 2, f_dedup);
+        for (j = 0; j < (int)regs.n; ++j) {
+            mem_alnreg_t *p = &regs.a[j];
+            int64_t rr[2] = {p->rb, p->re};
+            int32_t v[9] = {p->qb, p->qe, p->rid, p->score, p->truesc, p->w, p->seedcov,
+                            p->seedlen0, (int32_t)p->n_comp};
+            fwrite(rr, 8, 2, f_dedup);
+            fwrite(v, 4, 9, f_dedup);
+            fwrite(&p->frac_rep, 4, 1, f_dedup);
+        }
         free(regs.a);
         free(q);
     }
-    fclose(f_smem); fclose(f_chain); fclose(f_reg); fclose(g_kswlog); g_kswlog = 0;
+    fclose(f_smem); fclose(f_chain); fclose(f_reg); fclose(f_dedup); fclose(g_kswlog); g_kswlog = 0;
     bwa_idx_destroy(idx);
     free(buf); free(ov); free(opt);
     return 0;

@@ -32,7 +32,10 @@ def golden_genome():
 # a, b, o_del, e_del, o_ins, e_ins, w, zdrop, pen_clip5, pen_clip3,
 # min_seed_len, max_occ, split_width, max_mem_intv, max_chain_gap
 OPTS = {"L5": [1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000],
-        "L30": [1, 4, 6, 1, 6, 1, 100, 100, 30, 30, 19, 500, 10, 20, 10000]}
+        "L30": [1, 4, 6, 1, 6, 1, 100, 100, 30, 30, 19, 500, 10, 20, 10000],
+        # a narrow band: indels of a few bases split chains, so mem_sort_dedup_patch merges
+        # colinear regions (mem_patch_reg) as well as dropping redundant ones
+        "W5": [1, 4, 6, 1, 6, 1, 5, 100, 5, 5, 19, 500, 10, 20, 10000]}
 
 
 def golden_reads(n_pairs=700, seed=20261203 + 7):
@@ -53,6 +56,37 @@ def golden_reads(n_pairs=700, seed=20261203 + 7):
     return reads
 
 
+
+
+def golden_reads_indel(n=400, seed=20261203 + 8):
+    """Reads of 150-300 bases from the golden genome (both strands, converted), each with
+    one or two indels of 6-14 bases, plus copies that repeat a 20-60 base stretch: with
+    the W5 band their seeds fall into several chains, and their regions into the merge
+    and redundancy cases of mem_sort_dedup_patch."""
+    contigs = golden_genome()
+    contigs = [(nm, np.where(c > 3, 0, c).astype(np.uint8)) for nm, c in contigs]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    reads = []
+    for k in range(n):
+        c = contigs[int(rng.integers(0, len(contigs)))][1]
+        L = int(rng.integers(150, 301))
+        at = int(rng.integers(0, len(c) - L - 100))
+        frag = c[at:at + L + 60].copy()
+        for _ in range(int(rng.choice([1, 1, 2]))):
+            pos = int(rng.integers(40, L - 40))
+            ln = int(rng.integers(6, 15))
+            if rng.random() < 0.5:
+                frag = np.concatenate([frag[:pos], frag[pos + ln:]])
+            else:
+                frag = np.concatenate([frag[:pos], rng.integers(0, 4, ln).astype(np.uint8), frag[pos:]])
+        if k % 4 == 3:                                  # a repeated stretch (tandem duplication)
+            pos, ln = int(rng.integers(40, L - 80)), int(rng.integers(20, 61))
+            frag = np.concatenate([frag[:pos + ln], frag[pos:pos + ln], frag[pos + ln:]])
+        r = frag[:L]
+        if k % 2:
+            r = (3 - r[::-1]).astype(np.uint8)
+        reads.append(synth.bs_convert(r, g2a=bool(k % 3 == 0)))
+    return reads
 
 
 # ------------------------------------------------------------ repeat stress

@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 from bsbolt_gb300 import synth  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from golden_data import (GENOME, GENOME_REP, OPTS, golden_cigar_jobs, golden_genome,  # noqa: E402
+from golden_data import (GENOME, GENOME_REP, OPTS, golden_cigar_jobs, golden_genome, golden_reads_indel,  # noqa: E402
                          golden_genome_rep, golden_reads, golden_reads_rep, golden_sw_jobs)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -205,6 +205,19 @@ def parse_dump(prefix, n_reads):
         reg_off.append(len(regs))
     out["regs"] = np.array(regs, np.int64).reshape(-1, 11)
     out["reg_off"] = np.array(reg_off, np.int64)
+    # after mem_sort_dedup_patch: the same columns, n_comp in place of the padding
+    b = open(prefix + ".dedup.bin", "rb").read()
+    off, regs, reg_off = 0, [], [0]
+    for _ in range(n_reads):
+        r, n = np.frombuffer(b, np.int32, 2, off); off += 8
+        for _k in range(n):
+            rr = np.frombuffer(b, np.int64, 2, off); off += 16
+            v = np.frombuffer(b, np.int32, 9, off); off += 36
+            fr = np.frombuffer(b, np.float32, 1, off)[0]; off += 4
+            regs.append(list(rr) + list(v) + [int(np.float32(fr).view(np.int32))])
+        reg_off.append(len(regs))
+    out["dedup"] = np.array(regs, np.int64).reshape(-1, 12)
+    out["dedup_off"] = np.array(reg_off, np.int64)
     b = open(prefix + ".ksw.bin", "rb").read()
     off, kh, kr, kseq, koff = 0, [], [], [], [0]
     while off < len(b):
@@ -363,6 +376,7 @@ if __name__ == "__main__":
             prefix = make_index(td)
             if "reads" in what:
                 make_reads(td, prefix)
+                make_reads(td, prefix, golden_reads_indel(), ("W5",), "_indel")
             prefix = make_index(td, "_rep", golden_genome_rep, GENOME_REP)
             if "reads" in what:
                 make_reads(td, prefix, golden_reads_rep(), ("L5",), "_rep")

@@ -1,6 +1,8 @@
 """Seeds -> chains -> chain filter -> mem_chain2aln on the GPU (bsb_align_regs_batch)
-against the reference's pre-dedup regions (tests/golden/reads*_L*.npz) and the
-oracle, through the C ABI.  Bit-exact, including frac_rep's float bits."""
+against the reference's pre-dedup regions (tests/golden/reads*_*.npz) and the
+oracle, and with mem_sort_dedup_patch (bsb_mem_align1_batch) against the
+reference's post-dedup regions and the oracle, through the C ABI.  Bit-exact,
+including frac_rep's float bits."""
 import os
 import sys
 
@@ -37,8 +39,11 @@ def indexes(tmp_path_factory):
     return out
 
 
-@pytest.mark.parametrize("fn,tag", [("reads_L5.npz", "plain"), ("reads_L30.npz", "plain"),
-                                    ("reads_rep_L5.npz", "rep")])
+GOLDEN_SETS = [("reads_L5.npz", "plain"), ("reads_L30.npz", "plain"), ("reads_rep_L5.npz", "rep"),
+               ("reads_indel_W5.npz", "plain")]
+
+
+@pytest.mark.parametrize("fn,tag", GOLDEN_SETS)
 def test_regions_match_reference(gpu_ctx, indexes, fn, tag):
     seed.load_index(gpu_ctx, indexes[tag])
     g = np.load(os.path.join(GOLDEN, fn))
@@ -91,3 +96,44 @@ def test_align_rejects_long_reads(gpu_ctx, indexes):
     with pytest.raises(_lib.BsbError) as e:
         seed.align_regs(gpu_ctx, np.zeros(600, np.uint8), np.array([0, 600]))
     assert e.value.code == _lib.BSB_ETOOLONG
+
+
+@pytest.mark.parametrize("fn,tag", GOLDEN_SETS)
+def test_dedup_regions_match_reference(gpu_ctx, indexes, fn, tag):
+    """bsb_mem_align1_batch: the regions mem_align1_core returns (after mem_sort_dedup_patch),
+    including merged regions (n_comp, the merge's global-alignment score) in the indel set."""
+    seed.load_index(gpu_ctx, indexes[tag])
+    g = np.load(os.path.join(GOLDEN, fn))
+    regs, off = seed.align_regs(gpu_ctx, g["reads"], g["read_off"], opt_from(g["opts"]), dedup=True)
+    assert np.array_equal(off, g["dedup_off"]), "region counts per read differ"
+    gd = g["dedup"]
+    for i, f in enumerate(REG_FIELDS + ["n_comp"]):
+        bad = np.nonzero(regs[f] != gd[:, i])[0]
+        assert len(bad) == 0, f"{fn}: dedup.{f} differs at {bad[:5]}"
+    assert np.array_equal(regs["frac_rep"].view(np.int32), gd[:, 11].astype(np.int32))
+
+
+def test_dedup_random_indel_reads_vs_oracle(gpu_ctx, indexes):
+    """Reads of 150-300 bases with indels and duplicated stretches at band 5 and 10 (merges),
+    both strands, against the oracle's mem_sort_dedup_patch on the oracle's own regions."""
+    prefix = indexes["plain"]
+    seed.load_index(gpu_ctx, prefix)
+    bi = index.BwaIndex(prefix)
+    reads = golden_data.golden_reads_indel(n=1500, seed=20261203 + 71)
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    seqs = np.concatenate(reads)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    merged = 0
+    for w in (5, 10):
+        o = [1, 4, 6, 1, 6, 1, w, 100, 5, 5, 19, 500, 10, 20, 10000]
+        regs, off = seed.align_regs(gpu_ctx, seqs, offs, opt_from(o), dedup=True)
+        oo = oracle.Opt.from_list(o)
+        pre = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oo, seqs, offs, n_threads=8)
+        ref, ref_off = oracle.sort_dedup_batch(oo, bi.l_pac, bi.pac, seqs, offs, pre["regs"], pre["regs_off"])
+        assert np.array_equal(off, ref_off)
+        for f in REG_FIELDS + ["n_comp", "frac_rep"]:
+            assert np.array_equal(regs[f], ref[f]), f"w={w}: dedup.{f}"
+        merged += int((regs["n_comp"] > 1).sum())
+    assert merged > 100

@@ -1,9 +1,12 @@
-"""The chaining / chain-filter / mem_chain2aln oracle against the reference (CPU only).
+"""The chaining / chain-filter / mem_chain2aln / mem_sort_dedup_patch oracle against
+the reference (CPU only).
 
-Fixtures (tests/golden/reads*_L*.npz) hold, per read, the reference's chains
-straight out of mem_chain (tree order), after mem_chain_flt, and the
-pre-dedup regions of mem_chain2aln.  The repeat-stress set has reads with up
-to 125 chains (B-tree splits), equal chain keys and tied chain weights.
+Fixtures (tests/golden/reads*_*.npz) hold, per read, the reference's chains
+straight out of mem_chain (tree order), after mem_chain_flt, the pre-dedup
+regions of mem_chain2aln and the regions after mem_sort_dedup_patch.  The
+repeat-stress set has reads with up to 125 chains (B-tree splits), equal chain
+keys and tied chain weights; the indel set (band 5) has regions that
+mem_patch_reg merges and regions dropped as redundant.
 """
 import os
 import sys
@@ -19,7 +22,7 @@ sys.path.insert(0, GOLDEN)
 import golden_data  # noqa: E402
 
 CASES = [("reads_L5.npz", golden_data.golden_genome), ("reads_L30.npz", golden_data.golden_genome),
-         ("reads_rep_L5.npz", golden_data.golden_genome_rep)]
+         ("reads_rep_L5.npz", golden_data.golden_genome_rep), ("reads_indel_W5.npz", golden_data.golden_genome)]
 _IDX = {}
 
 
@@ -71,3 +74,29 @@ def test_repeat_fixture_covers_hard_cases():
     assert n.max() > 45                       # several B-tree levels
     dup = sum(1 for r in range(len(n)) if len(set(rows[off[r]:off[r + 1], 5].tolist())) != n[r])
     assert dup > 10                           # equal chain keys
+
+
+def check_dedup(r, g):
+    assert np.array_equal(r[1], g["dedup_off"])
+    d, gd = r[0], g["dedup"]
+    for i, f in enumerate(["rb", "re", "qb", "qe", "rid", "score", "truesc", "w", "seedcov", "seedlen0", "n_comp"]):
+        assert np.array_equal(d[f], gd[:, i]), f"dedup.{f}"
+    assert np.array_equal(d["frac_rep"].view(np.int32), gd[:, 11].astype(np.int32))
+
+
+@pytest.mark.parametrize("fn,genome", CASES, ids=[c[0] for c in CASES])
+def test_oracle_dedup_matches_reference(fn, genome, tmp_path_factory):
+    """mem_sort_dedup_patch on the reference's own pre-dedup regions gives the reference's
+    post-dedup regions (sort orders, redundancy, merges with their global alignments)."""
+    bi = index_for(genome, tmp_path_factory)
+    g = np.load(os.path.join(GOLDEN, fn))
+    pre = oracle.regs_from_golden(g["regs"])
+    r = oracle.sort_dedup_batch(oracle.Opt.from_list(g["opts"]), bi.l_pac, bi.pac, g["reads"], g["read_off"], pre,
+                                g["reg_off"])
+    check_dedup(r, g)
+
+
+def test_indel_fixture_covers_merges():
+    g = np.load(os.path.join(GOLDEN, "reads_indel_W5.npz"))
+    assert (g["dedup"][:, 10] > 1).sum() > 50                 # mem_patch_reg merges
+    assert len(g["regs"]) - len(g["dedup"]) > 80              # regions dropped
