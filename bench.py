@@ -400,6 +400,12 @@ def pipeline_secondary(ctx, steps, rank):
     for _ in range(k):
         sd, soff = seed.seed_batch(ctx, reads, offs)
     seed_s = (time.perf_counter() - t0) / k
+    # the whole of mem_align1_core (with mem_sort_dedup_patch): bsb_mem_align1_batch
+    dregs, droff = seed.align_regs(ctx, reads, offs, opt, dedup=True)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        dregs, droff = seed.align_regs(ctx, reads, offs, opt, dedup=True)
+    full_s = (time.perf_counter() - t0) / k
     bi = index.BwaIndex(prefix)
     ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
     anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
@@ -408,9 +414,15 @@ def pipeline_secondary(ctx, steps, rank):
     ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac,
                             oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000]),
                             reads, offs, n_threads=threads)
+    oo = oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000])
     cpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dref, dref_off = oracle.sort_dedup_batch(oo, bi.l_pac, bi.pac, reads, offs, ref["regs"], ref["regs_off"])
+    cpu_dedup_s = time.perf_counter() - t0
     exact = bool(np.array_equal(roff, ref["regs_off"]) and
                  all(np.array_equal(regs[f], ref["regs"][f]) for f in ("rb", "re", "qb", "qe", "score", "truesc")))
+    dexact = bool(np.array_equal(droff, dref_off) and
+                  all(np.array_equal(dregs[f], dref[f]) for f in dref.dtype.names))
     return {
         "workload": "2 Mb bisulfite reference (4x500 kb), 20k directional PE 2x100 pairs, "
                     "BWA defaults, -L 5",
@@ -425,6 +437,13 @@ def pipeline_secondary(ctx, steps, rank):
         "regions_bit_exact_vs_oracle": exact,
         "regions": int(roff[-1]),
         "ext_cells": int(ref["cells"]),
+        "mem_align1_stage": "the same plus mem_sort_dedup_patch per read (bsb_mem_align1_batch: the regions "
+                            "mem_align1_core returns)",
+        "gpu_mem_align1_read_pairs_per_s": round(n_pairs / full_s, 1),
+        "gpu_mem_align1_ms_per_batch": round(full_s * 1e3, 3),
+        "cpu_oracle_mem_align1_read_pairs_per_s": round(n_pairs / (cpu_s + cpu_dedup_s), 1),
+        "dedup_regions": int(droff[-1]),
+        "dedup_regions_bit_exact_vs_oracle": dexact,
     }
 
 
