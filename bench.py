@@ -325,6 +325,83 @@ def ref100mb_workload(n_pairs=100_000):
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
 
 
+def rrbs_workload(n_reads=3_000_000):
+    """The RRBS-like workload on the 100 Mb reference: directional single-end reads, half 1x75 and
+    half 1x100, starting at the ends of MspI fragments of 40-220 bases (so heavily duplicated),
+    CpG methylation 0.7.  Cached on disk beside the 100 Mb index."""
+    from bsbolt_gb300 import synth
+    prefix, _, _ = ref100mb_workload()
+    d = os.path.dirname(prefix)
+    fr, fo = os.path.join(d, f"rrbs_{n_reads}.npy"), os.path.join(d, f"rrbs_{n_reads}_offs.npy")
+    if not os.path.exists(fo):
+        contigs = synth.bs_genome(4, 25_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 2)
+        synth.add_repeats(contigs, 0.15, seed=20261203 + 2)
+        seqs, offs = synth.rrbs_reads_se(contigs, n_reads, seed=20261203 + 3)
+        conv = seqs.copy()
+        conv[conv == 1] = 3                     # the aligner's C->T conversion of read 1 (bs_helpers.cpp:18-31)
+        np.save(fr, conv)
+        np.save(fo, offs)
+    return prefix, np.load(fr), np.load(fo)
+
+
+def pipeline_rrbs(ctx, batch_bases=10_000_000, cpu_reads=4_000):
+    """bsb_mem_align1_batch on the RRBS-like workload in -K 10M-base batches, against the CPU
+    oracle (chains, extension and mem_sort_dedup_patch) on a sample."""
+    import oracle
+    from bsbolt_gb300 import _lib, index, seed
+    t0 = time.perf_counter()
+    prefix, reads, offs = rrbs_workload()
+    prep_s = time.perf_counter() - t0
+    n_reads = len(offs) - 1
+    seed.load_index(ctx, prefix)
+    opt = _lib.AlignOpt.bwa_defaults()
+    batches, lo = [], 0
+    while lo < n_reads:                        # -K: reads until the batch holds batch_bases bases
+        hi = int(np.searchsorted(offs, offs[lo] + batch_bases, side="left"))
+        hi = max(lo + 1, min(hi, n_reads))
+        batches.append((lo, hi))
+        lo = hi
+
+    def sub(a, b):
+        return reads[offs[a]:offs[b]], offs[a:b + 1] - offs[a]
+    seed.align_regs(ctx, *sub(*batches[0]), opt, dedup=True)     # warm-up
+    t0 = time.perf_counter()
+    first = None
+    for a, b in batches:
+        regs, roff = seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        if first is None:
+            first = (regs, roff)
+    gpu_s = time.perf_counter() - t0
+    bi = index.BwaIndex(prefix)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    threads = os.cpu_count() or 1
+    cr, co = sub(0, cpu_reads)
+    oo = oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000])
+    t0 = time.perf_counter()
+    pre = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oo, cr, co, n_threads=threads)
+    ref, ref_off = oracle.sort_dedup_batch(oo, bi.l_pac, bi.pac, cr, co, pre["regs"], pre["regs_off"])
+    cpu_s = time.perf_counter() - t0
+    regs, roff = first
+    k = int(roff[cpu_reads])
+    exact = bool(np.array_equal(roff[:cpu_reads + 1], ref_off) and
+                 all(np.array_equal(regs[f][:k], ref[f]) for f in ref.dtype.names))
+    lens = np.diff(offs)
+    return {
+        "workload": f"RRBS-like: {n_reads} directional single-end reads (1x75 and 1x100, shorter where the fragment is) "
+                    "starting at the ends of MspI fragments of 40-220 bases of the 100 Mb reference, CpG methylation "
+                    f"0.7, -K 10M-base batches ({len(batches)}), BWA defaults",
+        "stage": "bsb_mem_align1_batch (seeds -> ... -> mem_sort_dedup_patch), host buffers incl. H2D/D2H",
+        "gpu_reads_per_s": round(n_reads / gpu_s, 1),
+        "gpu_ms_per_batch": round(gpu_s / len(batches) * 1e3, 3),
+        "mean_read_len": round(float(lens.mean()), 1),
+        "cpu_oracle_reads_per_s": round(cpu_reads / cpu_s, 1),
+        "cpu_oracle_threads": threads, "cpu_sample_reads": cpu_reads,
+        "regions_bit_exact_vs_oracle_on_sample": exact,
+        "workload_prep_s": round(prep_s, 1),
+    }
+
+
 def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
     """Seeds -> regions on the 100 Mb reference (200 MB BWT, larger than L2) in -K 10M-base
     batches, against the CPU oracle on a sample."""
@@ -742,12 +819,16 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             learned = {"error": f"{type(e).__name__}: {e}"}
 
-    big = None
+    big = rrbs = None
     if rank == 0 and args.ref100mb:
         try:
             big = pipeline_ref100mb(ctx)
         except Exception as e:   # reported, never hidden
             big = {"error": f"{type(e).__name__}: {e}"}
+        try:
+            rrbs = pipeline_rrbs(ctx)
+        except Exception as e:   # reported, never hidden
+            rrbs = {"error": f"{type(e).__name__}: {e}"}
 
     tuned = None
     if rank == 0 and not args.no_autotune:
@@ -816,6 +897,7 @@ def run_ours(args, ws, rank, local):
             "learned_schedule": learned,
             "autotune": tuned,
             "pipeline_100mb_ref": big,
+            "pipeline_rrbs_100mb_ref": rrbs,
             "gen_cigar": cig,
             "mate_rescue_sw": msw,
         }
@@ -840,7 +922,8 @@ def main():
     ap.add_argument("--no-cigar", action="store_true", help="skip the bwa_gen_cigar2 block")
     ap.add_argument("--no-matesw", action="store_true", help="skip the mate-rescue Smith-Waterman block")
     ap.add_argument("--ref100mb", action="store_true",
-                    help="add the 100 Mb-reference seed->region block (builds a 100 Mb index: ~2 min the first time)")
+                    help="add the 100 Mb-reference blocks, WGBS-like PE and RRBS-like SE (builds a 100 Mb index: "
+                         "~2 min the first time)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

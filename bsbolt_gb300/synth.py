@@ -299,3 +299,61 @@ def matesw_jobs(n_jobs: int, seed: int = 20261203 + 5, a: int = 1, min_seed_len:
         parts += [q, t]
         off += L + wl
     return jobs, np.concatenate(parts)
+
+
+def rrbs_fragments(contigs, frag_len=(40, 220)):
+    """MspI fragments (C^CGG cuts) of frag_len[0]..frag_len[1] bases: (contig index, start, end)."""
+    out = []
+    for k, (_, g) in enumerate(contigs):
+        g = np.asarray(g)
+        hit = np.nonzero((g[:-3] == 1) & (g[1:-2] == 1) & (g[2:-1] == 2) & (g[3:] == 2))[0] + 1   # cut after the first C
+        if len(hit) < 2:
+            continue
+        ln = np.diff(hit)
+        keep = (ln >= frag_len[0]) & (ln <= frag_len[1])
+        out += [(k, int(a), int(b)) for a, b in zip(hit[:-1][keep], hit[1:][keep])]
+    return out
+
+
+def rrbs_reads_se(contigs, n_reads: int, read_lens=(75, 100), frag_len=(40, 220), meth_cpg: float = 0.7,
+                  meth_ch: float = 0.01, conversion: float = 0.995, err: float = 0.005, seed: int = 20261203,
+                  chunk: int = 200_000):
+    """RRBS-like directional single-end reads: every read starts at an end of an MspI fragment
+    (the top strand's first base or the bottom strand's), is as long as one of read_lens or the
+    fragment if shorter, and many reads share a start (fragments are few).  Methylation,
+    conversion and errors as in bs_reads_pe.  Returns (bases as sequenced, concatenated; offsets)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    frags = rrbs_fragments(contigs, frag_len)
+    if not frags:
+        raise ValueError("no MspI fragments in the length range")
+    W = max(read_lens)
+    # templates: per fragment and strand, the first W bases of the strand's sequence (padded with 4)
+    tmpl = np.full((2 * len(frags), W), 4, np.uint8)
+    tlen = np.zeros(2 * len(frags), np.int64)
+    for i, (k, a, b) in enumerate(frags):
+        f = np.asarray(contigs[k][1][a:b], np.uint8)
+        for s, seq in enumerate((f, COMP[f[::-1]])):
+            n = min(W, len(seq))
+            tmpl[2 * i + s, :n] = seq[:n]
+            tlen[2 * i + s] = n
+    nxt = np.concatenate([tmpl[:, 1:], np.full((len(tmpl), 1), 4, np.uint8)], axis=1)
+    is_c, is_cpg = tmpl == 1, (tmpl == 1) & (nxt == 2)
+    parts, lens = [], []
+    for lo in range(0, n_reads, chunk):
+        m = min(chunk, n_reads - lo)
+        tid = rng.integers(0, len(tmpl), m)
+        L = np.minimum(rng.choice(np.asarray(read_lens), m), tlen[tid])
+        r = tmpl[tid].copy()
+        u = rng.random((m, W), dtype=np.float32)
+        meth = np.where(is_cpg[tid], u < meth_cpg, u < meth_ch)
+        conv = is_c[tid] & ~meth & (rng.random((m, W), dtype=np.float32) < conversion)
+        r[conv] = 3
+        e = (rng.random((m, W), dtype=np.float32) < err) & (r < 4)
+        r[e] = (r[e] + rng.integers(1, 4, int(e.sum()), dtype=np.uint8)) % 4
+        keep = np.arange(W)[None, :] < L[:, None]
+        parts.append(r[keep])
+        lens.append(L)
+    lens = np.concatenate(lens)
+    offs = np.zeros(n_reads + 1, np.int64)
+    offs[1:] = np.cumsum(lens)
+    return np.concatenate(parts), offs
