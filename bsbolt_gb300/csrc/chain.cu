@@ -765,13 +765,15 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
     }
 }
 
+// One warp per read (reads hold a few regions each).
 __global__ void compact_regs(const bsb_reg_t *__restrict__ regs, const int64_t *__restrict__ seed_off,
                              const int64_t *__restrict__ row_off_of_seed, int n_reads, const int *__restrict__ n_regs,
                              const int64_t *__restrict__ out_off, bsb_reg_t *__restrict__ out)
 {
-    for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < n_reads; r += gridDim.x * wpb) {
         const bsb_reg_t *src = regs + row_off_of_seed[seed_off[r]];
-        for (int i = threadIdx.x; i < n_regs[r]; i += blockDim.x) out[out_off[r] + i] = src[i];
+        for (int i = lane; i < n_regs[r]; i += 32) out[out_off[r] + i] = src[i];
     }
 }
 
@@ -982,9 +984,10 @@ __global__ void compact_kept(const bsb_reg_t *__restrict__ regs, const int64_t *
                              const int *__restrict__ n_kept, const int64_t *__restrict__ out_off,
                              bsb_reg_t *__restrict__ out)
 {
-    for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < n_reads; r += gridDim.x * wpb) {
         const bsb_reg_t *src = regs + in_off[r];
-        for (int i = threadIdx.x; i < n_kept[r]; i += blockDim.x) out[out_off[r] + i] = src[i];
+        for (int i = lane; i < n_kept[r]; i += 32) out[out_off[r] + i] = src[i];
     }
 }
 
@@ -1107,7 +1110,8 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                              cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
     if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
-    compact_regs<<<ctx->n_sm * 4, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
+    const int cgrid = (int)((n_reads + 3) / 4) < ctx->n_sm * 16 ? (int)((n_reads + 3) / 4) : ctx->n_sm * 16;
+    compact_regs<<<cgrid, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
     if (dedup) {
         // mem_sort_dedup_patch: regs_out (pre-dedup, at reg_off) -> regs (kept, at reg_off,
         // n_kept per read) -> regs_out again, compacted at the new offsets
@@ -1122,7 +1126,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         dedup_kernel<<<db < ctx->n_sm * 8 ? db : ctx->n_sm * 8, kDedupWarps * 32, 0, st>>>(
             D, B, n_reads, d_reads, d_read_off, reg_off, regs_out, dtmp, iwork, regs, n_kept);
         if ((rc = bsb_cuda(ctx, scan_i32_i64(n_kept, n_reads, kept_off, scan_tmp, st), "kept offsets"))) return rc;
-        compact_kept<<<ctx->n_sm * 4, 128, 0, st>>>(regs, reg_off, n_reads, n_kept, kept_off, regs_out);
+        compact_kept<<<cgrid, 128, 0, st>>>(regs, reg_off, n_reads, n_kept, kept_off, regs_out);
         reg_off = kept_off;
     }
     cudaError_t e = cudaGetLastError();

@@ -395,14 +395,18 @@ __global__ void read_totals(const int *__restrict__ count, const int64_t *__rest
 // element's place is the number of elements with a smaller info, plus the number of
 // equal ones before it (ks_introsort with intv_lt, bwamem.c:92-93; elements with equal
 // info are equal, so the tie rule cannot show).
-constexpr int kSortStage = 1024;
-__global__ void compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads,
-                              const int *__restrict__ count, const int64_t *__restrict__ out_off,
-                              DevIntv *__restrict__ out)
+constexpr int kSortStage = 256, kCompactWarps = 4;
+// One warp per read: the read's two parts merged into info order by rank (keys staged in
+// the warp's slice of shared memory when they fit).
+__global__ void __launch_bounds__(kCompactWarps * 32)
+compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads,
+              const int *__restrict__ count, const int64_t *__restrict__ out_off, DevIntv *__restrict__ out)
 {
-    __shared__ uint64_t key[kSortStage];
+    __shared__ uint64_t keys[kCompactWarps][kSortStage];
+    const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    uint64_t *key = keys[wb];
     const int64_t base_off = offs[0];
-    for (int r = blockIdx.x; r < n_reads; r += gridDim.x) {
+    for (int r = blockIdx.x * kCompactWarps + wb; r < n_reads; r += gridDim.x * kCompactWarps) {
         const int len = (int)(offs[r + 1] - offs[r]);
         const DevIntv *a = padded + 2 * (offs[r] - base_off) + 32 * (int64_t)r;
         const DevIntv *b = a + part_cap0(len);
@@ -411,11 +415,11 @@ __global__ void compact_seeds(const DevIntv *__restrict__ padded, const int64_t 
         const int m = na + nb;
         DevIntv *dst = out + out_off[r];
         const bool staged = m <= kSortStage;
-        __syncthreads();
+        __syncwarp();
         if (staged)
-            for (int i = threadIdx.x; i < m; i += blockDim.x) key[i] = (i < na ? a[i] : b[i - na]).info;
-        __syncthreads();
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            for (int i = lane; i < m; i += 32) key[i] = (i < na ? a[i] : b[i - na]).info;
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) {
             const DevIntv v = i < na ? a[i] : b[i - na];
             int rank = 0;
             for (int j = 0; j < m; ++j) {
@@ -540,8 +544,9 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
     read_totals<<<n_sm * 4, 256, 0, st>>>(d_count, d_offs, n_reads, d_tot);
     e = scan_i32_i64(d_tot, n_reads, d_out_off, d_scan_tmp, st);
     if (e != cudaSuccess) return e;
-    compact_seeds<<<n_sm * 4, 128, 0, st>>>((const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off,
-                                            (DevIntv *)d_out);
+    const int cb = (int)((n_reads + kCompactWarps - 1) / kCompactWarps);
+    compact_seeds<<<cb < n_sm * 16 ? cb : n_sm * 16, kCompactWarps * 32, 0, st>>>(
+        (const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off, (DevIntv *)d_out);
     return cudaGetLastError();
 }
 
