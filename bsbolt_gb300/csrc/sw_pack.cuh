@@ -70,9 +70,23 @@ __device__ __forceinline__ uint32_t lane_up(uint32_t x, int tid, unsigned gm)   
     return tid ? r : r << 16;
 }
 
-// maximum / minimum over the group's threads of a non-negative value (one REDUX instruction)
-__device__ __forceinline__ int grp_max(unsigned gm, int v) { return (int)__reduce_max_sync(gm, (unsigned)v); }
-__device__ __forceinline__ int grp_min(unsigned gm, int v) { return (int)__reduce_min_sync(gm, (unsigned)v); }
+// maximum / minimum over the group's threads (G of them): a segmented butterfly, since a
+// reduction with per-group member masks is carried out one mask at a time
+template <int G>
+__device__ __forceinline__ int grp_max(unsigned gm, int v)
+{
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(gm, v, d, G));
+    return v;
+}
+
+template <int G>
+__device__ __forceinline__ int grp_min(unsigned gm, int v)
+{
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(gm, v, d, G));
+    return v;
+}
 
 // Segment counts per pass instance: a bucket of B consecutive counts (SLMAX - B, SLMAX] shares
 // one instance, the exact count sl a runtime value: the striping uses sl, segments at and past
@@ -166,7 +180,7 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
 #pragma unroll
         for (int j = SLMIN; j < SLMAX; ++j)
             if (j == sl - 1) hlast = H[j];
-        const int imax = grp_max(gm, max((int)(mx & 0xffffu), (int)(mx >> 16)));
+        const int imax = grp_max<G>(gm, max((int)(mx & 0xffffu), (int)(mx >> 16)));
         if (imax > gmax || imax >= minsc) {
             if (imax >= minsc) {                  // the rows of the suboptimal score (ksw.c:182-189)
                 if (n_b == 0 || last_row + 1 != i) {
@@ -199,8 +213,8 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
             if (v0 > best || (v0 == best && c0 < col)) best = v0, col = c0;
             if (v1 > best || (v1 == best && c1 < col)) best = v1, col = c1;
         }
-        const int gbest = grp_max(gm, best);
-        r.qe = grp_min(gm, best == gbest ? col : 0x7fffffff);
+        const int gbest = grp_max<G>(gm, best);
+        r.qe = grp_min<G>(gm, best == gbest ? col : 0x7fffffff);
         if (n_b) {                                 // ksw.c:218-225: the best row outside te +- d
             const int d = (r.score + S.qmax - 1) / S.qmax, low = te - d, high = te + d;
             int bs = -1, bk = 0x7fffffff;
@@ -209,8 +223,8 @@ __device__ __noinline__ PassOut pack_pass(const PackParams &S, const uint32_t *p
                 const int2 e = bbuf[k];
                 if ((e.y < low || e.y > high) && e.x > bs) bs = e.x, bk = k;
             }
-            const int gbs = grp_max(gm, bs + 1) - 1;
-            const int gk = grp_min(gm, bs == gbs ? bk : 0x7fffffff);
+            const int gbs = grp_max<G>(gm, bs);
+            const int gk = grp_min<G>(gm, bs == gbs ? bk : 0x7fffffff);
             if (gbs > r.score2 && gk != 0x7fffffff) r.score2 = gbs, r.te2 = bbuf[gk].y;
         }
     }
