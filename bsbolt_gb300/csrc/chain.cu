@@ -589,14 +589,16 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                  const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
                  const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
                  const DevChain *__restrict__ chains, const int *__restrict__ n_chains, uint64_t *__restrict__ srt_buf,
-                 bsb_reg_t *__restrict__ regs, int *__restrict__ n_regs, int *__restrict__ next)
+                 bsb_reg_t *__restrict__ regs, int *__restrict__ n_regs, int *__restrict__ next,
+                 const int *__restrict__ order)
 {
     const int lane = threadIdx.x & 31;
     for (;;) {
-        int r = 0;
-        if (lane == 0) r = atomicAdd(next, 1);
-        r = __shfl_sync(BSB_FULL_MASK, r, 0);
-        if (r >= n_reads) break;
+        int k = 0;
+        if (lane == 0) k = atomicAdd(next, 1);
+        k = __shfl_sync(BSB_FULL_MASK, k, 0);
+        if (k >= n_reads) break;
+        const int r = order[k];
         const int64_t R0 = row_off_of_seed[seed_off[r]];
         const int nc = n_chains[r];
         const int l_query = (int)(read_off[r + 1] - read_off[r]);
@@ -762,6 +764,33 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
             }
         }
         if (lane == 0) n_regs[r] = nav;
+    }
+}
+
+// The order chain2aln_kernel takes reads in: most chains first (reads are independent, so the
+// order changes no result; it shortens the tail a few repeat-laden reads would otherwise set).
+constexpr int kOrderBins = 64;
+
+__device__ __forceinline__ int order_bin(int nc) { return kOrderBins - 1 - (nc < kOrderBins - 1 ? nc : kOrderBins - 1); }
+
+__global__ void order_hist(const int *__restrict__ n_chains, int n_reads, int *__restrict__ cnt)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x)
+        atomicAdd(&cnt[order_bin(n_chains[r])], 1);
+}
+
+__global__ void order_scatter(const int *__restrict__ n_chains, int n_reads, const int *__restrict__ cnt,
+                              int *__restrict__ cur, int *__restrict__ order)
+{
+    __shared__ int off[kOrderBins];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < kOrderBins; ++b) off[b] = acc, acc += cnt[b];
+    }
+    __syncthreads();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        const int b = order_bin(n_chains[r]);
+        order[off[b] + atomicAdd(&cur[b], 1)] = r;
     }
 }
 
@@ -1054,6 +1083,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     const size_t o_ctrl = off; off += al(sizeof(int) * 4);
     const size_t o_regoff = off; off += al(sizeof(int64_t) * (n_reads + 1));
     const size_t o_out = off; off += al(sizeof(bsb_reg_t) * Rb);
+    const size_t o_order = off; off += al(sizeof(int) * (n_reads + 1)) + al(sizeof(int) * 2 * kOrderBins);
     const size_t o_dtmp = off; off += dedup ? al(sizeof(bsb_reg_t) * Rb) : 0;
     const size_t o_dn = off; off += dedup ? al(sizeof(int) * (n_reads + 1)) : 0;
     const size_t o_doff = off; off += dedup ? al(sizeof(int64_t) * (n_reads + 1)) : 0;
@@ -1096,19 +1126,27 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     P.pack16 = 0;
     chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
                                                  pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
+    int *order = (int *)(A + o_order);
+    int *ocnt = (int *)(A + o_order + al(sizeof(int) * (n_reads + 1)));
+    {
+        const int ob = (int)((n_reads + 255) / 256) < ctx->n_sm * 4 ? (int)((n_reads + 255) / 256) : ctx->n_sm * 4;
+        if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ocnt, 0, sizeof(int) * 2 * kOrderBins, st), "read order"))) return rc;
+        order_hist<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt);
+        order_scatter<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt, ocnt + kOrderBins, order);
+    }
     // every extension of these reads fits (max_len + 1) columns: the narrowest variant that holds them
     if (max_len <= 127)
         chain2aln_kernel<4><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
     else if (max_len <= 159)
         chain2aln_kernel<5><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
     else if (max_len <= 255)
         chain2aln_kernel<8><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
     else
         chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1);
+                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
     if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
     const int cgrid = (int)((n_reads + 3) / 4) < ctx->n_sm * 16 ? (int)((n_reads + 3) / 4) : ctx->n_sm * 16;
     compact_regs<<<cgrid, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
