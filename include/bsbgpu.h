@@ -324,7 +324,8 @@ int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int64_t crick_
  * width, the lazy-F loop, padded query columns.  One case differs by design: a
  * byte-lane pass that saturates (score 255) with KSW_XSTART leaves tb = qb = -1,
  * where the reference profiles a zero-length query.  Needs a positive matrix
- * entry.  Host buffers; synchronous. */
+ * entry; at most 2^31 - 1 jobs per call, queries up to BSB_SW_MAX_QLEN.  Host
+ * buffers; synchronous. */
 #define BSB_SW_MAX_QLEN 1024
 typedef struct {
     int64_t qoff, toff;
