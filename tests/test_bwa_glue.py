@@ -112,3 +112,15 @@ def test_glue_matesw_results_are_served(data):
     assert kept > 0 and served > 0, line
     env = dict(os.environ, BSB_SHIM_PERTURB_SW="1")
     assert run_mem(GLUE, fa, r1, r2, extra, env) != run_mem(BWA, fa, r1, r2, extra)
+
+
+def test_glue_single_end_identical(data):
+    """Single-end reads (worker2 without pairing or mate rescue) through the glue: the same SAM."""
+    fa, r1, _ = data
+    extra = ["-L", "5,5"]
+    cmd = ["-Y", "-t", "4", "-K", "10000000"] + extra + [fa, r1]
+    ref = subprocess.run([BWA, "mem"] + cmd, capture_output=True, check=True).stdout.decode().splitlines()
+    glue = subprocess.run([GLUE, "mem"] + cmd, capture_output=True, check=True).stdout.decode().splitlines()
+    ref = [x for x in ref if not x.startswith("@PG")]
+    glue = [x for x in glue if not x.startswith("@PG")]
+    assert len(ref) > 3000 and glue == ref
