@@ -211,7 +211,9 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         // and the non-zero cells.  Column 0's shifted H needs the left lane's last column
         // and column C2-1 of this lane, so it is finished after the loop.
         const int rend = end - base;               // |rend| <= 1023: exact in 16 bits
-        const uint32_t t_lt = pk16(rend, rend - C2), t_le = pk16(rend + 1, rend + 1 - C2);
+        // per half: ltm(u) = [column < rend]; lem(u) = [column <= rend] = ltm(u - 1)
+        const uint32_t t_lt = pk16(rend, rend - C2);
+        uint32_t ltm_prev = below16(t_lt, -1) * 0xffffu;
         uint32_t kmx = 0;                          // per half: max of H*16 + u over band columns
         uint32_t cF = carry2;                      // per half: the carry minus e_ins per column
         uint32_t Hprev = 0, nE0 = 0, lem0 = 0, nzw = 0;
@@ -220,7 +222,8 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
             const uint32_t F = __vimax_s16x2_relu(cF, Pf[u]);            // F >= 0 (ksw.c:446-447)
             cF = __viaddmax_s16x2(cF, ne_ins, 0x80008000u);
             const uint32_t H = __vimax3_s16x2(Mv[u], Es[u], F);
-            const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = below16(t_le, u) * 0xffffu;
+            const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = ltm_prev;
+            ltm_prev = ltm;
             kmx = __vimax_s16x2_relu(kmx, (H & ltm) * 16u + pk16(u, u));   // ties: the later column
             const uint32_t nE = (En[u] & ltm) | (Es[u] & ~lem);
             Es[u] = nE;
