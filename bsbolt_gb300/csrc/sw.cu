@@ -17,7 +17,7 @@
 //                          passes in the order of a host counting sort by segments and length,
 //                          sw_rev_scatter grouping the jobs that want start positions by the
 //                          segment count of their reversed query, then their reverse passes
-//   sw_pack_kernel<8, ..>  the same for word-lane jobs of 1..32 segments whose scores stay
+//   sw_pack_kernel<8, ..>  the same for word-lane jobs of 1..40 segments whose scores stay
 //                          clear of 16-bit saturation (sw_pack16a.cu, sw_pack16b.cu), on a
 //                          second stream
 //   sw_kernel<16>, <8>     every other job (longer queries, extreme scores or penalties, empty
@@ -313,7 +313,7 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
     if (S.qmax < 1) return bsb_fail(ctx, BSB_EINVAL, "the scoring matrix needs a positive entry");
     if (n == 0) return 0;
     if (n > 0x7fffffff) return bsb_fail(ctx, BSB_EINVAL, "at most 2^31 - 1 jobs per call");
-    // Four job lists: packed byte lanes (1..16 segments), packed word lanes (1..32 segments, when
+    // Four job lists: packed byte lanes (1..16 segments), packed word lanes (1..40 segments, when
     // 16-bit arithmetic without saturation is exact: qlen * max score <= 32640 and penalties
     // below 32768), then the one-lane byte and word jobs.  The packed lists are in counting-sort
     // order by segment count and then target length, both descending.
@@ -426,10 +426,10 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
         if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->ms.fork, st), "SW fork")) ||
             (rc = bsb_cuda(ctx, cudaStreamWaitEvent(st2, ctx->ms.fork, 0), "SW fork")))
             return rc;
-        if (n_p16) {   // word lanes: the 17..32-segment part of the list, then the 1..16 part
+        if (n_p16) {   // word lanes: the 17..40-segment part of the list, then the 1..16 part
             const int32_t *l16 = d_list + n_p8;
             int32_t *r16 = d_rlist + n_p8;
-            const int n_hi = (int)(kcnt[(size_t)(kKeys8 + 16 * kLenBins - 1)] - n_p8), n16 = (int)n_p16;
+            const int n_hi = (int)(kcnt[(size_t)(kKeys8 + (kPackMaxSeg16 - 16) * kLenBins - 1)] - n_p8), n16 = (int)n_p16;
             if ((rc = bsb_cuda(ctx, sw_pack16_run_hi(false, P16, d_jobs, d_seq, l16, n_hi, d_boff, d_b, d_out, d_rsl,
                                                      ctr16, 0, ctx->n_sm, st2), "SW word-lane kernels")) ||
                 (rc = bsb_cuda(ctx, sw_pack16_run_lo(false, P16, d_jobs, d_seq, l16 + n_hi, n16 - n_hi, d_boff, d_b,

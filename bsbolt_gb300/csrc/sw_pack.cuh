@@ -27,7 +27,7 @@ namespace bsbsw {
 constexpr int kXByte = 0x10000, kXStop = 0x20000, kXSubo = 0x40000, kXStart = 0x80000;
 constexpr int kPackBlock = 128;
 constexpr int kPackMaxSeg8 = 16;    // byte lanes: queries of up to 256 bases
-constexpr int kPackMaxSeg16 = 32;   // word lanes: queries of up to 256 bases
+constexpr int kPackMaxSeg16 = 40;   // word lanes: queries of up to 320 bases
 // counter block of one lane width: [0..3] queues, [kRcnt + s] reverse passes of s segments,
 // [kRcur + s] their scatter cursors
 constexpr int kRcnt = 64, kRcur = 128, kCtrInts = 192;
@@ -364,7 +364,7 @@ cudaError_t sw_pack_run(bool rev, const PackParams &S, const bsb_sw_job_t *jobs,
 }
 
 // The word-lane ranges, each in a translation unit of its own (sw_pack16a.cu: 1..16 segments,
-// sw_pack16b.cu: 17..32) so that they compile side by side.
+// sw_pack16b.cu: 17..40) so that they compile side by side.
 cudaError_t sw_pack16_run_lo(bool rev, const PackParams &S, const bsb_sw_job_t *jobs, const uint8_t *seq,
                              const int32_t *list, int n, const int64_t *boff, int2 *bscratch, bsb_kswr_t *out,
                              uint8_t *rsl, int *ctr, int q, int n_sm, cudaStream_t st);

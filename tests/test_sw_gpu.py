@@ -84,3 +84,34 @@ def test_align2_scorings_match_oracle(gpu_ctx, scoring):
     out = matesw.align2_batch(gpu_ctx, jobs.view(matesw.JOB_DTYPE), seq, mat, o_del, e_del, o_ins, e_ins)
     ref = oracle.align2_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, n_threads=8)
     assert_same(out, ref, tags, f"scoring {scoring}")
+
+
+@pytest.mark.parametrize("a,lo,hi", [(1, 250, 330), (2, 125, 200)])
+def test_align2_long_word_lane_mates(gpu_ctx, a, lo, hi):
+    """Mates too long for byte lanes (qlen * a >= 250): word lanes of 17-42 segments, the
+    packed kernels up to 40 segments (320 bases) and the one-lane kernel beyond."""
+    rng = np.random.Generator(np.random.PCG64(20261203 + 90 + a))
+    jobs, parts, off = [], [], 0
+    for k in range(1500):
+        L = int(rng.integers(lo, hi + 1))
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        wl = int(rng.integers(L + 20, L + 500))
+        t = rng.integers(0, 4, wl).astype(np.uint8)
+        if k % 4:
+            m = q.copy()
+            sub = rng.random(L) < 0.05
+            m[sub] = rng.integers(0, 4, int(sub.sum()))
+            at = int(rng.integers(0, wl - L + 1))
+            t[at:at + L] = m
+        xtra = matesw.matesw_xtra(L, a)
+        jobs.append((off, off + L, L, wl, xtra, 0))
+        parts += [q, t]
+        off += L + wl
+    jobs = np.array(jobs, matesw.JOB_DTYPE)
+    seq = np.concatenate(parts)
+    assert not (jobs["xtra"] & matesw.KSW_XBYTE).any()
+    mat = synth.fill_scmat(a, 4)
+    out = matesw.align2_batch(gpu_ctx, jobs, seq, mat, 6, 1, 6, 1)
+    ref = oracle.align2_batch(jobs.view(golden_data.SW_JOB_DTYPE), seq, mat, 6, 1, 6, 1, n_threads=8)
+    assert_same(out, ref, None, f"a={a} qlen {lo}-{hi}")
+    assert (out["tb"] >= 0).sum() > 800
