@@ -406,7 +406,7 @@ int mem_matesw_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *b
         for (i = 0; i < 2; ++i) {
             const bseq1_t *m = &seqs[id + !i];
             int taken = 0;
-            if (m->l_seq > BSB_SW_MAX_QLEN) continue;
+            if (m->l_seq <= 0 || m->l_seq > BSB_SW_MAX_QLEN) continue;   /* left to the reference */
             for (j = 0; j < (int)a[i].n && taken < opt->max_matesw; ++j) {
                 if (a[i].a[j].score < a[i].a[0].score - opt->pen_unpaired) continue;
                 ++taken;
