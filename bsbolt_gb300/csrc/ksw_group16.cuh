@@ -230,7 +230,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
             if (u > 0) {
                 const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);
                 Hs[u] = nH;
-                nzw |= __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;
+                nzw += __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;     // distinct bits: + is |, one shift-add
             } else {
                 nE0 = nE, lem0 = lem;
             }
@@ -241,7 +241,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         {
             const uint32_t nH = (pk16(Hleft, lo16(Hprev)) & lem0) | (Hs[0] & ~lem0);
             Hs[0] = nH;
-            nzw |= __vimin_s16x2_relu(nH | nE0, 0x00010001u);
+            nzw += __vimin_s16x2_relu(nH | nE0, 0x00010001u);
         }
         uint32_t nzb = (nzw & 0xffffu) | (nzw >> 16) << C2;
         nzb &= rend < 0 ? 0u : rend >= C - 1 ? 0xffffffffu : (2u << rend) - 1u;   // columns s <= rend
