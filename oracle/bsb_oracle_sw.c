@@ -113,6 +113,7 @@ static orc_kswr_t sw_pass(const prof_t *q, int tlen, const uint8_t *target, int 
                 h[l] = H0[x];
             }
         }
+#ifndef ORC_SW_LAZY_F_CLOSED_FORM
         /* lazy F (ksw.c:166-177 / 284-295): at most 16 passes, each shifting f up one lane */
         for (int k = 0; k < 16; ++k) {
             for (int l = p - 1; l > 0; --l) f[l] = f[l - 1];
@@ -141,6 +142,46 @@ static orc_kswr_t sw_pass(const prof_t *q, int tlen, const uint8_t *target, int 
             }
             if (done) break;
         }
+#else
+        /* Test build only (-DORC_SW_LAZY_F_CLOSED_FORM): the closed form the GPU kernels use
+         * where oe_ins >= e_ins as the lanes hold them -- H(l, j) raised to relu(G(l) - j*e_ins),
+         * G(0) = 0, G(l) = max(x(l), relu(G(l-1) - slen*e_ins)), x(l) the f leaving lane l-1,
+         * applied when a lane fails the reference's first exit test.  The default build runs the
+         * loop above, as the reference does. */
+        for (int l = p - 1; l > 0; --l) f[l] = f[l - 1];
+        f[0] = 0;
+        if (slen) {
+            int any = 0, h0[16];
+            for (int l = 0; l < p; ++l) {
+                int hh, fn;
+                if (u8) {
+                    h0[l] = H1[l] > f[l] ? H1[l] : f[l];
+                    hh = sat_u8(h0[l] - poe_ins), fn = sat_u8(f[l] - pe_ins);
+                    any |= fn > hh;
+                } else {
+                    h0[l] = max_s16(H1[l], f[l]);
+                    hh = subs_u16(h0[l], poe_ins), fn = subs_u16(f[l], pe_ins);
+                    any |= (int16_t)fn > (int16_t)hh;
+                }
+            }
+            if (any) {
+                long d = (long)pe_ins * slen, G[16];
+                G[0] = f[0];
+                for (int l = 1; l < p; ++l) {
+                    const long a = G[l - 1] - d > 0 ? G[l - 1] - d : 0;
+                    G[l] = f[l] > a ? f[l] : a;
+                }
+                for (int l = 0; l < p; ++l)
+                    for (int j = 0; j < slen; ++j) {
+                        const long g = G[l] - (long)pe_ins * j > 0 ? G[l] - (long)pe_ins * j : 0;
+                        const int x = j * p + l;
+                        if (u8 ? g > H1[x] : g > (int16_t)H1[x]) H1[x] = (int)g;
+                    }
+            } else {
+                for (int l = 0; l < p; ++l) H1[l] = h0[l];
+            }
+        }
+#endif
         int imax = 0;
         for (int l = 0; l < p; ++l) imax = u8 ? (imax > mx[l] ? imax : mx[l]) : max_s16(imax, mx[l]);
         if (!u8) imax = (uint16_t)imax;                 /* _mm_extract_epi16 (ksw.c:249) */
