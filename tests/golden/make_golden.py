@@ -6,7 +6,8 @@ sources (this script, and only this script, reads them):
     make -f oracle/Makefile.ref -j8          # reference objects -> oracle/_ref/
     python tests/golden/make_golden.py ksw     # ksw_extend2 tuples
     python tests/golden/make_golden.py index   # reference `bwa index` checksums
-    python tests/golden/make_golden.py reads   # seeds / chains / regions / job stream
+    python tests/golden/make_golden.py reads   # seeds / chains / regions (before and after
+                                               # mem_sort_dedup_patch) / job stream
     python tests/golden/make_golden.py cigar   # bwa_gen_cigar2 records (CIGAR, MD, XB)
     python tests/golden/make_golden.py sw      # ksw_align2 results (mate-rescue Smith-Waterman)
 
