@@ -124,3 +124,14 @@ def test_glue_single_end_identical(data):
     ref = [x for x in ref if not x.startswith("@PG")]
     glue = [x for x in glue if not x.startswith("@PG")]
     assert len(ref) > 3000 and glue == ref
+
+
+def test_glue_without_mate_rescue(data):
+    """`-S` (MEM_F_NO_RESCUE): the rescue pre-pass keeps nothing and the SAM stays the reference's."""
+    fa, r1, r2 = data
+    extra = ["-L", "5,5", "-S"]
+    assert run_mem(GLUE, fa, r1, r2, extra) == run_mem(BWA, fa, r1, r2, extra)
+    cmd = [GLUE, "mem", "-Y", "-t", "4", "-K", "10000000"] + extra + [fa, r1, r2]
+    res = subprocess.run(cmd, capture_output=True, check=True, env=dict(os.environ, BSB_SHIM_STATS="1"))
+    line = [x for x in res.stderr.decode().splitlines() if x.startswith("[bsb_glue] matesw jobs")][-1]
+    assert int(line.split()[4]) == 0 and int(line.split()[6]) == 0, line
