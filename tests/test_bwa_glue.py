@@ -135,3 +135,14 @@ def test_glue_without_mate_rescue(data):
     res = subprocess.run(cmd, capture_output=True, check=True, env=dict(os.environ, BSB_SHIM_STATS="1"))
     line = [x for x in res.stderr.decode().splitlines() if x.startswith("[bsb_glue] matesw jobs")][-1]
     assert int(line.split()[4]) == 0 and int(line.split()[6]) == 0, line
+
+
+@pytest.mark.parametrize("scoring", [["-A", "2", "-B", "5", "-O", "5,7", "-E", "2,1"],
+                                     ["-A", "3", "-B", "5", "-O", "6,6", "-E", "1,1", "-T", "60"]])
+def test_glue_other_scorings(data, scoring):
+    """Other scoring through every hook: with -A 3 a 100-base mate's rescue runs on word lanes
+    (qlen * a >= 250) and the CIGAR band and dedup thresholds move."""
+    fa, r1, r2 = data
+    extra = scoring + ["-L", "5,5"]
+    ref = run_mem(BWA, fa, r1, r2, extra)
+    assert len(ref) > 6000 and run_mem(GLUE, fa, r1, r2, extra) == ref
