@@ -1245,10 +1245,14 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
     if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, dedup, &d_regs,
                                  &d_reg_off, &n_regs)))
         return rc;
-    if (n_regs > max_regs)
-        return bsb_fail(ctx, BSB_EINVAL, "%lld regions do not fit max_regs %lld", (long long)n_regs, (long long)max_regs);
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(regs_off, d_reg_off, off_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H offsets")))
         return rc;
+    if (n_regs > max_regs) {
+        // the offsets still go back: regs_off[n_reads] tells the caller the size to call again with
+        if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "align batch"))) return rc;
+        return bsb_fail(ctx, BSB_ECAPACITY, "%lld regions do not fit max_regs %lld", (long long)n_regs,
+                        (long long)max_regs);
+    }
     if (n_regs > 0 &&
         (rc = bsb_cuda(ctx, cudaMemcpyAsync(regs, d_regs, sizeof(bsb_reg_t) * n_regs, cudaMemcpyDeviceToHost, ctx->stream),
                        "D2H regions")))

@@ -37,11 +37,15 @@ void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o)
     memcpy(o->mat, opt->mat, 25);
 }
 
+static int64_t g_align_regrown;   /* batches whose region buffer had to grow */
+
+int64_t mem_align_regrown(void) { return __atomic_load_n(&g_align_regrown, __ATOMIC_RELAXED); }
+
 int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
                         int n, bseq1_t *seqs, mem_alnreg_v *regs)
 {
     bsb_align_opt_t o;
-    int64_t *offs, total = 0, *roff;
+    int64_t *offs, total = 0, *roff, cap;
     uint8_t *buf;
     bsb_reg_t *out;
     int i, j, rc;
@@ -58,9 +62,19 @@ int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns,
         memcpy(buf + offs[i], s, seqs[i].l_seq);
         offs[i + 1] = offs[i] + seqs[i].l_seq;
     }
-    /* every region comes from one extended seed, so 4 per base is a safe bound */
-    out = (bsb_reg_t *)malloc(sizeof(bsb_reg_t) * (4 * total + 64 * (int64_t)n + 1));
-    rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, 4 * total + 64 * (int64_t)n, roff);
+    /* A first guess at the region count; a read in a family of many copies can have up to
+     * max_occ regions per seed (bwamem.c:281-283), and then the library answers
+     * BSB_ECAPACITY with the count it needs in roff[n], and the batch runs again. */
+    cap = 4 * total + 64 * (int64_t)n;
+    out = (bsb_reg_t *)malloc(sizeof(bsb_reg_t) * (cap + 1));
+    rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, cap, roff);
+    if (rc == BSB_ECAPACITY && roff[n] > cap) {
+        __atomic_add_fetch(&g_align_regrown, 1, __ATOMIC_RELAXED);
+        cap = roff[n];
+        free(out);
+        out = (bsb_reg_t *)malloc(sizeof(bsb_reg_t) * (cap + 1));
+        rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, cap, roff);
+    }
     if (rc == 0) {
         for (i = 0; i < n; ++i) {
             mem_alnreg_v *v = &regs[i];

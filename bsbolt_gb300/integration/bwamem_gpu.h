@@ -27,6 +27,9 @@ void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o);
  * malloc()ed (worker2 frees it).  Returns 0 or a BSB_E* code. */
 int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
                         int n, bseq1_t *seqs, mem_alnreg_v *regs);
+/* Batches so far whose first region buffer was too small (reads in a family of more
+ * copies than a read has bases / 4, say) and ran again with the size the library gave. */
+int64_t mem_align_regrown(void);
 
 /* CIGAR pre-pass (bwa_gen_cigar2 on the GPU).  Called after mem_align_batch_gpu
  * and before worker2: runs bsb_gen_cigar_batch for every region of the batch

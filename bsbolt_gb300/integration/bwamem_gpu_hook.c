@@ -1,0 +1,141 @@
+/*
+ * bwamem_gpu_hook.c -- plugs the GPU path into an unmodified build of BSBolt's
+ * BWA fork at link time, so `bwa mem` runs its worker1 pass, its CIGAR/MD/XB
+ * strings and its mate-rescue Smith-Waterman on the GPU without a source edit.
+ *
+ * Link the BWA objects with this file, bwamem_gpu.c and libbsbgpu.so, and
+ *   -Wl,--wrap=kt_for -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2
+ * (bsbolt_gb300/integration/Makefile does this and names the result bwa_gpu).
+ *
+ * kt_for is called only by mem_process_seqs (bwamem.c:1336 and :1344), twice
+ * per -K batch: worker1 (mem_align1_core per read) and then, after
+ * mem_pestat, worker2 (pairing, rescue, SAM).  The wrapper therefore
+ *   - on the first call of a batch, runs mem_align_batch_gpu and the CIGAR
+ *     pre-pass instead of worker1 (the context and the device index are made
+ *     on the first batch from the arrays bwa_idx_load already holds);
+ *   - on the second, runs the mate-rescue pre-pass with the batch's pes and
+ *     then the reference's own worker2 loop over its threads.
+ * A library error ends the run through err_fatal, as the reference ends on
+ * its own errors.  BSB_GPU_DEVICE picks the CUDA device (default 0);
+ * BSB_GPU_STATS=1 prints, at exit, how many CIGAR and rescue calls the GPU
+ * results answered, and the time spent in the GPU passes.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+
+#include "bntseq.h"
+#include "bwt.h"
+#include "utils.h"
+#include "bwamem_gpu.h"
+
+/* the leading fields of worker_t (bwamem.c:1274-1285), as kt_for receives them */
+typedef struct {
+    const mem_opt_t *opt;
+    const bwt_t *bwt;
+    const bntseq_t *bns;
+    const uint8_t *pac;
+    const uint8_t *opac;
+    const mem_pestat_t *pes;
+    void **aux;
+    bseq1_t *seqs;
+    mem_alnreg_v *regs;
+    int64_t n_processed;
+} hook_worker_t;
+
+static bsb_ctx *g_hook_ctx;
+static long g_hook_calls;
+static double g_t_align, g_t_cigar, g_t_sw;
+static int64_t g_cig_kept, g_cig_served, g_sw_kept, g_sw_served, g_reads;
+
+static double hook_now(void)
+{
+    struct timeval tv;
+    gettimeofday(&tv, 0);
+    return tv.tv_sec + tv.tv_usec * 1e-6;
+}
+
+static void hook_take_stats(void)
+{
+    int64_t k, s;
+    mem_gen_cigar_stats(&k, &s);
+    g_cig_kept += k, g_cig_served += s;
+    mem_matesw_stats(&k, &s);
+    g_sw_kept += k, g_sw_served += s;
+}
+
+static void hook_report(void)
+{
+    hook_take_stats();
+    fprintf(stderr, "[bsb_gpu] reads %lld; GPU time: regions %.3f s, cigar %.3f s, rescue %.3f s\n",
+            (long long)g_reads, g_t_align, g_t_cigar, g_t_sw);
+    fprintf(stderr, "[bsb_gpu] cigar records kept %lld served %lld\n", (long long)g_cig_kept,
+            (long long)g_cig_served);
+    fprintf(stderr, "[bsb_gpu] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
+    fprintf(stderr, "[bsb_gpu] region buffer regrown %lld\n", (long long)mem_align_regrown());
+}
+
+static void hook_fail(bsb_ctx *ctx, int rc, const char *what)
+{
+    err_fatal("bwa_gpu", "%s: %s (%s)", what, ctx ? bsb_last_error(ctx) : "no context", bsb_strerror(rc));
+}
+
+/* One context per process, with the index bwa_idx_load holds (bwa.c:363-524): the
+ * occurrence array, the sampled SA, the converted pac, the contig table and the
+ * original-sequence opac the methylation strings read. */
+static void hook_init(const hook_worker_t *w)
+{
+    const bwt_t *bwt = w->bwt;
+    const bntseq_t *bns = w->bns;
+    bsb_index_view_t v;
+    int64_t *ann_off;
+    int32_t *ann_len;
+    const char *dev = getenv("BSB_GPU_DEVICE");
+    int i, rc;
+    if ((rc = bsb_ctx_create(dev ? atoi(dev) : 0, &g_hook_ctx))) hook_fail(g_hook_ctx, rc, "GPU context");
+    ann_off = (int64_t *)malloc(sizeof(int64_t) * (bns->n_seqs + 1));
+    ann_len = (int32_t *)malloc(sizeof(int32_t) * (bns->n_seqs + 1));
+    for (i = 0; i < bns->n_seqs; ++i) ann_off[i] = bns->anns[i].offset, ann_len[i] = bns->anns[i].len;
+    memset(&v, 0, sizeof v);
+    v.primary = bwt->primary;
+    for (i = 0; i < 5; ++i) v.L2[i] = bwt->L2[i];
+    v.bwt = bwt->bwt, v.bwt_size = bwt->bwt_size;
+    v.sa = bwt->sa, v.n_sa = bwt->n_sa, v.sa_intv = bwt->sa_intv;
+    v.pac = w->pac, v.l_pac = bns->l_pac;
+    v.n_seqs = bns->n_seqs, v.ann_offset = ann_off, v.ann_len = ann_len;
+    if ((rc = bsb_index_upload(g_hook_ctx, &v))) hook_fail(g_hook_ctx, rc, "index upload");
+    if (w->opac && (rc = bsb_index_upload_opac(g_hook_ctx, w->opac, bns->l_pac)))
+        hook_fail(g_hook_ctx, rc, "opac upload");
+    free(ann_off);
+    free(ann_len);
+    if (getenv("BSB_GPU_STATS")) atexit(hook_report);
+}
+
+void __real_kt_for(int n_threads, void (*func)(void *, long, int), void *data, long n);
+
+void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, long n)
+{
+    hook_worker_t *w = (hook_worker_t *)data;
+    const int n_reads = (w->opt->flag & MEM_F_PE) ? (int)(n << 1) : (int)n;
+    double t0, t1;
+    int rc;
+    if ((g_hook_calls++ & 1) == 0) {   /* worker1 of mem_process_seqs */
+        if (!g_hook_ctx) hook_init(w);
+        hook_take_stats();             /* the previous batch's counts, before the pre-passes reset them */
+        t0 = hook_now();
+        if ((rc = mem_align_batch_gpu(g_hook_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs)))
+            hook_fail(g_hook_ctx, rc, "GPU alignment");
+        t1 = hook_now();
+        if ((rc = mem_gen_cigar_prepass_gpu(g_hook_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs)))
+            hook_fail(g_hook_ctx, rc, "GPU CIGAR pre-pass");
+        g_t_align += t1 - t0, g_t_cigar += hook_now() - t1, g_reads += n_reads;
+        return;
+    }
+    /* worker2: w->pes now holds mem_pestat's (or -I's) insert-size model */
+    t0 = hook_now();
+    if ((rc = mem_matesw_prepass_gpu(g_hook_ctx, w->opt, w->bns, w->pac, w->pes, n_reads, w->seqs, w->regs)))
+        hook_fail(g_hook_ctx, rc, "GPU mate-rescue pre-pass");
+    g_t_sw += hook_now() - t0;
+    __real_kt_for(n_threads, func, data, n);
+}

@@ -248,7 +248,11 @@ typedef struct {
  * reference's order, are regs[regs_off[r] .. regs_off[r+1]).  Needs an index
  * with pac and contig table.  Supports reads up to 512 bp whose length keeps
  * mem_flt_chained_seeds a no-op (bwamem.c:606), indexes without ALT contigs
- * (BSBolt writes none).  Host buffers; synchronous. */
+ * (BSBolt writes none).  Host buffers; synchronous.  When the batch has more
+ * regions than max_regs (mem_chain samples up to max_occ rows per seed, so a
+ * read in a large repeat family can have hundreds), nothing is written to regs,
+ * regs_off is filled all the same (regs_off[n_reads] = the regions needed) and
+ * the call returns BSB_ECAPACITY: call again with a buffer that large. */
 int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
@@ -261,7 +265,8 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_rea
  * identical regions dropped.  Read r's regions, in the order mem_align1_core
  * returns them, are regs[regs_off[r] .. regs_off[r+1]); n_comp as the reference
  * sets it.  Marking regions on ALT contigs (bwamem.c:1189-1193) stays with the
- * caller (BSBolt's indexes have none).  Same limits as bsb_align_regs_batch. */
+ * caller (BSBolt's indexes have none).  Same limits, and the same BSB_ECAPACITY
+ * answer to a short regs buffer, as bsb_align_regs_batch. */
 int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);

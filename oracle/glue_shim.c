@@ -60,7 +60,11 @@ static int shim_align(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, c
         free(out.regs_off);
         out.regs = kept, out.regs_off = kept_off;
     }
-    if (rc == 0 && out.regs_off[n_reads] > max_regs) rc = BSB_EINVAL;
+    if (rc == 0 && out.regs_off[n_reads] > max_regs) {   /* the library's answer to a short buffer */
+        for (r = 0; r <= n_reads; ++r) regs_off[r] = out.regs_off[r];
+        orc_align_out_free(&out);
+        return BSB_ECAPACITY;
+    }
     if (rc == 0) {
         for (r = 0; r <= n_reads; ++r) regs_off[r] = out.regs_off[r];
         for (r = 0; r < out.regs_off[n_reads]; ++r) {
@@ -145,6 +149,7 @@ static void print_stats(void)
     mem_gen_cigar_stats(&kept, &served);
     fprintf(stderr, "[bsb_glue] cigar records kept %lld served %lld\n", (long long)kept, (long long)served);
     fprintf(stderr, "[bsb_glue] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
+    fprintf(stderr, "[bsb_glue] region buffer regrown %lld\n", (long long)mem_align_regrown());
 }
 
 /* worker_t of bwamem.c:1274-1285 */

@@ -11,11 +11,9 @@ CPU only; skipped where the reference build is absent.
 """
 import os
 import subprocess
+import sys
 
-import numpy as np
 import pytest
-
-from bsbolt_gb300 import synth
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.path.join(ROOT, "oracle", "_ref")
@@ -25,45 +23,27 @@ pytestmark = pytest.mark.skipif(not (os.path.exists(BWA) and os.path.exists(GLUE
                                 reason="reference bwa / bwa_glue not built here (oracle/Makefile.ref)")
 
 
-def write_fastq(path, reads, tag):
-    letters = np.frombuffer(b"ACGTN", np.uint8)
-    with open(path, "w") as f:
-        for i, r in enumerate(reads):
-            s = letters[r].tobytes().decode()
-            f.write(f"@r{i}/{tag}\n{s}\n+\n{'?' * len(s)}\n")
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import sam_sets  # noqa: E402
 
 
 @pytest.fixture(scope="module")
-def data(tmp_path_factory):
-    d = tmp_path_factory.mktemp("glue")
-    contigs = synth.bs_genome(3, 200_000, seed=4242)
-    contigs[1][1][50_000:55_000] = contigs[0][1][10_000:15_000]      # a duplicated block
-    fa = str(d / "ref.fa")
-    synth.write_fasta(fa, contigs)
-    subprocess.check_call([BWA, "index", "-a", "bwtsw", fa], stderr=subprocess.DEVNULL)
-    r1, r2 = synth.bs_reads_pe(contigs, 3000, 100, 300, 30, seed=4243)
-    # pairs with one end mutated at every 10th base (by +1, which neither conversion
-    # undoes): no exact 19-mer, so that end has no seed and only mate rescue places it
-    m1, m2 = synth.bs_reads_pe(contigs, 60, 100, 300, 30, seed=4245)
-    for k, (a, b) in enumerate(zip(m1, m2)):
-        x = b if k % 2 == 0 else a
-        x[5::10] = (x[5::10] + 1) % 4
-    r1 += m1
-    r2 += m2
-    # a few adapter-like / random / short reads
-    rng = np.random.Generator(np.random.PCG64(4244))
-    for _ in range(20):
-        r1.append(rng.integers(0, 4, 100).astype(np.uint8))
-        r2.append(rng.integers(0, 4, 100).astype(np.uint8))
-    write_fastq(str(d / "r1.fq"), r1, 1)
-    write_fastq(str(d / "r2.fq"), r2, 2)
-    return fa, str(d / "r1.fq"), str(d / "r2.fq")
+def pe(tmp_path_factory):
+    return sam_sets.pe_set(str(tmp_path_factory.mktemp("glue")), BWA)
+
+
+@pytest.fixture(scope="module")
+def data(pe):
+    return pe[:3]
+
+
+@pytest.fixture(scope="module")
+def undirectional(pe):
+    return pe[0], pe[3], pe[4]
 
 
 def run_mem(binary, fa, r1, r2, extra, env=None):
-    cmd = [binary, "mem", "-Y", "-t", "4", "-K", "10000000"] + extra + [fa, r1, r2]
-    out = subprocess.run(cmd, capture_output=True, check=True, env=env).stdout.decode()
-    return [line for line in out.splitlines() if not line.startswith("@PG")]
+    return sam_sets.run_mem(binary, fa, [r1, r2], extra, env)
 
 
 @pytest.mark.parametrize("bonus", ["5,5", "30,30"])
@@ -146,3 +126,33 @@ def test_glue_other_scorings(data, scoring):
     extra = scoring + ["-L", "5,5"]
     ref = run_mem(BWA, fa, r1, r2, extra)
     assert len(ref) > 6000 and run_mem(GLUE, fa, r1, r2, extra) == ref
+
+
+def test_glue_bsbolt_default_argv(data):
+    """bsbolt Align's own default `bwa mem` command line (-L 30,30, -T 10, the XA and
+    bisulfite options)."""
+    fa, r1, r2 = data
+    ref = run_mem(BWA, fa, r1, r2, sam_sets.BSBOLT_ARGS)
+    assert len(ref) > 6000 and run_mem(GLUE, fa, r1, r2, sam_sets.BSBOLT_ARGS) == ref
+
+
+def test_glue_undirectional(undirectional):
+    """`-z` (bsbolt Align -UN): ambiguous pairs are aligned under both conversions
+    (bwa.c:95-133), and the glue sees the duplicated reads as any others."""
+    fa, u1, u2 = undirectional
+    extra = ["-z", "-L", "5,5"]
+    ref = run_mem(BWA, fa, u1, u2, extra)
+    assert len(ref) > 6000 and run_mem(GLUE, fa, u1, u2, extra) == ref
+
+
+def test_glue_repeat_family_over_max_occ(tmp_path):
+    """Reads inside a family of 700 exact copies: each has ~500 regions (max_occ rows
+    sampled per seed), more than the glue's first region buffer holds; the library
+    answers BSB_ECAPACITY with the size it needs, the batch runs again, and the SAM is the
+    reference's."""
+    fa, r1, r2 = sam_sets.repeat_set(str(tmp_path), BWA)
+    extra = ["-L", "5,5"]
+    ref = run_mem(BWA, fa, r1, r2, extra)
+    assert len(ref) >= 80 and run_mem(GLUE, fa, r1, r2, extra) == ref
+    st = sam_sets.run_stats(GLUE, fa, [r1, r2], extra, "BSB_SHIM_STATS", "[bsb_glue]")
+    assert st["regrown"] >= 1, st
