@@ -154,6 +154,30 @@ def cpu_port_gcups(jobs, seq, n_sample, threads, mat):
     return float(cells.sum()) / dt / 1e9, dt, out, cells
 
 
+_SAMPLE_CELLS = {}
+
+
+def cpu_reference_gcups(jobs, seq, n_sample, threads, mat):
+    """The reference's own compiled ksw_extend2 (oracle/_ref/libref_ksw.so) on the first
+    n_sample jobs over `threads` host threads, when the reference sources were staged and
+    built; else the C port (oracle/bsb_oracle.c).  The sample's cell count comes from the
+    port (once, untimed): the reference does not report it.  Returns (GCUPS, seconds, tuples,
+    cells, kind)."""
+    import oracle
+    if not oracle.have_reference_ksw():
+        g, dt, out, cells = cpu_port_gcups(jobs, seq, n_sample, threads, mat)
+        return g, dt, out, cells, "port"
+    sub = jobs[:n_sample]
+    key = (id(jobs), n_sample)
+    if key not in _SAMPLE_CELLS:
+        _SAMPLE_CELLS[key] = oracle.ksw_batch(sub, seq, mat, 6, 1, 6, 1, 100, n_threads=threads)[1]
+    cells = _SAMPLE_CELLS[key]
+    t0 = time.perf_counter()
+    out = oracle.ref_ksw_batch(sub, seq, mat, 6, 1, 6, 1, 100, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return float(cells.sum()) / dt / 1e9, dt, out, cells, "reference"
+
+
 def ref2mb_workload(n_pairs=20000):
     """The 2 Mb-reference workload: 4 x 500 kb reference (GC 41 %, CpG 1 %), directional PE 2x100,
     insert N(300,30), CpG meth 0.8, CH 0.01, 99.5 % conversion, 0.5 % errors; the reads
@@ -300,6 +324,14 @@ def cigar_block(ctx, steps):
     }
 
 
+def ref100mb_contigs():
+    """The 100 Mb reference: 4 x 25 Mb (GC 41 %, CpG 1 %) with 15 % interspersed repeats of
+    300 bp - 6 kb families at 2-15 % divergence."""
+    from bsbolt_gb300 import synth
+    contigs = synth.bs_genome(4, 25_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 2)
+    return synth.add_repeats(contigs, 0.15, seed=20261203 + 2)
+
+
 def ref100mb_workload(n_pairs=100_000):
     """The 100 Mb-reference workload: 4 x 25 Mb reference (GC 41 %, CpG 1 %, 15 % interspersed
     repeats of 300 bp - 6 kb families at 2-15 % divergence), directional PE 2x150, insert
@@ -308,19 +340,17 @@ def ref100mb_workload(n_pairs=100_000):
     d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", f"ref100mb_{n_pairs}")
     os.makedirs(d, exist_ok=True)
     prefix = os.path.join(d, "ref")
-    if not os.path.exists(prefix + ".sa"):
-        contigs = synth.bs_genome(4, 25_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 2)
-        synth.add_repeats(contigs, 0.15, seed=20261203 + 2)
-        synth.write_fasta(prefix + ".fa", contigs)
-        index.build_index(prefix + ".fa", prefix)
-        r1, r2 = synth.bs_reads_pe(contigs, n_pairs, 150, 400, 50, seed=20261203 + 2)
-        reads = []
-        for a, b in zip(r1, r2):
-            reads.append(synth.bs_convert(a, g2a=False))
-            reads.append(synth.bs_convert(b, g2a=True))
-        offs = np.zeros(len(reads) + 1, np.int64)
-        offs[1:] = np.cumsum([len(r) for r in reads])
-        np.save(os.path.join(d, "reads.npy"), np.concatenate(reads))
+    if not os.path.exists(os.path.join(d, "offs.npy")):
+        contigs = ref100mb_contigs()
+        if not os.path.exists(prefix + ".sa"):
+            synth.write_fasta(prefix + ".fa", contigs)
+            index.build_index(prefix + ".fa", prefix)
+        r1, r2 = synth.bs_reads_pe_block(contigs, n_pairs, 150, 400, 50, seed=20261203 + 2)
+        r1 = synth.bs_convert(r1, g2a=False)          # the aligner's in-silico conversion
+        r2 = synth.bs_convert(r2, g2a=True)
+        reads = np.stack([r1, r2], axis=1).reshape(-1)
+        offs = np.arange(2 * n_pairs + 1, dtype=np.int64) * 150
+        np.save(os.path.join(d, "reads.npy"), reads)
         np.save(os.path.join(d, "offs.npy"), offs)
     return prefix, np.load(os.path.join(d, "reads.npy")), np.load(os.path.join(d, "offs.npy"))
 
@@ -334,9 +364,7 @@ def rrbs_workload(n_reads=3_000_000):
     d = os.path.dirname(prefix)
     fr, fo = os.path.join(d, f"rrbs_{n_reads}.npy"), os.path.join(d, f"rrbs_{n_reads}_offs.npy")
     if not os.path.exists(fo):
-        contigs = synth.bs_genome(4, 25_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 2)
-        synth.add_repeats(contigs, 0.15, seed=20261203 + 2)
-        seqs, offs = synth.rrbs_reads_se(contigs, n_reads, seed=20261203 + 3)
+        seqs, offs = synth.rrbs_reads_se(ref100mb_contigs(), n_reads, seed=20261203 + 3)
         conv = seqs.copy()
         conv[conv == 1] = 3                     # the aligner's C->T conversion of read 1 (bs_helpers.cpp:18-31)
         np.save(fr, conv)
@@ -402,6 +430,65 @@ def pipeline_rrbs(ctx, batch_bases=10_000_000, cpu_reads=4_000):
     }
 
 
+def measured_hbm_gbs():
+    """HBM copy bandwidth of this GPU pool (MEASURED_PEAKS.json, written per machine), else the
+    fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def seeding_roofline(ctx, reads, offs, reps=5):
+    """Device time of one seeding batch (seed_kernel's two launches, the offset scan and the
+    compaction: bsb_seed_batch_device) with CUDA events on the context stream, and the
+    occurrence-query bytes it reads as algorithmic traffic: per bwt_extend one bwt_2occ4 =
+    two queries, 32 B each in the device's sector layout (64 B each in the reference's
+    128-symbol blocks)."""
+    import ctypes
+    import torch
+    from bsbolt_gb300 import _lib, seed
+    n = len(offs) - 1
+    total = int(offs[-1] - offs[0])
+    d_reads = torch.from_numpy(np.ascontiguousarray(reads[offs[0]:offs[-1]])).cuda()
+    d_offs = torch.from_numpy(np.ascontiguousarray(offs - offs[0])).cuda()
+    d_out = torch.empty((2 * total + 32 * n) * 4, dtype=torch.int64, device="cuda")
+    d_off = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    opt = _lib.SeedOpt(19, 1.5, 10, 20)
+    max_len = int(np.diff(offs).max())
+
+    def launch():
+        _lib.check(ctx.handle, ctx.L.bsb_seed_batch_device(ctx.handle, ctypes.byref(opt), n,
+                                                           ctypes.c_void_p(d_reads.data_ptr()),
+                                                           ctypes.c_void_p(d_offs.data_ptr()), total, max_len,
+                                                           ctypes.c_void_p(d_out.data_ptr()),
+                                                           ctypes.c_void_p(d_off.data_ptr())))
+    s = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(2):
+        launch()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(reps):
+        launch()
+    b.record(s)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    n_ext = seed.last_extensions(ctx)
+    seeds = int(d_off[-1].item())
+    peak, src = measured_hbm_gbs()
+    bytes32 = n_ext * 2 * 32
+    gbs = bytes32 / (ms * 1e-3) / 1e9
+    return {"reads": n, "seeds": seeds, "bwt_extend_calls": n_ext, "occ_queries": 2 * n_ext,
+            "ms_per_batch": round(ms, 4), "seeds_per_s": round(seeds / (ms * 1e-3), 1),
+            "reads_per_s": round(n / (ms * 1e-3), 1),
+            "algorithmic_bytes_sector_layout": bytes32, "algorithmic_bytes_reference_layout": 2 * bytes32,
+            "achieved_gbs": round(gbs, 2), "peak_gbs": peak, "frac": round(gbs / peak, 4),
+            "frac_reference_layout_bytes": round(2 * gbs / peak, 4),
+            "peak_source": f"HBM copy bandwidth, {src} (MEASURED_PEAKS.json hbm_gbs)"}
+
+
 def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
     """Seeds -> regions on the 100 Mb reference (200 MB BWT, larger than L2) in -K 10M-base
     batches, against the CPU oracle on a sample."""
@@ -430,6 +517,8 @@ def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
     for lo, hi in batches:
         seed.seed_batch(ctx, *sub(lo, hi))
     seed_s = time.perf_counter() - t0
+    lo, hi = batches[0]
+    seeding = seeding_roofline(ctx, reads, offs[lo:hi + 1])
     bi = index.BwaIndex(prefix)
     ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
     anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
@@ -455,7 +544,118 @@ def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
         "cpu_oracle_threads": threads, "cpu_sample_pairs": cpu_pairs,
         "regions_bit_exact_vs_oracle_on_sample": exact,
         "workload_prep_s": round(prep_s, 1),
+        "seeding_roofline_one_batch": seeding,
     }
+
+
+def sam_sha(path):
+    """SHA-256 of a SAM file without its @PG line (which carries argv[0]), and its line count."""
+    import hashlib
+    h, n = hashlib.sha256(), 0
+    with open(path, "rb") as f:
+        for line in f:
+            if not line.startswith(b"@PG"):
+                h.update(line)
+                n += 1
+    return h.hexdigest(), n
+
+
+def time_bwa_mem(binary, db, fastqs, threads, out_sam, env=None):
+    """Wall time of `binary mem` with bsbolt Align's default argv (bsbolt_gb300.align) at
+    -t threads and -K 10000000, SAM to out_sam; returns (seconds, BSStat counts)."""
+    from bsbolt_gb300 import align
+    cmd = align.bwa_command(binary, db, fastqs[0], fastqs[1] if len(fastqs) > 1 else None, t=threads)
+    t0 = time.perf_counter()
+    lines = []
+    with open(out_sam, "wb") as f:
+        stats = align.run_alignment(cmd, f, ["-K", "10000000"], env=env, echo=False, keep=lines)
+    return time.perf_counter() - t0, stats, [x for x in lines if x.startswith("[bsb_gpu]")]
+
+
+def bsbolt_db(prefix):
+    """A bsbolt database directory (<db>/BSB_ref.fa.*, the layout `bsbolt Align -DB` reads)
+    whose files link to the index at prefix."""
+    db = prefix + "_bsbdb"
+    os.makedirs(db, exist_ok=True)
+    for ext in ("bwt", "sa", "pac", "opac", "ann", "amb"):
+        link = os.path.join(db, "BSB_ref.fa." + ext)
+        if not os.path.lexists(link):
+            os.symlink(os.path.abspath(prefix + "." + ext), link)
+    return db
+
+
+def sam_workloads(n_pairs_100mb, n_rrbs):
+    """FASTQ files of the SAM-level runs: the 2 Mb workload's 20k 2x100 pairs (as sequenced),
+    n_pairs_100mb 2x150 pairs on the 100 Mb reference (insert N(400,50)) and n_rrbs RRBS-like
+    single-end reads on it.  Cached on disk beside the indexes (whose files the bwa binaries read:
+    they are byte-identical to the reference `bwa index`'s)."""
+    from bsbolt_gb300 import synth
+    out = {}
+    prefix2, _, offs2 = ref2mb_workload()
+    d2 = os.path.dirname(prefix2)
+    if not os.path.exists(os.path.join(d2, "r2.fq")):
+        o = ref2mb_original_reads().reshape(-1, 100)
+        synth.write_fastq_block(os.path.join(d2, "r1.fq"), o[0::2], 1)
+        synth.write_fastq_block(os.path.join(d2, "r2.fq"), o[1::2], 2)
+    out["pe_2mb"] = (bsbolt_db(prefix2), [os.path.join(d2, "r1.fq"), os.path.join(d2, "r2.fq")], (len(offs2) - 1) // 2)
+    if n_pairs_100mb or n_rrbs:
+        prefix, _, _ = ref100mb_workload()
+        d = os.path.dirname(prefix)
+        contigs = None
+        if n_pairs_100mb:
+            f1, f2 = (os.path.join(d, f"pe150_{n_pairs_100mb}_{k}.fq") for k in (1, 2))
+            if not os.path.exists(f2):
+                contigs = contigs or ref100mb_contigs()
+                r1, r2 = synth.bs_reads_pe_block(contigs, n_pairs_100mb, 150, 400, 50, seed=20261203 + 2 + 100)
+                synth.write_fastq_block(f1, r1, 1)
+                synth.write_fastq_block(f2 + ".tmp", r2, 2)
+                os.replace(f2 + ".tmp", f2)
+            out["pe_100mb"] = (bsbolt_db(prefix), [f1, f2], n_pairs_100mb)
+        if n_rrbs:
+            f1 = os.path.join(d, f"rrbs_{n_rrbs}.fq")
+            if not os.path.exists(f1):
+                contigs = contigs or ref100mb_contigs()
+                seqs, offs = synth.rrbs_reads_se(contigs, n_rrbs, seed=20261203 + 3)
+                synth.write_fastq_ragged(f1 + ".tmp", seqs, offs, 1)
+                os.replace(f1 + ".tmp", f1)
+            out["rrbs_100mb"] = (bsbolt_db(prefix), [f1], n_rrbs)
+    return out
+
+
+def sam_block(n_pairs_100mb=500_000, n_rrbs=1_000_000, threads=None):
+    """Aligned read pairs/s from SAM: the stock `bwa mem` (the reference BWA fork built from its
+    own sources, oracle/Makefile.ref) against `bwa_gpu mem` (the same sources linked to
+    libbsbgpu.so), both with bsbolt Align's default argv, -t = all host cores, -K 10000000, on
+    the same FASTQ; the two SAM files must be identical but for @PG."""
+    stock = os.path.join(ROOT, "oracle", "_ref", "bwa")
+    gpu = os.path.join(ROOT, "bsbolt_gb300", "integration", "_build", "bwa_gpu")
+    if not (os.path.exists(stock) and os.path.exists(gpu)):
+        return {"error": "bwa / bwa_gpu not built (the reference sources were not staged)"}
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    wl = sam_workloads(n_pairs_100mb, n_rrbs)
+    prep_s = time.perf_counter() - t0
+    tmp = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "sam")
+    os.makedirs(tmp, exist_ok=True)
+    res = {"argv": "bsbolt Align defaults (-Y -A1 -B4 -O6,6 -E1,1 -L30,30 -T10 -U17 -w100 -d100 -k19 -c500 "
+                   "-h100,200 -e0.1 -l0.5 -n5 -Z0.95 ...) -t %d -K 10000000" % threads,
+           "threads": threads, "workload_prep_s": round(prep_s, 1)}
+    env = dict(os.environ, BSB_GPU_STATS="1")
+    for name, (db, fqs, n_units) in wl.items():
+        sam_r, sam_g = os.path.join(tmp, name + ".ref.sam"), os.path.join(tmp, name + ".gpu.sam")
+        tr, st_r, _ = time_bwa_mem(stock, db, fqs, threads, sam_r)
+        tg, st_g, glog = time_bwa_mem(gpu, db, fqs, threads, sam_g, env)
+        hr, nr = sam_sha(sam_r)
+        hg, ng = sam_sha(sam_g)
+        unit = "read pairs" if len(fqs) == 2 else "reads"
+        res[name] = {unit: n_units, "sam_lines": nr,
+                     f"stock_bwa_{unit.replace(' ', '_')}_per_s": round(n_units / tr, 1), "stock_bwa_s": round(tr, 3),
+                     f"bwa_gpu_{unit.replace(' ', '_')}_per_s": round(n_units / tg, 1), "bwa_gpu_s": round(tg, 3),
+                     "speedup": round(tr / tg, 3), "sam_identical": bool(hr == hg and nr == ng),
+                     "bsstat_identical": st_r == st_g, "bsstat": st_g, "bwa_gpu_log": glog}
+        for f in (sam_r, sam_g):
+            os.unlink(f)
+    return res
 
 
 def pipeline_secondary(ctx, steps, rank):
@@ -649,10 +849,10 @@ def run_reference(args, ws, rank):
     mat = synth.fill_scmat(1, 4)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_port_gcups(jobs, seq, args.ref_sample, threads, mat)
+        cpu_reference_gcups(jobs, seq, args.ref_sample, threads, mat)
     vals, tms = [], []
     for _ in range(args.steps):
-        g, dt, _, _ = cpu_port_gcups(jobs, seq, args.ref_sample, threads, mat)
+        g, dt, _, _, kind = cpu_reference_gcups(jobs, seq, args.ref_sample, threads, mat)
         vals.append(g)
         tms.append(dt)
     v = float(np.mean(vals))
@@ -663,9 +863,12 @@ def run_reference(args, ws, rank):
         "data": "synthetic (seeded PCG64): the 4M-job extension workload's shapes",
         "config": {"workload": "batched ksw_extend2, 4M jobs, qlen U[10,140], w=100, BWA default scoring",
                    "sample_jobs_per_step": args.ref_sample, "parallelism": "host threads"},
-        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"first {args.ref_sample} of the 4M jobs per step, ksw.c:380-479 CPU port "
-                                   "(oracle/bsb_oracle.c), pthreads over all host cores"},
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"first {args.ref_sample} of the 4M jobs per step, " +
+                                   ("the reference's own ksw_extend2 (ksw.c:380-479 compiled from BSBolt's "
+                                    "sources, oracle/_ref/libref_ksw.so)" if kind == "reference" else
+                                    "ksw.c:380-479 CPU port (oracle/bsb_oracle.c)") +
+                                   ", pthreads over all host cores"},
         "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -803,12 +1006,13 @@ def run_ours(args, ws, rank, local):
     parity = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        g, dt, ref_out, ref_cells = cpu_port_gcups(jobs, seq, args.cpu_sample, threads, mat)
+        g, dt, ref_out, ref_cells, kind = cpu_reference_gcups(jobs, seq, args.cpu_sample, threads, mat)
         parity = bool(np.array_equal(ref_out, out_host[: args.cpu_sample]))
         cells_match = int(ref_cells.sum()) == int(d_cells[: args.cpu_sample].sum().item())
-        cpu = {"value": round(g, 4), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {args.cpu_sample} jobs ({int(ref_cells.sum())} cells, {dt:.2f} s wall), "
-                         "CPU port of ksw.c:380-479, pthreads over all host cores",
+        cpu = {"value": round(g, 4), "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"first {args.cpu_sample} jobs ({int(ref_cells.sum())} cells, {dt:.2f} s wall), " +
+                         ("the reference's own ksw_extend2 compiled from BSBolt's sources" if kind == "reference"
+                          else "CPU port of ksw.c:380-479") + ", pthreads over all host cores",
                "tuples_bit_exact_on_sample": parity, "cells_match_on_sample": bool(cells_match)}
 
     learned = None
@@ -820,7 +1024,7 @@ def run_ours(args, ws, rank, local):
             learned = {"error": f"{type(e).__name__}: {e}"}
 
     big = rrbs = None
-    if rank == 0 and args.ref100mb:
+    if rank == 0 and not args.no_ref100mb:
         try:
             big = pipeline_ref100mb(ctx)
         except Exception as e:   # reported, never hidden
@@ -858,6 +1062,13 @@ def run_ours(args, ws, rank, local):
             msw = matesw_block(ctx, args.steps)
         except Exception as e:   # reported, never hidden
             msw = {"error": f"{type(e).__name__}: {e}"}
+
+    sam = None
+    if rank == 0 and not args.no_sam:
+        try:
+            sam = sam_block(0 if args.no_ref100mb else args.sam_pairs, 0 if args.no_ref100mb else args.sam_rrbs)
+        except Exception as e:   # reported, never hidden
+            sam = {"error": f"{type(e).__name__}: {e}"}
 
     if rank == 0:
         line = {
@@ -900,6 +1111,7 @@ def run_ours(args, ws, rank, local):
             "pipeline_rrbs_100mb_ref": rrbs,
             "gen_cigar": cig,
             "mate_rescue_sw": msw,
+            "sam_pipeline": sam,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -921,9 +1133,14 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="skip the tile-shape autotuner block")
     ap.add_argument("--no-cigar", action="store_true", help="skip the bwa_gen_cigar2 block")
     ap.add_argument("--no-matesw", action="store_true", help="skip the mate-rescue Smith-Waterman block")
-    ap.add_argument("--ref100mb", action="store_true",
-                    help="add the 100 Mb-reference blocks, WGBS-like PE and RRBS-like SE (builds a 100 Mb index: "
-                         "~2 min the first time)")
+    ap.add_argument("--no-ref100mb", action="store_true",
+                    help="skip the 100 Mb-reference blocks, WGBS-like PE and RRBS-like SE (they build a 100 Mb "
+                         "index: ~1 min the first time)")
+    ap.add_argument("--no-sam", action="store_true", help="skip the stock bwa vs bwa_gpu SAM block")
+    ap.add_argument("--sam-pairs", type=int, default=500_000,
+                    help="2x150 pairs of the SAM block on the 100 Mb reference (the full workload is 4M)")
+    ap.add_argument("--sam-rrbs", type=int, default=1_000_000,
+                    help="RRBS-like reads of the SAM block (the full workload is 3M)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

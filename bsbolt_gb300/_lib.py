@@ -170,6 +170,8 @@ def load(path: str = LIB_PATH):
     L.bsb_gen_cigar_batch.argtypes = [P, P, I64, I32, P, P, I64, P, I64, P, P, I64, ctypes.POINTER(I64)]
     L.bsb_gen_cigar_batch.restype = I32
     L.bsb_align2_batch.argtypes = [P, P, P, I64, P, I64, P]
+    L.bsb_last_seed_extensions.argtypes = [P, ctypes.POINTER(I64)]
+    L.bsb_last_seed_extensions.restype = I32
     L.bsb_align2_batch.restype = I32
     _lib = L
     return L

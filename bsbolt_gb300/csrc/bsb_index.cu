@@ -312,6 +312,21 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     return bsb_cuda(ctx, e, "seed launch");
 }
 
+extern "C" int bsb_last_seed_extensions(bsb_ctx *ctx, int64_t *n_ext)
+{
+    if (!ctx || !n_ext) return BSB_EINVAL;
+    *n_ext = 0;
+    if (!ctx->seed_ctrl) return 0;
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    uint64_t v = 0;
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&v, ctx->seed_ctrl + 4, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H ext")))
+        return rc;
+    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seed stats"))) return rc;
+    *n_ext = (int64_t)v;
+    return 0;
+}
+
 extern "C" int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *seqs,
                               const int64_t *offs, bsb_intv_t *out, int64_t max_out, int64_t *out_off)
 {

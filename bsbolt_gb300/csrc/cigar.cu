@@ -426,6 +426,8 @@ extern "C" int bsb_gen_cigar_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int64
         return bsb_fail(ctx, BSB_EINVAL, "unsupported gap penalties");
     if (blob_used) *blob_used = 0;
     if (n == 0) return 0;
+    int rc0;
+    if ((rc0 = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc0;
     const int64_t lp = ctx->l_pac;
     for (int32_t i = 0; i < n; ++i) {
         const bsb_cigar_job_t &j = jobs[i];

@@ -79,8 +79,9 @@ enum SeedState : int {
 };
 
 // Launch control words: [0] next item of the first launch, [1] overflow (read + 1),
-// [2] pass-2 items queued, [3] next item of the second launch.
-enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrlWords = 4 };
+// [2] pass-2 items queued, [3] next item of the second launch, [4..5] the bwt_extend
+// calls of both launches (uint64; each is one bwt_2occ4, two occurrence queries).
+enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrlExt = 4, kCtrlWords = 8 };
 
 // Persistent: each thread takes work items from a counter.
 //   mode 0: item r < n_reads runs pass 1 of read r and queues its pass-2 re-seeds;
@@ -127,6 +128,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
     ik.x0 = ik.x1 = ik.x2 = ik.info = 0;
     p = ik;
     pn = ik;
+    unsigned n_ext = 0;
 
     for (;;) {
         // ---- bookkeeping up to the next extension (or the end of the work)
@@ -317,6 +319,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
             if (st == kExit) break;
             continue;
         }
+        n_ext += need;
 
         // ---- the extension, converged across the warp
         DevIntv ok;
@@ -368,6 +371,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
             break;
         }
     }
+    if (n_ext) atomicAdd((unsigned long long *)(ctrl + kCtrlExt), (unsigned long long)n_ext);
 }
 
 // Seeds of read r in the two parts of its padded region (a part that overflowed holds

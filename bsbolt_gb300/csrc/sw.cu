@@ -313,6 +313,10 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
     if (S.qmax < 1) return bsb_fail(ctx, BSB_EINVAL, "the scoring matrix needs a positive entry");
     if (n == 0) return 0;
     if (n > 0x7fffffff) return bsb_fail(ctx, BSB_EINVAL, "at most 2^31 - 1 jobs per call");
+    {
+        int rc0;
+        if ((rc0 = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc0;
+    }
     // Four job lists: packed byte lanes (1..16 segments), packed word lanes (1..40 segments, when
     // 16-bit arithmetic without saturation is exact: qlen * max score <= 32640 and penalties
     // below 32768), then the one-lane byte and word jobs.  The packed lists are in counting-sort

@@ -4,8 +4,13 @@
  * strings and its mate-rescue Smith-Waterman on the GPU without a source edit.
  *
  * Link the BWA objects with this file, bwamem_gpu.c and libbsbgpu.so, and
- *   -Wl,--wrap=kt_for -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2
+ *   -Wl,--wrap=kt_for -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2 -Wl,--wrap=bwa_idx_load
  * (bsbolt_gb300/integration/Makefile does this and names the result bwa_gpu).
+ *
+ * bwa_idx_load (bwa.c:440, called by main_mem, fastmap.c:321) is wrapped so that the CUDA
+ * context starts on a second thread while the index is read from disk, and the index goes
+ * to the GPU as soon as it is in memory; the thread is joined before the wrapper returns,
+ * so no CUDA work is in flight when BWA goes on (or exits on an error of its own).
  *
  * kt_for is called only by mem_process_seqs (bwamem.c:1336 and :1344), twice
  * per -K batch: worker1 (mem_align1_core per read) and then, after
@@ -20,12 +25,14 @@
  * BSB_GPU_STATS=1 prints, at exit, how many CIGAR and rescue calls the GPU
  * results answered, and the time spent in the GPU passes.
  */
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/time.h>
 
 #include "bntseq.h"
+#include "bwa.h"
 #include "bwt.h"
 #include "utils.h"
 #include "bwamem_gpu.h"
@@ -81,19 +88,20 @@ static void hook_fail(bsb_ctx *ctx, int rc, const char *what)
     err_fatal("bwa_gpu", "%s: %s (%s)", what, ctx ? bsb_last_error(ctx) : "no context", bsb_strerror(rc));
 }
 
-/* One context per process, with the index bwa_idx_load holds (bwa.c:363-524): the
- * occurrence array, the sampled SA, the converted pac, the contig table and the
- * original-sequence opac the methylation strings read. */
-static void hook_init(const hook_worker_t *w)
+static int hook_device(void)
 {
-    const bwt_t *bwt = w->bwt;
-    const bntseq_t *bns = w->bns;
+    const char *dev = getenv("BSB_GPU_DEVICE");
+    return dev ? atoi(dev) : 0;
+}
+
+/* The index bwa_idx_load holds (bwa.c:363-524): the occurrence array, the sampled SA, the
+ * converted pac, the contig table and the original-sequence opac the methylation strings read. */
+static void hook_upload(const bwt_t *bwt, const bntseq_t *bns, const uint8_t *pac, const uint8_t *opac)
+{
     bsb_index_view_t v;
     int64_t *ann_off;
     int32_t *ann_len;
-    const char *dev = getenv("BSB_GPU_DEVICE");
     int i, rc;
-    if ((rc = bsb_ctx_create(dev ? atoi(dev) : 0, &g_hook_ctx))) hook_fail(g_hook_ctx, rc, "GPU context");
     ann_off = (int64_t *)malloc(sizeof(int64_t) * (bns->n_seqs + 1));
     ann_len = (int32_t *)malloc(sizeof(int32_t) * (bns->n_seqs + 1));
     for (i = 0; i < bns->n_seqs; ++i) ann_off[i] = bns->anns[i].offset, ann_len[i] = bns->anns[i].len;
@@ -102,14 +110,48 @@ static void hook_init(const hook_worker_t *w)
     for (i = 0; i < 5; ++i) v.L2[i] = bwt->L2[i];
     v.bwt = bwt->bwt, v.bwt_size = bwt->bwt_size;
     v.sa = bwt->sa, v.n_sa = bwt->n_sa, v.sa_intv = bwt->sa_intv;
-    v.pac = w->pac, v.l_pac = bns->l_pac;
+    v.pac = pac, v.l_pac = bns->l_pac;
     v.n_seqs = bns->n_seqs, v.ann_offset = ann_off, v.ann_len = ann_len;
     if ((rc = bsb_index_upload(g_hook_ctx, &v))) hook_fail(g_hook_ctx, rc, "index upload");
-    if (w->opac && (rc = bsb_index_upload_opac(g_hook_ctx, w->opac, bns->l_pac)))
-        hook_fail(g_hook_ctx, rc, "opac upload");
+    if (opac && (rc = bsb_index_upload_opac(g_hook_ctx, opac, bns->l_pac))) hook_fail(g_hook_ctx, rc, "opac upload");
     free(ann_off);
     free(ann_len);
     if (getenv("BSB_GPU_STATS")) atexit(hook_report);
+}
+
+static int g_boot_rc;
+
+static void *hook_boot(void *arg)
+{
+    (void)arg;
+    g_boot_rc = bsb_ctx_create(hook_device(), &g_hook_ctx);
+    return 0;
+}
+
+bwaidx_t *__real_bwa_idx_load(const char *hint, int which);
+
+bwaidx_t *__wrap_bwa_idx_load(const char *hint, int which)
+{
+    pthread_t boot;
+    bwaidx_t *idx;
+    const int full = (which & BWA_IDX_ALL) == BWA_IDX_ALL;   /* bwa mem's load (fastmap.c:321) */
+    int started = full && !g_hook_ctx && pthread_create(&boot, 0, hook_boot, 0) == 0;
+    idx = __real_bwa_idx_load(hint, which);
+    if (started) {
+        pthread_join(boot, 0);
+        if (g_boot_rc) hook_fail(g_hook_ctx, g_boot_rc, "GPU context");
+        if (idx) hook_upload(idx->bwt, idx->bns, idx->pac, idx->opac);
+    }
+    return idx;
+}
+
+/* Without the wrapped load (an index from shared memory, bwashm.c), the context and the
+ * index upload happen on the first batch, from the arrays the worker sees. */
+static void hook_init(const hook_worker_t *w)
+{
+    int rc;
+    if ((rc = bsb_ctx_create(hook_device(), &g_hook_ctx))) hook_fail(g_hook_ctx, rc, "GPU context");
+    hook_upload(w->bwt, w->bns, w->pac, w->opac);
 }
 
 void __real_kt_for(int n_threads, void (*func)(void *, long, int), void *data, long n);

@@ -42,6 +42,13 @@ def seed_batch(ctx: Context, seqs: np.ndarray, offs: np.ndarray, min_seed_len: i
     return out[: out_off[-1]].copy(), out_off
 
 
+def last_extensions(ctx: Context) -> int:
+    """bwt_extend calls (one bwt_2occ4 each) of the context's most recent seeding batch."""
+    v = ctypes.c_int64()
+    _lib.check(ctx.handle, ctx.L.bsb_last_seed_extensions(ctx.handle, ctypes.byref(v)))
+    return int(v.value)
+
+
 def sa_batch(ctx: Context, rows: np.ndarray) -> np.ndarray:
     rows = np.ascontiguousarray(rows, dtype=np.uint64)
     pos = np.zeros(len(rows), np.uint64)
@@ -75,5 +82,11 @@ def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.Alig
     fn = ctx.L.bsb_mem_align1_batch if dedup else ctx.L.bsb_align_regs_batch
     rc = fn(ctx.handle, ctypes.byref(opt), n, _ptr(seqs) if len(seqs) else None, _ptr(offs), _ptr(regs), cap,
             _ptr(regs_off))
+    if rc == _lib.BSB_ECAPACITY and regs_off[-1] > cap:    # more regions than the first guess: size and rerun
+        cap = int(regs_off[-1])
+        regs = np.empty(cap, REG_DTYPE)
+        ctx._regs_buf = regs
+        rc = fn(ctx.handle, ctypes.byref(opt), n, _ptr(seqs) if len(seqs) else None, _ptr(offs), _ptr(regs), cap,
+                _ptr(regs_off))
     _lib.check(ctx.handle, rc)
     return regs[: regs_off[-1]].copy(), regs_off

@@ -253,6 +253,94 @@ def bs_reads_pe(contigs, n_pairs: int, read_len: int = 100, insert_mean: float =
     return r1s, r2s
 
 
+def bs_reads_pe_block(contigs, n_pairs: int, read_len: int = 150, insert_mean: float = 400,
+                      insert_sd: float = 50, meth_cpg: float = 0.8, meth_ch: float = 0.01,
+                      conversion: float = 0.995, err: float = 0.005, seed: int = 20261203,
+                      chunk: int = 250_000):
+    """bs_reads_pe's model, vectorised for millions of pairs: directional pairs of read_len
+    bases from either strand, insert ~ N(insert_mean, insert_sd) (at least read_len),
+    methylation and conversion on the sequenced strand, substitution errors.  Where the two
+    reads of a short insert overlap, each draws its own methylation there.  Returns (r1, r2)
+    as (n_pairs, read_len) uint8 arrays of bases as sequenced."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    G = np.concatenate([np.asarray(c[1], np.uint8) for c in contigs] + [np.full(1, 4, np.uint8)])
+    starts = np.cumsum([0] + [len(c[1]) for c in contigs])
+    lens = np.diff(starts).astype(np.float64)
+    rl = int(read_len)
+    j = np.arange(rl, dtype=np.int64)[None, :]
+    out1 = np.empty((n_pairs, rl), np.uint8)
+    out2 = np.empty((n_pairs, rl), np.uint8)
+
+    def convert(b, nxt):
+        u = rng.random(b.shape, dtype=np.float32)
+        meth = np.where((b == 1) & (nxt == 2), u < meth_cpg, u < meth_ch)
+        conv = (b == 1) & ~meth & (rng.random(b.shape, dtype=np.float32) < conversion)
+        b = b.copy()
+        b[conv] = 3
+        return b
+
+    for lo in range(0, n_pairs, chunk):
+        m = min(chunk, n_pairs - lo)
+        which = rng.choice(len(contigs), size=m, p=lens / lens.sum())
+        ins = np.maximum(np.round(rng.normal(insert_mean, insert_sd, m)).astype(np.int64), rl)
+        L = np.minimum(ins, lens[which].astype(np.int64))[:, None]
+        s = (starts[which] + (rng.random(m) * (lens[which] - L[:, 0] + 1)).astype(np.int64))[:, None]
+        bottom = (rng.random(m) < 0.5)[:, None]
+        # the sequenced strand S (top: the contig; bottom: its reverse complement) as positions
+        # of G: S[i] = G[s+i] or COMP[G[s+L-1-i]]; read 1 = S[0:rl], read 2 = revcomp(S[L-rl:L])
+        def strand(i):
+            pos = np.where(bottom, s + L - 1 - i, s + i)
+            inside = i < L
+            b = G[np.where(inside, pos, len(G) - 1)]
+            return np.where(inside & bottom, COMP[b], b)
+        a1 = convert(strand(j), strand(j + 1))
+        a2 = convert(strand(L - rl + j), strand(L - rl + j + 1))
+        r2 = COMP[a2[:, ::-1]]
+        for r in (a1, r2):
+            e = rng.random(r.shape, dtype=np.float32) < err
+            r[e] = (r[e] + rng.integers(1, 4, int(e.sum()), dtype=np.uint8)) % 4
+        out1[lo:lo + m], out2[lo:lo + m] = a1, r2
+    return out1, out2
+
+
+def write_fastq_block(path: str, reads, tag: int, first: int = 0, qual: int = ord("?")) -> None:
+    """FASTQ of equal-length reads ((n, L) codes 0..4), names @r<9-digit index>/<tag>,
+    every quality `qual` (Phred 30 by default), written with fixed-width records."""
+    reads = np.asarray(reads, np.uint8)
+    n, L = reads.shape
+    letters = np.frombuffer(b"ACGTN", np.uint8)
+    rec = 18 + 2 * L
+    with open(path, "wb") as f:
+        for lo in range(0, n, 200_000):
+            m = min(200_000, n - lo)
+            buf = np.empty((m, rec), np.uint8)
+            buf[:, 0], buf[:, 1] = ord("@"), ord("r")
+            idx = np.arange(first + lo, first + lo + m, dtype=np.int64)
+            for d in range(9):
+                buf[:, 10 - d] = ord("0") + (idx // 10 ** d) % 10
+            buf[:, 11], buf[:, 12], buf[:, 13] = ord("/"), ord("0") + tag, ord("\n")
+            buf[:, 14:14 + L] = letters[reads[lo:lo + m]]
+            buf[:, 14 + L], buf[:, 15 + L], buf[:, 16 + L] = ord("\n"), ord("+"), ord("\n")
+            buf[:, 17 + L:17 + 2 * L] = qual
+            buf[:, 17 + 2 * L] = ord("\n")
+            f.write(buf.tobytes())
+
+
+def write_fastq_ragged(path: str, seqs, offs, tag: int = 1, qual: int = ord("?")) -> None:
+    """FASTQ of reads of any length (seqs[offs[i]:offs[i+1]], codes 0..4), names as above."""
+    letters = np.frombuffer(b"ACGTN", np.uint8)
+    txt = letters[np.asarray(seqs, np.uint8)].tobytes()
+    with open(path, "wb") as f:
+        parts = []
+        for i in range(len(offs) - 1):
+            a, b = int(offs[i]), int(offs[i + 1])
+            parts.append(b"@r%09d/%d\n%s\n+\n%s\n" % (i, tag, txt[a:b], bytes([qual]) * (b - a)))
+            if len(parts) >= 100_000:
+                f.write(b"".join(parts))
+                parts = []
+        f.write(b"".join(parts))
+
+
 def bs_convert(read: np.ndarray, g2a: bool) -> np.ndarray:
     """In-silico conversion of bsConversion (bs_helpers.cpp:18-31): C->T for read 1,
     G->A for read 2."""

@@ -209,6 +209,12 @@ int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_rea
                           const uint8_t *d_seqs, const int64_t *d_offs, int64_t total_bases,
                           int32_t max_len, bsb_intv_t *d_out, int64_t *d_out_off);
 
+/* Measurement helper (no reference counterpart): the bwt_extend calls -- each one
+ * bwt_2occ4, i.e. two occurrence queries (bwt.c:189-220, 262-275) -- that the most
+ * recent seeding batch of this context made, passes 1-3 together.  Waits for the
+ * context stream. */
+int bsb_last_seed_extensions(bsb_ctx *ctx, int64_t *n_ext);
+
 /* ---- suffix-array lookup: bwt_sa ---------------------------------------- */
 
 /* pos[i] = bwt_sa(bwt, rows[i]) (bwt.c:86-96) for every row; host buffers. */

@@ -87,6 +87,32 @@ def ksw_batch(jobs: np.ndarray, seq: np.ndarray, mat: np.ndarray, o_del: int, e_
     return out, cells
 
 
+_REF_KSW = os.path.join(_HERE, "_ref", "libref_ksw.so")
+
+
+def have_reference_ksw() -> bool:
+    """Whether the reference's own ksw_extend2 was built here (oracle/Makefile.ref, from the
+    staged reference sources)."""
+    return os.path.exists(_REF_KSW)
+
+
+def ref_ksw_batch(jobs: np.ndarray, seq: np.ndarray, mat: np.ndarray, o_del: int, e_del: int,
+                  o_ins: int, e_ins: int, zdrop: int, n_threads: int = 1) -> np.ndarray:
+    """The reference's compiled ksw_extend2 (ksw.c:380-479, linked from its sources into
+    oracle/_ref/libref_ksw.so by oracle/ref_ksw_batch.c) over a job table on n_threads host
+    threads.  Returns out[n,6] int32."""
+    L = ctypes.CDLL(_REF_KSW)
+    P = ctypes.c_void_p
+    L.ref_ksw_batch.restype = ctypes.c_int
+    L.ref_ksw_batch.argtypes = [ctypes.c_int64, P, P, P] + [ctypes.c_int] * 5 + [P, ctypes.c_int]
+    jobs = np.ascontiguousarray(jobs)
+    seq = np.ascontiguousarray(seq, dtype=np.uint8)
+    mat = np.ascontiguousarray(mat, dtype=np.int8)
+    out = np.zeros((len(jobs), 6), np.int32)
+    L.ref_ksw_batch(len(jobs), _p(jobs), _p(seq), _p(mat), o_del, e_del, o_ins, e_ins, zdrop, _p(out), n_threads)
+    return out
+
+
 class OracleBwt:
     """The FM-index as the oracle sees it (bwt.h:46-58)."""
 

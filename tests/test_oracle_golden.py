@@ -53,3 +53,12 @@ def test_generator_is_seeded():
     jobs, seq = a
     assert jobs["qlen"].min() >= 10 and jobs["qlen"].max() <= 140
     assert (jobs["qoff"] + jobs["qlen"] <= len(seq)).all() and (jobs["toff"] + jobs["tlen"] <= len(seq)).all()
+
+
+@pytest.mark.skipif(not oracle.have_reference_ksw(), reason="reference sources not staged (oracle/_ref)")
+@pytest.mark.parametrize("fn", KSW_FIXTURES, ids=lambda f: os.path.basename(f))
+def test_reference_ksw_harness_reproduces_fixtures(fn):
+    """The threaded harness around the reference's own ksw_extend2 (the CPU baseline of the
+    extension bench) returns the fixtures' tuples: it runs the reference unchanged."""
+    jobs, seq, mat, params, ref = load_ksw(fn)
+    assert np.array_equal(oracle.ref_ksw_batch(jobs, seq, mat, *params, n_threads=4), ref)
