@@ -163,10 +163,12 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         const int h1_init = beg == 0 ? max(h0 - (P.o_del + e_del * (i + 1)), 0) : 0;   // ksw.c:421-424
         const bool empty = beg >= end;         // empty band: the zero row max stops the job
 
-        // pass 1: M, next-row E, and the two halves' F runs from a zero carry-in.
+        // pass 1: M, and the two halves' F runs from a zero carry-in (only their ends are
+        // kept: pass 2 runs the recurrence again from the true carry-in, which keeps E(i+1, j)
+        // and F out of the registers between the passes).
         // M = H(i-1,j-1) + score, or at most 0 when H(i-1,j-1) == 0 (ksw.c:431): the
         // minimum with H*16, which is >= H + score when H > 0 (scores <= 15).
-        uint32_t Mv[C2], En[C2], Pf[C2];
+        uint32_t Mv[C2];
         uint32_t local = 0;
         if (!__any_sync(act, tc >= 4)) {
             const uint32_t sel = sext2_selector(tc, tc);
@@ -175,8 +177,6 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                 const uint32_t sc = prmt2(prof[u], prof[u + C2], sel);
                 const uint32_t Hp = Hs[u];
                 const uint32_t M = __viaddmin_s16x2(Hp, sc, Hp * 16u);   // Hp <= 2047: no carry between halves
-                En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
-                Pf[u] = local;
                 local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
                 Mv[u] = M;
             }
@@ -189,8 +189,6 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                                                    sext2_selector(u & 3, (u + C2) & 3));
                 const uint32_t Hp = Hs[u];
                 const uint32_t M = __viaddmin_s16x2(Hp, sc, Hp * 16u);   // Hp <= 2047: no carry between halves
-                En[u] = __viaddmax_s16x2(Es[u], ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
-                Pf[u] = local;
                 local = __viaddmax_s16x2(local, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
                 Mv[u] = M;
             }
@@ -204,28 +202,29 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
             incl = __viaddmax_s32(__shfl_up_sync(act, incl, d, G), -eC * d, incl);
         const int excl = __shfl_up_sync(act, incl, 1, G);
         const int carry = gl == 0 ? 0 : excl;
-        const uint32_t carry2 = pk16(carry, max(carry - e_ins * C2, f_lo_end));
 
-        // pass 2: F, H, the row maximum key, and the new eh[] -- E(i+1, j) inside the
-        // band, 0 at end, kept beyond; H shifted one column up to end, kept beyond --
-        // and the non-zero cells.  Column 0's shifted H needs the left lane's last column
-        // and column C2-1 of this lane, so it is finished after the loop.
+        // pass 2: F (the recurrence F(i,j+1) = max(F(i,j) - e_ins, max(M - oe_ins, 0)) of
+        // ksw.c:446-447 from each half's carry-in), H, E(i+1,j), the row maximum key, and the
+        // new eh[] -- E(i+1, j) inside the band, 0 at end, kept beyond; H shifted one column
+        // up to end, kept beyond -- and the non-zero cells.  Column 0's shifted H needs the
+        // left lane's last column and column C2-1 of this lane, so it is finished after the loop.
         const int rend = end - base;               // |rend| <= 1023: exact in 16 bits
         // per half: ltm(u) = [column < rend]; lem(u) = [column <= rend] = ltm(u - 1)
         const uint32_t t_lt = pk16(rend, rend - C2);
         uint32_t ltm_prev = below16(t_lt, -1) * 0xffffu;
         uint32_t kmx = 0;                          // per half: max of H*16 + u over band columns
-        uint32_t cF = carry2;                      // per half: the carry minus e_ins per column
+        uint32_t F = pk16(carry, max(carry - e_ins * C2, f_lo_end));   // F entering each half
         uint32_t Hprev = 0, nE0 = 0, lem0 = 0, nzw = 0;
 #pragma unroll
         for (int u = 0; u < C2; ++u) {
-            const uint32_t F = __vimax_s16x2_relu(cF, Pf[u]);            // F >= 0 (ksw.c:446-447)
-            cF = __viaddmax_s16x2(cF, ne_ins, 0x80008000u);
-            const uint32_t H = __vimax3_s16x2(Mv[u], Es[u], F);
+            const uint32_t M = Mv[u], Eo = Es[u];
+            const uint32_t H = __vimax3_s16x2(M, Eo, F);
+            const uint32_t En = __viaddmax_s16x2(Eo, ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
+            F = __viaddmax_s16x2(F, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
             const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = ltm_prev;
             ltm_prev = ltm;
             kmx = __vimax_s16x2_relu(kmx, (H & ltm) * 16u + pk16(u, u));   // ties: the later column
-            const uint32_t nE = (En[u] & ltm) | (Es[u] & ~lem);
+            const uint32_t nE = (En & ltm) | (Eo & ~lem);
             Es[u] = nE;
             if (u > 0) {
                 const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);

@@ -57,8 +57,7 @@ extern "C" int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_
 {
     if (!param || n_jobs < 0) return BSB_EINVAL;
     if (n_jobs > BSB_NOALLOC_MAX_JOBS) return BSB_ECAPACITY;
-    if (n_jobs == 0) return 0;
-    if (!d_jobs || !d_seq || !d_out) return BSB_EINVAL;
+    if (n_jobs > 0 && (!d_jobs || !d_seq || !d_out)) return BSB_EINVAL;
     if (param->e_del < 1 || param->e_ins < 1 || param->o_del < 0 || param->o_ins < 0 || param->o_del > 65535 ||
         param->o_ins > 65535 || param->e_del > 65535 || param->e_ins > 65535)
         return BSB_EINVAL;
@@ -78,8 +77,9 @@ extern "C" int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return BSB_ECUDA;
     void *scratch = nullptr;
     int n_sm = 0;
-    int rc = setup_device(dev, &scratch, &n_sm);
+    int rc = setup_device(dev, &scratch, &n_sm);    // also for an empty batch: a warm-up call sets up
     if (rc) return rc;
+    if (n_jobs == 0) return 0;
     static const uint64_t tiles = ksw_map_tiles(ksw_default_tile_map());
     cudaError_t e = ksw_launch(P, d_jobs, n_jobs, seq_bytes, d_seq, nullptr, nullptr, tiles, d_out, d_cells, scratch,
                                n_sm, (cudaStream_t)stream, nullptr, nullptr);

@@ -25,7 +25,8 @@ constexpr KswTile kTileList[] = {
     {16, 13}, {16, 14}, {16, 15}, {16, 16},                                             // 37..40
     {32, 5},  {32, 6},  {32, 7},  {32, 8},  {32, 9},  {32, 10}, {32, 11}, {32, 12},    // 41..48
     {32, 13}, {32, 14}, {32, 15}, {32, 16},                                             // 49..52
-    {32, 20}, {32, 24}, {32, 28}, {32, 32}};                                            // 53..56
+    {32, 20}, {32, 24}, {32, 28}, {32, 32},                                             // 53..56
+    {4, 20},  {4, 24},  {4, 28},  {4, 32},  {4, 36}};                                   // 57..61
 constexpr int kNumTiles = sizeof(kTileList) / sizeof(kTileList[0]);
 constexpr int kMaxNeed = BSB_TILE_MAP_LEN - 1;    // columns 0..qlen with qlen <= 1023
 constexpr int kKswBlock = 128;                      // threads per block (4 warps)

@@ -13,6 +13,11 @@ KswTileLaunch ksw_tiles16_g4(int C)
     case 12: return ksw_tile16_launch<6, 4>;
     case 14: return ksw_tile16_launch<7, 4>;
     case 16: return ksw_tile16_launch<8, 4>;
+    case 20: return ksw_tile16_launch<10, 4>;
+    case 24: return ksw_tile16_launch<12, 4>;
+    case 28: return ksw_tile16_launch<14, 4>;
+    case 32: return ksw_tile16_launch<16, 4>;
+    case 36: return ksw_tile16_launch<18, 4>;
     default: return nullptr;
     }
 }

@@ -20,6 +20,11 @@ KswTileLaunch ksw_tiles_g4(int C)
     case 14: return ksw_tile_launch<14, 4>;
     case 15: return ksw_tile_launch<15, 4>;
     case 16: return ksw_tile_launch<16, 4>;
+    case 20: return ksw_tile_launch<20, 4>;
+    case 24: return ksw_tile_launch<24, 4>;
+    case 28: return ksw_tile_launch<28, 4>;
+    case 32: return ksw_tile_launch<32, 4>;
+    case 36: return ksw_tile_launch<36, 4>;
     default: return nullptr;
     }
 }

@@ -10,8 +10,14 @@
 // Shapes up to 18 columns per lane are held to 128 registers (4 blocks = 16 warps per
 // SM): measured on GB300, the extra warps hide the ALU dependency latency better than
 // the registers they cost (a few bytes of spill at C >= 15), 3-18 % faster.  Wider
-// shapes keep their registers.
+// 32-bit shapes keep their registers.
 constexpr int ksw_min_blocks(int C) { return C <= 18 ? 4 : 1; }
+// The 16-bit kernels hold E, H and M of their C2 = C/2 registers plus the C profile words:
+// without spills 4 blocks fit up to C2 = 12 (128 registers), 3 up to C2 = 16 (168), then 2.
+constexpr int ksw16_min_blocks(int C2, int G)
+{
+    return G != 4 ? ksw_min_blocks(2 * C2) : C2 <= 12 ? 4 : C2 <= 16 ? 3 : 2;
+}
 
 // range[0], range[1]: the jobs order[range[0] .. range[1]) this launch drains.
 template <int C, int G>
@@ -24,7 +30,7 @@ ksw_tile_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8
 }
 
 template <int C2, int G>
-__global__ void __launch_bounds__(kKswBlock, ksw_min_blocks(2 * C2))
+__global__ void __launch_bounds__(kKswBlock, ksw16_min_blocks(C2, G))
 ksw_tile16_kernel(KswParams P, const bsb_ext_job_t *__restrict__ jobs, const uint8_t *__restrict__ seq,
                   const int32_t *__restrict__ order, const int32_t *__restrict__ range, int *__restrict__ counter,
                   bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)

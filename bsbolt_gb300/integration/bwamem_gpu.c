@@ -7,7 +7,7 @@
  *   kt_for(opt->n_threads, worker1, &w, (opt->flag&MEM_F_PE)? n>>1 : n);
  * with
  *   if (mem_align_batch_gpu(g_bsb, opt, bns, pac, n, seqs, w.regs) ||
- *       mem_gen_cigar_prepass_gpu(g_bsb, opt, bns, n, seqs, w.regs))
+ *       mem_gen_cigar_prepass_gpu(g_bsb, opt, bns, n, seqs, w.regs, n_processed))
  *       err_fatal(__func__, "%s", bsb_last_error(g_bsb));
  * after mem_pestat (bwamem.c:1342) add
  *   if (mem_matesw_prepass_gpu(g_bsb, opt, bns, pac, pes, n, seqs, w.regs))
@@ -128,7 +128,7 @@ static struct {
     int8_t mat[25];
     int o_del, e_del, o_ins, e_ins;
     int64_t l_pac, crick_l;
-    int64_t served;
+    int64_t served, passed;
 } g_cig;
 
 static uint64_t cig_hash(int64_t rb, int64_t re, int l, int w)
@@ -151,58 +151,135 @@ void mem_gen_cigar_stats(int64_t *kept, int64_t *served)
     if (served) *served = __atomic_load_n(&g_cig.served, __ATOMIC_RELAXED);
 }
 
+int64_t mem_gen_cigar_passed(void) { return __atomic_load_n(&g_cig.passed, __ATOMIC_RELAXED); }
+
+int mem_mark_primary_se(const mem_opt_t *opt, int n, mem_alnreg_t *a, int64_t id);   /* bwamem.c:525 */
+
+/* A region the CIGAR pre-pass prepares: its read and the fields mem_reg2aln uses. */
+typedef struct {
+    int64_t rb, re;
+    int32_t qb, qe, truesc, w, read;
+} cig_pick_t;
+
+static int cig_eligible(const mem_opt_t *opt, const bseq1_t *s, const mem_alnreg_t *a)
+{
+    return s->oseq && a->score >= opt->T && a->rb >= 0 && a->qe - a->qb <= BSB_CIGAR_MAX_LEN &&
+           a->re - a->rb <= BSB_CIGAR_MAX_LEN;
+}
+
+/* The regions worker2 is expected to hand to mem_reg2aln: on a copy of each read's regions,
+ * mem_mark_primary_se with the id worker2 gives it (bwamem.c:1300, bwamem_pair.c:277-278),
+ * then the primary and supplementary regions (mem_reg2sam, bwamem.c:1121-1128), the XA
+ * candidates (mem_gen_alt's get_pri_idx and hit limits, bwamem_extra.c:91-120) and, for
+ * pairs, the regions within XA_drop_ratio of the read's best when there are at most
+ * CIG_PAIR_NEAR of them (mem_pair may choose any, bwamem_pair.c:188-196; in a large repeat
+ * family the choice is one of hundreds and is left to the reference's function).  A region
+ * that worker2 asks for and that is not here -- a mate rescue moved the marking, or the
+ * pair chose another hit -- is answered by the reference's own function; with -a
+ * (MEM_F_ALL) every region is prepared. */
+#define CIG_PAIR_NEAR 16
+static cig_pick_t *cig_select(const mem_opt_t *opt, int n, const bseq1_t *seqs, const mem_alnreg_v *regs,
+                              int64_t n_processed, int64_t *n_pick)
+{
+    int64_t m = 0, cap = 0;
+    cig_pick_t *pick = 0;
+    mem_alnreg_t *tmp = 0;
+    int *cnt = 0, i, j, tmax = 0;
+    for (i = 0; i < n; ++i) {
+        cap += regs[i].n;
+        tmax = (int)regs[i].n > tmax ? (int)regs[i].n : tmax;
+    }
+    pick = (cig_pick_t *)malloc(sizeof(cig_pick_t) * (cap + 1));
+    tmp = (mem_alnreg_t *)malloc(sizeof(mem_alnreg_t) * (tmax + 1));
+    cnt = (int *)malloc(sizeof(int) * (tmax + 1));
+    for (i = 0; i < n; ++i) {
+        const int k = (int)regs[i].n;
+        const mem_alnreg_t *a = regs[i].a;
+        int near = 0;
+        if (k == 0 || !seqs[i].oseq) continue;
+        if (!(opt->flag & MEM_F_ALL)) {
+            memcpy(tmp, a, sizeof(mem_alnreg_t) * k);
+            mem_mark_primary_se(opt, k, tmp, n_processed + i);
+            memset(cnt, 0, sizeof(int) * k);
+            for (j = 0; j < k; ++j) {
+                const int r = tmp[j].secondary_all;
+                if (r >= 0 && tmp[j].score >= tmp[r].score * opt->XA_drop_ratio) ++cnt[r];
+            }
+            a = tmp;
+            for (j = 0; j < k; ++j) near += a[j].score >= a[0].score * opt->XA_drop_ratio;
+        }
+        for (j = 0; j < k; ++j) {
+            const mem_alnreg_t *p = &a[j];
+            if (!cig_eligible(opt, &seqs[i], p)) continue;
+            if (!(opt->flag & MEM_F_ALL) && p->secondary >= 0) {
+                const int r = p->secondary_all;
+                const int xa = r >= 0 && p->score >= a[r].score * opt->XA_drop_ratio && cnt[r] <= opt->max_XA_hits;
+                const int pair = (opt->flag & MEM_F_PE) && near <= CIG_PAIR_NEAR &&
+                                 p->score >= a[0].score * opt->XA_drop_ratio;
+                if (!xa && !pair) continue;
+            }
+            pick[m].rb = p->rb, pick[m].re = p->re, pick[m].qb = p->qb, pick[m].qe = p->qe;
+            pick[m].truesc = p->truesc, pick[m].w = p->w, pick[m].read = i;
+            ++m;
+        }
+    }
+    free(tmp);
+    free(cnt);
+    *n_pick = m;
+    return pick;
+}
+
 int mem_gen_cigar_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, int n, const bseq1_t *seqs,
-                              const mem_alnreg_v *regs)
+                              const mem_alnreg_v *regs, int64_t n_processed)
 {
     bsb_align_opt_t o;
-    int64_t n_jobs = 0, qn = 0, on = 0, cap = 0, used = 0, k, t;
-    int i, j, rc;
+    int64_t n_jobs = 0, qn = 0, on = 0, cap = 0, used = 0, k, t, n_pick = 0;
+    int rc;
+    cig_pick_t *pick;
     cig_clear();
-    for (i = 0; i < n; ++i)
-        for (j = 0; j < (int)regs[i].n; ++j) {
-            const mem_alnreg_t *a = &regs[i].a[j];
-            if (!seqs[i].oseq || a->score < opt->T || a->rb < 0 || a->qe - a->qb > BSB_CIGAR_MAX_LEN ||
-                a->re - a->rb > BSB_CIGAR_MAX_LEN)
-                continue;
-            ++n_jobs, qn += a->qe - a->qb, on += a->qe - a->qb;
-            cap += 14 * ((a->qe - a->qb) + (a->re - a->rb)) + 48;
-        }
-    if (n_jobs == 0) return 0;
+    pick = cig_select(opt, n, seqs, regs, n_processed, &n_pick);
+    for (k = 0; k < n_pick; ++k) {
+        const cig_pick_t *a = &pick[k];
+        ++n_jobs, qn += a->qe - a->qb, on += a->qe - a->qb;
+        cap += 14 * ((a->qe - a->qb) + (a->re - a->rb)) + 48;
+    }
+    if (n_jobs == 0) {
+        free(pick);
+        return 0;
+    }
     g_cig.jobs = (bsb_cigar_job_t *)malloc(sizeof(bsb_cigar_job_t) * n_jobs);
     g_cig.out = (bsb_cigar_out_t *)malloc(sizeof(bsb_cigar_out_t) * n_jobs);
     g_cig.qbuf = (uint8_t *)malloc(qn + 1);
     g_cig.obuf = (uint8_t *)malloc(on + 1);
     g_cig.blob = (uint8_t *)malloc(cap + 64);
     qn = on = 0;
-    for (i = 0, k = 0; i < n; ++i)
-        for (j = 0; j < (int)regs[i].n; ++j) {
-            const mem_alnreg_t *a = &regs[i].a[j];
-            bsb_cigar_job_t *jb;
-            int l, w2, tmp, x;
-            if (!seqs[i].oseq || a->score < opt->T || a->rb < 0 || a->qe - a->qb > BSB_CIGAR_MAX_LEN ||
-                a->re - a->rb > BSB_CIGAR_MAX_LEN)
-                continue;
-            l = a->qe - a->qb;
-            /* the band of mem_reg2aln's first bwa_gen_cigar2 call (bwamem.c:1219-1227) */
-            tmp = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_del, opt->e_del);
-            w2 = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_ins, opt->e_ins);
-            w2 = w2 > tmp ? w2 : tmp;
-            if (w2 > opt->w) w2 = w2 < a->w ? w2 : a->w;
-            w2 = w2 < opt->w << 2 ? w2 : opt->w << 2;
-            jb = &g_cig.jobs[k++];
-            jb->rb = a->rb, jb->re = a->re, jb->l_query = l, jb->w = w2;
-            /* the nt4 query from qb and the original read from its start, as mem_reg2aln
-             * hands them over (bwamem.c:1211-1216, 1228) */
-            jb->qoff = qn, jb->ooff = on;
-            for (x = 0; x < l; ++x) {
-                const int c = (uint8_t)seqs[i].seq[a->qb + x];
-                g_cig.qbuf[qn++] = c < 5 ? c : nst_nt4_table[c];
-            }
-            for (x = 0; x < l; ++x) {
-                const int c = x < seqs[i].l_seq ? (uint8_t)seqs[i].oseq[x] : 4;
-                g_cig.obuf[on++] = c < 5 ? c : nst_nt4_table[c];
-            }
+    for (k = 0; k < n_pick; ++k) {
+        const cig_pick_t *a = &pick[k];
+        const bseq1_t *s = &seqs[a->read];
+        bsb_cigar_job_t *jb;
+        int l, w2, tmp, x;
+        l = a->qe - a->qb;
+        /* the band of mem_reg2aln's first bwa_gen_cigar2 call (bwamem.c:1219-1227) */
+        tmp = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_del, opt->e_del);
+        w2 = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_ins, opt->e_ins);
+        w2 = w2 > tmp ? w2 : tmp;
+        if (w2 > opt->w) w2 = w2 < a->w ? w2 : a->w;
+        w2 = w2 < opt->w << 2 ? w2 : opt->w << 2;
+        jb = &g_cig.jobs[k];
+        jb->rb = a->rb, jb->re = a->re, jb->l_query = l, jb->w = w2;
+        /* the nt4 query from qb and the original read from its start, as mem_reg2aln
+         * hands them over (bwamem.c:1211-1216, 1228) */
+        jb->qoff = qn, jb->ooff = on;
+        for (x = 0; x < l; ++x) {
+            const int c = (uint8_t)s->seq[a->qb + x];
+            g_cig.qbuf[qn++] = c < 5 ? c : nst_nt4_table[c];
         }
+        for (x = 0; x < l; ++x) {
+            const int c = x < s->l_seq ? (uint8_t)s->oseq[x] : 4;
+            g_cig.obuf[on++] = c < 5 ? c : nst_nt4_table[c];
+        }
+    }
+    free(pick);
     mem_opt_to_bsb(opt, &o);
     rc = bsb_gen_cigar_batch(ctx, &o, bns->crick_l, (int32_t)n_jobs, g_cig.jobs, g_cig.qbuf, qn, g_cig.obuf, on,
                              g_cig.out, g_cig.blob, cap + 64, &used);
@@ -261,6 +338,7 @@ uint32_t *__wrap_bwa_gen_cigar2(const int8_t mat[25], int o_del, int e_del, int 
             }
         }
     }
+    if (n_cigar && oquery) __atomic_add_fetch(&g_cig.passed, 1, __ATOMIC_RELAXED);   /* a full call not served */
     return __real_bwa_gen_cigar2(mat, o_del, e_del, o_ins, e_ins, w_, l_pac, pac, opac, l_query, query, rb, re, score,
                                  n_cigar, NM, crick_l, oquery, cg_meth, cg_unmeth, ch_meth, ch_unmeth);
 }

@@ -32,19 +32,24 @@ int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns,
 int64_t mem_align_regrown(void);
 
 /* CIGAR pre-pass (bwa_gen_cigar2 on the GPU).  Called after mem_align_batch_gpu
- * and before worker2: runs bsb_gen_cigar_batch for every region of the batch
- * that worker2 may turn into a SAM record (score >= opt->T), with the first band
- * mem_reg2aln tries (bwamem.c:1219-1228), and keeps the records.  The glue's
- * __wrap_bwa_gen_cigar2 (link with -Wl,--wrap=bwa_gen_cigar2) answers a call
- * whose job -- interval, band, query and original-read bytes, scoring -- equals a
- * kept record with a copy of it, and passes every other call (band retries,
- * mate-rescued regions, score-only calls) to the reference's own function, so
- * the output is the reference's either way.  The records live until the next
- * pre-pass.  Returns 0 or a BSB_E* code. */
+ * and before worker2: runs bsb_gen_cigar_batch for the regions of the batch that
+ * worker2 is expected to turn into SAM records or XA hits (score >= opt->T; which ones is
+ * read off mem_mark_primary_se run on a copy of each read's regions with the id worker2
+ * gives it, n_processed + i), with the first band mem_reg2aln tries
+ * (bwamem.c:1219-1228), and keeps the records.  The glue's __wrap_bwa_gen_cigar2 (link
+ * with -Wl,--wrap=bwa_gen_cigar2) answers a call whose job -- interval, band, query and
+ * original-read bytes, scoring -- equals a kept record with a copy of it, and passes
+ * every other call (band retries, mate-rescued regions, score-only calls, regions the
+ * selection did not foresee) to the reference's own function, so the output is the
+ * reference's either way.  The records live until the next pre-pass.  Returns 0 or a
+ * BSB_E* code. */
 int mem_gen_cigar_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, int n, const bseq1_t *seqs,
-                              const mem_alnreg_v *regs);
+                              const mem_alnreg_v *regs, int64_t n_processed);
 /* Records kept by the last pre-pass, and calls answered from them since. */
 void mem_gen_cigar_stats(int64_t *kept, int64_t *served);
+/* Full bwa_gen_cigar2 calls (CIGAR and methylation outputs wanted) since the last pre-pass
+ * that no kept record answered. */
+int64_t mem_gen_cigar_passed(void);
 
 /* Mate-rescue pre-pass (ksw_align2 on the GPU).  Called after mem_pestat and
  * before worker2 of a paired-end batch: for every pair it lists the ksw_align2

@@ -53,8 +53,8 @@ typedef struct {
 
 static bsb_ctx *g_hook_ctx;
 static long g_hook_calls;
-static double g_t_align, g_t_cigar, g_t_sw;
-static int64_t g_cig_kept, g_cig_served, g_sw_kept, g_sw_served, g_reads;
+static double g_t_align, g_t_cigar, g_t_sw, g_t_worker2;
+static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
 static double hook_now(void)
 {
@@ -67,7 +67,7 @@ static void hook_take_stats(void)
 {
     int64_t k, s;
     mem_gen_cigar_stats(&k, &s);
-    g_cig_kept += k, g_cig_served += s;
+    g_cig_kept += k, g_cig_served += s, g_cig_passed += mem_gen_cigar_passed();
     mem_matesw_stats(&k, &s);
     g_sw_kept += k, g_sw_served += s;
 }
@@ -75,10 +75,10 @@ static void hook_take_stats(void)
 static void hook_report(void)
 {
     hook_take_stats();
-    fprintf(stderr, "[bsb_gpu] reads %lld; GPU time: regions %.3f s, cigar %.3f s, rescue %.3f s\n",
-            (long long)g_reads, g_t_align, g_t_cigar, g_t_sw);
-    fprintf(stderr, "[bsb_gpu] cigar records kept %lld served %lld\n", (long long)g_cig_kept,
-            (long long)g_cig_served);
+    fprintf(stderr, "[bsb_gpu] reads %lld; GPU time: regions %.3f s, cigar %.3f s, rescue %.3f s; worker2 %.3f s\n",
+            (long long)g_reads, g_t_align, g_t_cigar, g_t_sw, g_t_worker2);
+    fprintf(stderr, "[bsb_gpu] cigar records kept %lld served %lld passed %lld\n", (long long)g_cig_kept,
+            (long long)g_cig_served, (long long)g_cig_passed);
     fprintf(stderr, "[bsb_gpu] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
     fprintf(stderr, "[bsb_gpu] region buffer regrown %lld\n", (long long)mem_align_regrown());
 }
@@ -169,7 +169,7 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
         if ((rc = mem_align_batch_gpu(g_hook_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs)))
             hook_fail(g_hook_ctx, rc, "GPU alignment");
         t1 = hook_now();
-        if ((rc = mem_gen_cigar_prepass_gpu(g_hook_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs)))
+        if ((rc = mem_gen_cigar_prepass_gpu(g_hook_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs, w->n_processed)))
             hook_fail(g_hook_ctx, rc, "GPU CIGAR pre-pass");
         g_t_align += t1 - t0, g_t_cigar += hook_now() - t1, g_reads += n_reads;
         return;
@@ -178,6 +178,8 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
     t0 = hook_now();
     if ((rc = mem_matesw_prepass_gpu(g_hook_ctx, w->opt, w->bns, w->pac, w->pes, n_reads, w->seqs, w->regs)))
         hook_fail(g_hook_ctx, rc, "GPU mate-rescue pre-pass");
-    g_t_sw += hook_now() - t0;
+    t1 = hook_now();
+    g_t_sw += t1 - t0;
     __real_kt_for(n_threads, func, data, n);
+    g_t_worker2 += hook_now() - t1;
 }

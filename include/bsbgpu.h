@@ -113,7 +113,7 @@ float bsb_last_kernel_ms(const bsb_ctx *ctx);
  * query length.  The shape changes the time, never a result.  The library
  * ships a default map measured on GB300; an autotuner (bsbolt_gb300.autotune)
  * can measure the shapes on the caller's own jobs and install its map. */
-#define BSB_NUM_TILES 57
+#define BSB_NUM_TILES 62
 #define BSB_TILE_MAP_LEN 1025    /* entry [qlen + 1] for qlen = 0..1023; [0] unused */
 
 /* Fills G[t], C[t] for the compiled shapes t < min(max, BSB_NUM_TILES);
@@ -399,13 +399,23 @@ int bsb_mlp_adam(bsb_ctx *ctx, bsb_mlp_weights_t *d_w, float *d_master, float *d
  *   - At most BSB_NOALLOC_MAX_JOBS jobs per call; a larger n_jobs returns
  *     BSB_ECAPACITY before any work is queued.
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream
- *     capture.
+ *     (cudaGetSymbolAddress), also when n_jobs is 0; make that first call
+ *     before any stream capture.  The extension kernels themselves are
+ *     loaded by the CUDA runtime on their first launch, which takes device
+ *     memory for their code: a warm-up batch that reaches the shapes and
+ *     cell widths the later calls use (16-bit cells need penalties and
+ *     scores as bsb_extend_batch allows them, max score <= 15) leaves
+ *     nothing to load later.
+ *   - Every shape of the library's default tile map is launched on every
+ *     call (those with no jobs exit at once): the tile map is not chosen
+ *     per batch.
  *   - Every call shares the array and it keeps the last call's contents
  *     (the launch clears what must start at zero).  Calls whose work
  *     overlaps on the GPU race on it: order them on one stream.
  *   - Jobs that fail the preconditions of bsb_extend_batch are skipped and
- *     their output slots left untouched. */
+ *     their output slots left untouched, and nothing reports them: validate
+ *     jobs as bsb_extend_batch does (qlen <= 1023, 0 < h0 <= 2^20, ranges
+ *     inside seq_bytes, flags 0) before the call. */
 #define BSB_NOALLOC_MAX_JOBS (1 << 18)
 int bsb_extend_batch_noalloc(const bsb_ext_param_t *param, const bsb_ext_job_t *d_jobs,
                              int64_t n_jobs, const uint8_t *d_seq, int64_t seq_bytes,

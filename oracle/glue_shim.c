@@ -147,7 +147,8 @@ static void print_stats(void)
     int64_t kept, served;
     take_sw_stats();
     mem_gen_cigar_stats(&kept, &served);
-    fprintf(stderr, "[bsb_glue] cigar records kept %lld served %lld\n", (long long)kept, (long long)served);
+    fprintf(stderr, "[bsb_glue] cigar records kept %lld served %lld passed %lld\n", (long long)kept, (long long)served,
+            (long long)mem_gen_cigar_passed());
     fprintf(stderr, "[bsb_glue] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
     fprintf(stderr, "[bsb_glue] region buffer regrown %lld\n", (long long)mem_align_regrown());
 }
@@ -192,7 +193,7 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
             if (getenv("BSB_SHIM_STATS")) atexit(print_stats);
         }
         if (mem_align_batch_gpu(&g_ctx, w->opt, w->bns, w->pac, n_reads, w->seqs, w->regs) != 0 ||
-            mem_gen_cigar_prepass_gpu(&g_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs) != 0)
+            mem_gen_cigar_prepass_gpu(&g_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs, w->n_processed) != 0)
             abort();
         return;
     }

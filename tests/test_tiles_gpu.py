@@ -116,3 +116,29 @@ def test_autotune_map_is_valid_and_exact(gpu_ctx):
     finally:
         autotune.set_map(gpu_ctx, None)
     assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 100), (16, 4, 6, 1, 6, 1, 100)],
+                         ids=["bwa_16bit_cells", "a16_32bit_cells"])
+def test_every_shape_matches_oracle(gpu_ctx, scoring):
+    """Each compiled shape, alone in the map for the query lengths it holds, on jobs of those
+    lengths: tuples equal the oracle's.  With a = 16 the scores leave the 16-bit cells' range
+    and every shape runs its 32-bit kernel."""
+    a, b, o_del, e_del, o_ins, e_ins, zd = scoring
+    jobs, seq = mixed_jobs(seed=9, n_long=120)
+    mat = synth.fill_scmat(a, b)
+    ref, _ = oracle.ksw_batch(jobs, seq, mat, o_del, e_del, o_ins, e_ins, zd, n_threads=os.cpu_count() or 4)
+    sl = autotune.shapes()
+    base = autotune.default_map()
+    need = jobs["qlen"].astype(np.int64) + 1
+    try:
+        for t, (g, c) in enumerate(sl):
+            m = base.copy()
+            m[1:g * c + 1] = t
+            autotune.set_map(gpu_ctx, m)
+            sel = np.nonzero(need <= g * c)[0]
+            out = extend.ksw_extend2_batch(gpu_ctx, jobs[sel], seq, mat, o_del, e_del, o_ins, e_ins, zd)
+            bad = np.nonzero((out != ref[sel]).any(axis=1))[0]
+            assert len(bad) == 0, f"shape {g}x{c}: {len(bad)} tuples differ, first job {sel[bad[:3]]}"
+    finally:
+        autotune.set_map(gpu_ctx, None)
