@@ -969,10 +969,11 @@ def run_ours(args, ws, rank, local):
     dom_ms = float(tile_ms[dom])
     achieved = tile_cells[dom] * INT_OPS_PER_CELL / (dom_ms * 1e-3) / 1e12
     dom_g, dom_c = shape_list[dom]
-    dom16 = dom_c % 2 == 0             # even C: 16-bit cells (the jobs of this batch all fit)
+    dom16 = dom_c % 2 == 0 and dom_c <= 32    # even C up to 32: 16-bit cells (the jobs of this batch all fit)
     dom_name = ("ksw_tile16_kernel<%d,%d>" % (dom_c // 2, dom_g)) if dom16 else ("ksw_tile_kernel<%d,%d>" % (dom_c, dom_g))
     dom_peak = int16_peak if dom16 else int_peak
-    cells16_frac = float(sum(tile_cells[t] for t in range(len(shape_list)) if shape_list[t][1] % 2 == 0)
+    cells16_frac = float(sum(tile_cells[t] for t in range(len(shape_list))
+                             if shape_list[t][1] % 2 == 0 and shape_list[t][1] <= 32)
                          / max(tile_cells.sum(), 1.0))
     traffic = None
     prof = os.path.join(ROOT, "profiles", "ksw_tile_kernel_traffic.txt")
@@ -1102,7 +1103,8 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
                     "h2d_bytes_per_step": int(jobs_u8.nbytes + len(seq)), "d2h_bytes_per_step": int(n * 24),
                     "tuples_match_device_run": e2e_match, "s_per_step": round(e2e_s, 4)},
-            "gpu_launches": (SCHED_KERNELS + sum(2 if shape_list[t][1] % 2 == 0 else 1 for t in mapped)) * args.steps,
+            "gpu_launches": (SCHED_KERNELS + sum(2 if shape_list[t][1] % 2 == 0 and shape_list[t][1] <= 32 else 1
+                                                 for t in mapped)) * args.steps,
             "clocks": clocks,
             "pipeline": secondary,
             "learned_schedule": learned,

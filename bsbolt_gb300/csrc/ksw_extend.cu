@@ -55,12 +55,12 @@ __device__ __forceinline__ int cost_class(uint32_t key)
     return c < kWideClass ? c : kWideClass - 1;
 }
 
-// Shapes with a 16-bit kernel (even C), as a bit set.
+// Shapes with a 16-bit kernel (tile_has_pack16), as a bit set.
 constexpr uint64_t pack16_tiles()
 {
     uint64_t m = 0;
     for (int t = 0; t < kNumTiles; ++t)
-        if (kTileList[t].C % 2 == 0) m |= 1ull << t;
+        if (tile_has_pack16(kTileList[t].C)) m |= 1ull << t;
     return m;
 }
 constexpr uint64_t kPack16Tiles = pack16_tiles();

@@ -57,6 +57,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                                                 int lo, int hi, int *__restrict__ counter,
                                                 bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
 {
+    static_assert(C2 <= 16, "the row-maximum key and the non-zero bits hold a column index in 4 bits per half");
     constexpr int C = 2 * C2;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);

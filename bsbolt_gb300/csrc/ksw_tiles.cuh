@@ -34,6 +34,10 @@ constexpr int kKswBlock = 128;                      // threads per block (4 warp
 static_assert(kNumTiles == BSB_NUM_TILES, "tile list and public header disagree");
 static_assert(kNumTiles <= 64, "tile sets are 64-bit masks");
 
+// Shapes with a 16-bit two-columns-per-register kernel: an even C of at most 32 (the
+// row-maximum key and the non-zero-column bits keep a column index in 4 bits per half).
+constexpr bool tile_has_pack16(int C) { return C % 2 == 0 && C <= 32; }
+
 constexpr int tile_index(int G, int C)
 {
     for (int t = 0; t < kNumTiles; ++t)
@@ -98,10 +102,10 @@ inline KswTileLaunch ksw_tile_launcher(int t)
     }
 }
 
-// The 16-bit two-columns-per-register kernel of tile t (shapes with an even C), or NULL.
+// The 16-bit two-columns-per-register kernel of tile t (tile_has_pack16), or NULL.
 inline KswTileLaunch ksw_tile16_launcher(int t)
 {
-    if (t < 0 || t >= kNumTiles || kTileList[t].C % 2) return nullptr;
+    if (t < 0 || t >= kNumTiles || !tile_has_pack16(kTileList[t].C)) return nullptr;
     const KswTile s = kTileList[t];
     switch (s.G) {
     case 4: return ksw_tiles16_g4(s.C);

@@ -17,7 +17,6 @@ KswTileLaunch ksw_tiles16_g4(int C)
     case 24: return ksw_tile16_launch<12, 4>;
     case 28: return ksw_tile16_launch<14, 4>;
     case 32: return ksw_tile16_launch<16, 4>;
-    case 36: return ksw_tile16_launch<18, 4>;
     default: return nullptr;
     }
 }

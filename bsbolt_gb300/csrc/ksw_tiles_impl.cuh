@@ -13,10 +13,11 @@
 // 32-bit shapes keep their registers.
 constexpr int ksw_min_blocks(int C) { return C <= 18 ? 4 : 1; }
 // The 16-bit kernels hold E, H and M of their C2 = C/2 registers plus the C profile words:
-// without spills 4 blocks fit up to C2 = 12 (128 registers), 3 up to C2 = 16 (168), then 2.
+// with 4 lanes per job, 4 blocks fit without spills up to C2 = 12 (128 registers), 3 up to
+// C2 = 16 (168).
 constexpr int ksw16_min_blocks(int C2, int G)
 {
-    return G != 4 ? ksw_min_blocks(2 * C2) : C2 <= 12 ? 4 : C2 <= 16 ? 3 : 2;
+    return G != 4 ? ksw_min_blocks(2 * C2) : C2 <= 12 ? 4 : 3;
 }
 
 // range[0], range[1]: the jobs order[range[0] .. range[1]) this launch drains.
