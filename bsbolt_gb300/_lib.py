@@ -22,7 +22,7 @@ BSB_ETOOLONG = -6
 BSB_ENOINDEX = -7
 BSB_ECAPACITY = -8
 BSB_NOALLOC_MAX_JOBS = 1 << 18
-BSB_NUM_TILES = 62
+BSB_NUM_TILES = 61
 BSB_TILE_MAP_LEN = 1025
 
 # every extern "C" symbol include/bsbgpu.h declares

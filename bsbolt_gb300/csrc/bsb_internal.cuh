@@ -12,8 +12,9 @@
 
 // Longest read the seeding kernels accept (bounds the per-thread interval lists).
 #define BSB_SEED_MAX_LEN 1024
-// Longest read the full seed-chain-extend batch accepts (extension tiles up to 16 columns per lane).
-#define BSB_ALIGN_MAX_LEN 512
+// Longest read the full seed-chain-extend batch accepts: its extensions fit the widest
+// warp DP of chain2aln_kernel, 32 columns per lane (max_len + 1 <= 1024 columns).
+#define BSB_ALIGN_MAX_LEN 1023
 // Most pieces the host extension entry splits a batch into (copies overlap the extension).
 #define BSB_MAX_CHUNKS 8
 #define BSB_AUX_STREAMS 3
@@ -78,7 +79,17 @@ struct bsb_ctx {
     // chaining / chain-extension scratch
     void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
     size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;
+    // staging of the seed-level Smith-Waterman filter inside an alignment batch (the
+    // batch's own reads and seeds occupy d_in / d_out meanwhile)
+    void *flt_in = nullptr, *flt_out = nullptr, *flt_dev = nullptr;
+    size_t flt_in_bytes = 0, flt_out_bytes = 0, flt_dev_bytes = 0;
 };
+
+// bsb_align2_batch with explicit device staging buffers (grown as needed) in place of the
+// context's d_in / d_out.
+int bsb_align2_run(bsb_ctx *ctx, const bsb_ext_param_t *p, const bsb_sw_job_t *jobs, int64_t n, const uint8_t *seq,
+                   int64_t seq_bytes, bsb_kswr_t *out, void **in_buf, size_t *in_bytes, void **out_buf,
+                   size_t *out_bytes);
 
 // SA lookups of device rows with the context's index (bwt_sa, bwt.c:86-96).
 cudaError_t bsb_sa_launch_ctx(bsb_ctx *ctx, const uint64_t *d_rows, int64_t n, uint64_t *d_pos);

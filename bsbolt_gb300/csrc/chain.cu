@@ -14,6 +14,7 @@
 //                           read and the device 2-bit reference directly, so no
 //                           reversed copies or target windows are materialised.
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -767,6 +768,143 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
     }
 }
 
+// ---------------------------------------------------------------- mem_flt_chained_seeds
+
+// mem_flt_chained_seeds (bwamem.c:602-619) for the reads whose length makes it run
+// (min_hsp[r] >= 0; the host evaluates the reference's double and float thresholds):
+// each seed of each kept chain gets mem_seed_sw's score (bwamem.c:574-598) -- ksw_align2
+// with KSW_XSTART over windows of 50 bases around the seed, on the GPU's ksw_align2 --
+// and the chain keeps the seeds with no Smith-Waterman or a score of at least min_hsp,
+// rescored.  seed_sw_window is mem_seed_sw up to its ksw_align2 call, with bns_fetch_seq's
+// clip to the contig of the window's middle (bntseq.c:436-461); false: no SW, score -1.
+constexpr int kSeedSwShortLen = 200, kSeedSwExt = 50;     // MEM_SHORT_LEN, MEM_SHORT_EXT
+
+__device__ bool seed_sw_window(const DevBns &B, int l_query, const DevSeed &s, int &qb, int &qe, int64_t &rb,
+                               int64_t &re)
+{
+    const int64_t l_pac = B.l_pac;
+    if (s.len >= kSeedSwShortLen) return false;
+    qb = s.qbeg, qe = s.qbeg + s.len;
+    rb = s.rbeg, re = s.rbeg + s.len;
+    const int64_t mid = (rb + re) >> 1;
+    qb -= kSeedSwExt; qb = qb > 0 ? qb : 0;
+    qe += kSeedSwExt; qe = qe < l_query ? qe : l_query;
+    rb -= kSeedSwExt; rb = rb > 0 ? rb : 0;
+    re += kSeedSwExt; re = re < l_pac << 1 ? re : l_pac << 1;
+    if (rb < l_pac && l_pac < re) {
+        if (mid < l_pac) re = l_pac;
+        else rb = l_pac;
+    }
+    if (qe - qb >= kSeedSwShortLen || re - rb >= kSeedSwShortLen) return false;
+    int is_rev;
+    const int rid = pos2rid(B, depos(B, mid, is_rev));
+    int64_t far_beg = B.ann_offset[rid], far_end = far_beg + B.ann_len[rid];
+    if (is_rev) {
+        const int64_t t = far_beg;
+        far_beg = (l_pac << 1) - far_end;
+        far_end = (l_pac << 1) - t;
+    }
+    rb = rb > far_beg ? rb : far_beg;
+    re = re < far_end ? re : far_end;
+    return true;
+}
+
+// Per read (thread per read): the Smith-Waterman jobs its seeds need and their bytes.
+__global__ void seed_sw_count(DevBns B, int n_reads, const int *__restrict__ min_hsp,
+                              const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
+                              const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
+                              const DevChain *__restrict__ chains, const int *__restrict__ n_chains,
+                              int *__restrict__ n_jobs, int64_t *__restrict__ n_bytes)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        int nj = 0;
+        int64_t nb = 0;
+        if (min_hsp[r] >= 0) {
+            const int64_t R0 = row_off_of_seed[seed_off[r]];
+            const int l_query = (int)(read_off[r + 1] - read_off[r]);
+            for (int ci = 0; ci < n_chains[r]; ++ci) {
+                const DevChain c = chains[R0 + ci];
+                for (int i = 0; i < c.n; ++i) {
+                    int qb, qe;
+                    int64_t rb, re;
+                    if (seed_sw_window(B, l_query, seeds[R0 + c.seed_off + i], qb, qe, rb, re))
+                        ++nj, nb += (qe - qb) + (re - rb);
+                }
+            }
+        }
+        n_jobs[r] = nj;
+        n_bytes[r] = nb;
+    }
+}
+
+// The jobs (ksw_align2(qe-qb, query+qb, re-rb, rseq, ..., KSW_XSTART, 0)) and their bytes at
+// each read's offsets, in chain and seed order.
+__global__ void seed_sw_fill(DevBns B, int n_reads, const int *__restrict__ min_hsp,
+                             const uint8_t *__restrict__ reads, const int64_t *__restrict__ read_off,
+                             const int64_t *__restrict__ seed_off, const int64_t *__restrict__ row_off_of_seed,
+                             const DevSeed *__restrict__ seeds, const DevChain *__restrict__ chains,
+                             const int *__restrict__ n_chains, const int64_t *__restrict__ job_off,
+                             const int64_t *__restrict__ byte_off, bsb_sw_job_t *__restrict__ jobs,
+                             uint8_t *__restrict__ bytes)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        if (min_hsp[r] < 0) continue;
+        const int64_t R0 = row_off_of_seed[seed_off[r]];
+        const int l_query = (int)(read_off[r + 1] - read_off[r]);
+        const uint8_t *q = reads + read_off[r];
+        int64_t j = job_off[r], b = byte_off[r];
+        for (int ci = 0; ci < n_chains[r]; ++ci) {
+            const DevChain c = chains[R0 + ci];
+            for (int i = 0; i < c.n; ++i) {
+                int qb, qe;
+                int64_t rb, re;
+                if (!seed_sw_window(B, l_query, seeds[R0 + c.seed_off + i], qb, qe, rb, re)) continue;
+                bsb_sw_job_t jb;
+                jb.qoff = b, jb.qlen = qe - qb;
+                for (int x = qb; x < qe; ++x) bytes[b++] = q[x];
+                jb.toff = b, jb.tlen = (int32_t)(re - rb);
+                for (int64_t x = rb; x < re; ++x) bytes[b++] = (uint8_t)text_base(B, x);
+                jb.xtra = 0x80000;                                   // KSW_XSTART
+                jb.pad_ = 0;
+                jobs[j++] = jb;
+            }
+        }
+    }
+}
+
+// The filter itself (bwamem.c:608-617): seeds keep their order, a seed without SW scores
+// len * a, and chains shrink in place.
+__global__ void seed_sw_apply(AlnOpt opt, DevBns B, int n_reads, const int *__restrict__ min_hsp,
+                              const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
+                              const int64_t *__restrict__ row_off_of_seed, DevSeed *__restrict__ seeds,
+                              DevChain *__restrict__ chains, const int *__restrict__ n_chains,
+                              const int64_t *__restrict__ job_off, const int *__restrict__ score)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        const int mh = min_hsp[r];
+        if (mh < 0) continue;
+        const int64_t R0 = row_off_of_seed[seed_off[r]];
+        const int l_query = (int)(read_off[r + 1] - read_off[r]);
+        int64_t j = job_off[r];
+        for (int ci = 0; ci < n_chains[r]; ++ci) {
+            DevChain &c = chains[R0 + ci];
+            DevSeed *cs = seeds + R0 + c.seed_off;
+            int k = 0;
+            for (int i = 0; i < c.n; ++i) {
+                DevSeed sd = cs[i];
+                int qb, qe;
+                int64_t rb, re;
+                const int sc = seed_sw_window(B, l_query, sd, qb, qe, rb, re) ? score[j++] : -1;
+                if (sc < 0 || sc >= mh) {
+                    sd.score = sc < 0 ? sd.len * opt.a : sc;
+                    cs[k++] = sd;
+                }
+            }
+            c.n = k;
+        }
+    }
+}
+
 // The order chain2aln_kernel takes reads in: most chains first (reads are independent, so the
 // order changes no result; it shortens the tail a few repeat-laden reads would otherwise set).
 constexpr int kOrderBins = 64;
@@ -1042,10 +1180,85 @@ struct AlignScratch {
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // dedup: also run mem_sort_dedup_patch per read (the regions mem_align1_core returns).
+// The seed-level Smith-Waterman filter of the batch (mem_flt_chained_seeds) between chain_kernel
+// and chain2aln_kernel, for the reads with h_min_hsp[r] >= 0: jobs and their bytes are built on
+// the device, run through ksw_align2 on the GPU (bsb_align2_run, with staging of its own: d_in
+// and d_out hold the batch meanwhile), and the scores go back to the chains on the device.
+static int seed_sw_filter(bsb_ctx *ctx, const bsb_align_opt_t *o, const DevBns &B, int n_reads,
+                          const int *h_min_hsp, const uint8_t *d_reads, const int64_t *d_read_off,
+                          const int64_t *d_seed_off, const int64_t *roff, DevSeed *cseeds, DevChain *cchains,
+                          const int *n_chains, const AlnOpt &ao)
+{
+    int rc;
+    cudaStream_t st = ctx->stream;
+    const size_t nr = (size_t)n_reads;
+    const size_t head = al(4 * nr) + al(4 * nr) + al(8 * nr) + 2 * al(8 * (nr + 1));
+    if ((rc = bsb_ensure(ctx, &ctx->flt_dev, &ctx->flt_dev_bytes, head + 256, "seed SW filter"))) return rc;
+    char *D = (char *)ctx->flt_dev;
+    int *d_mh = (int *)D, *d_nj = (int *)(D + al(4 * nr));
+    int64_t *d_nb = (int64_t *)(D + 2 * al(4 * nr));
+    int64_t *d_joff = (int64_t *)(D + 2 * al(4 * nr) + al(8 * nr)), *d_boff = d_joff + al(8 * (nr + 1)) / 8;
+    const int grid = (int)std::min<int64_t>((n_reads + 127) / 128, (int64_t)ctx->n_sm * 8);
+    std::vector<int> nj(nr);
+    std::vector<int64_t> nbytes(nr), joff(nr + 1), boff(nr + 1);
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_mh, h_min_hsp, 4 * nr, cudaMemcpyHostToDevice, st), "H2D min_hsp")))
+        return rc;
+    seed_sw_count<<<grid, 128, 0, st>>>(B, n_reads, d_mh, d_read_off, d_seed_off, roff, cseeds, cchains, n_chains,
+                                        d_nj, d_nb);
+    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(nj.data(), d_nj, 4 * nr, cudaMemcpyDeviceToHost, st), "D2H SW jobs")) ||
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(nbytes.data(), d_nb, 8 * nr, cudaMemcpyDeviceToHost, st), "D2H SW bytes")) ||
+        (rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "seed SW count")))
+        return rc;
+    joff[0] = boff[0] = 0;
+    for (size_t r = 0; r < nr; ++r) joff[r + 1] = joff[r] + nj[r], boff[r + 1] = boff[r] + nbytes[r];
+    const int64_t NJ = joff[nr], NB = boff[nr];
+    std::vector<int> score((size_t)NJ + 1);
+    if (NJ > 0) {
+        const size_t need = head + al(sizeof(bsb_sw_job_t) * (size_t)NJ) + al((size_t)NB) + al(4 * (size_t)NJ);
+        if ((rc = bsb_ensure(ctx, &ctx->flt_dev, &ctx->flt_dev_bytes, need + 256, "seed SW filter"))) return rc;
+        D = (char *)ctx->flt_dev;        // (re)allocated: recompute the views
+        d_mh = (int *)D;
+        d_joff = (int64_t *)(D + 2 * al(4 * nr) + al(8 * nr)), d_boff = d_joff + al(8 * (nr + 1)) / 8;
+        bsb_sw_job_t *d_jobs = (bsb_sw_job_t *)(D + head);
+        uint8_t *d_bytes = (uint8_t *)(D + head + al(sizeof(bsb_sw_job_t) * (size_t)NJ));
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_mh, h_min_hsp, 4 * nr, cudaMemcpyHostToDevice, st), "H2D min_hsp")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_joff, joff.data(), 8 * (nr + 1), cudaMemcpyHostToDevice, st), "H2D")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_boff, boff.data(), 8 * (nr + 1), cudaMemcpyHostToDevice, st), "H2D")))
+            return rc;
+        seed_sw_fill<<<grid, 128, 0, st>>>(B, n_reads, d_mh, d_reads, d_read_off, d_seed_off, roff, cseeds, cchains,
+                                           n_chains, d_joff, d_boff, d_jobs, d_bytes);
+        std::vector<bsb_sw_job_t> jobs((size_t)NJ);
+        std::vector<uint8_t> bytes((size_t)NB + 1);
+        std::vector<bsb_kswr_t> res((size_t)NJ);
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(jobs.data(), d_jobs, sizeof(bsb_sw_job_t) * NJ, cudaMemcpyDeviceToHost,
+                                                st), "D2H SW jobs")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(bytes.data(), d_bytes, NB, cudaMemcpyDeviceToHost, st), "D2H SW bytes")) ||
+            (rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "seed SW jobs")))
+            return rc;
+        bsb_ext_param_t p;
+        memset(&p, 0, sizeof p);
+        memcpy(p.mat, o->mat, 25);
+        p.o_del = o->o_del, p.e_del = o->e_del, p.o_ins = o->o_ins, p.e_ins = o->e_ins, p.zdrop = o->zdrop;
+        if ((rc = bsb_align2_run(ctx, &p, jobs.data(), NJ, bytes.data(), NB, res.data(), &ctx->flt_in,
+                                 &ctx->flt_in_bytes, &ctx->flt_out, &ctx->flt_out_bytes)))
+            return rc;
+        for (int64_t i = 0; i < NJ; ++i) score[(size_t)i] = res[(size_t)i].score;
+    }
+    int *d_score = (int *)(D + head + al(sizeof(bsb_sw_job_t) * (size_t)NJ) + al((size_t)NB));
+    if (NJ > 0 &&
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_score, score.data(), 4 * (size_t)NJ, cudaMemcpyHostToDevice, st), "H2D")))
+        return rc;
+    seed_sw_apply<<<grid, 128, 0, st>>>(ao, B, n_reads, d_mh, d_read_off, d_seed_off, roff, cseeds, cchains, n_chains,
+                                        d_joff, d_score);
+    if ((rc = bsb_cuda(ctx, cudaGetLastError(), "seed SW filter"))) return rc;
+    // the host vectors above must outlive the copies that read them
+    return bsb_cuda(ctx, cudaStreamSynchronize(st), "seed SW filter");
+}
+
 static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_reads, const uint8_t *d_reads,
                        const int64_t *d_read_off, const bsb_intv_t *d_seeds, const int64_t *d_seed_off,
                        int64_t n_seeds, int max_len, bool dedup, bsb_reg_t **d_regs_out, int64_t **d_reg_off_out,
-                       int64_t *n_regs_total)
+                       int64_t *n_regs_total, const int *h_min_hsp)
 {
     int rc;
     cudaStream_t st = ctx->stream;
@@ -1126,6 +1339,10 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     P.pack16 = 0;
     chain_kernel<<<ctx->n_sm * 8, 128, 0, st>>>(ao, B, n_reads, d_read_off, (const DevIntv *)d_seeds, d_seed_off, roff,
                                                  pos, chains, nodes, row_chain, iwork, cseeds, cchains, n_chains, ctrl);
+    if (h_min_hsp &&
+        (rc = seed_sw_filter(ctx, o, B, n_reads, h_min_hsp, d_reads, d_read_off, d_seed_off, roff, cseeds, cchains,
+                             n_chains, ao)))
+        return rc;
     int *order = (int *)(A + o_order);
     int *ocnt = (int *)(A + o_order + al(sizeof(int) * (n_reads + 1)));
     {
@@ -1144,8 +1361,11 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     else if (max_len <= 255)
         chain2aln_kernel<8><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
-    else
+    else if (max_len <= 511)
         chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
+                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+    else
+        chain2aln_kernel<32><<<ctx->n_sm * 2, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                              cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
     if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
     const int cgrid = (int)((n_reads + 3) / 4) < ctx->n_sm * 16 ? (int)((n_reads + 3) / 4) : ctx->n_sm * 16;
@@ -1193,20 +1413,21 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
         return 0;
     }
     int max_len = 0;
-    signed char sw_filter[BSB_ALIGN_MAX_LEN + 1];        // per length: -1 not yet known, 0 / 1
-    memset(sw_filter, -1, sizeof sw_filter);
+    // mem_flt_chained_seeds (bwamem.c:602-606): per read length, its min_HSP_score when the
+    // seed-level SW filter runs for that length, else -1 (the reference returns early)
+    int hsp_of_len[BSB_ALIGN_MAX_LEN + 1];
+    for (int l = 0; l <= BSB_ALIGN_MAX_LEN; ++l) {
+        const double min_l = o->min_chain_weight ? 1.1f * o->min_chain_weight : 5.5f * log((double)l);
+        hsp_of_len[l] = l > 0 && !(min_l > 0.05f * l) ? (int)(o->a * min_l + .499) : -1;
+    }
+    std::vector<int> min_hsp((size_t)n_reads);
+    bool any_filter = false;
     for (int r = 0; r < n_reads; ++r) {
         const int64_t l = offs[r + 1] - offs[r];
         if (l < 0) return bsb_fail(ctx, BSB_EINVAL, "read %d: negative length", r);
         if (l > BSB_ALIGN_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld > %d", r, (long long)l, BSB_ALIGN_MAX_LEN);
-        // mem_flt_chained_seeds (bwamem.c:604-606) runs its seed-level SW only past this
-        // point; reads shorter than min_seed_len never have chains (bwamem.c:266)
-        if (sw_filter[l] < 0) {
-            const double min_l = o->min_chain_weight ? 1.1f * o->min_chain_weight : 5.5f * log((double)l);
-            sw_filter[l] = l >= o->min_seed_len && !(min_l > 0.05f * l);
-        }
-        if (sw_filter[l])
-            return bsb_fail(ctx, BSB_ETOOLONG, "read %d: length %lld needs the seed-level SW filter", r, (long long)l);
+        min_hsp[(size_t)r] = hsp_of_len[l];
+        any_filter |= hsp_of_len[l] >= 0;
         if (l > max_len) max_len = (int)l;
     }
     const int64_t total = offs[n_reads] - offs[0];
@@ -1243,7 +1464,7 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
     bsb_reg_t *d_regs = nullptr;
     int64_t *d_reg_off = nullptr, n_regs = 0;
     if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, dedup, &d_regs,
-                                 &d_reg_off, &n_regs)))
+                                 &d_reg_off, &n_regs, any_filter ? min_hsp.data() : nullptr)))
         return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(regs_off, d_reg_off, off_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H offsets")))
         return rc;

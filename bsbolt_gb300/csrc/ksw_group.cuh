@@ -55,6 +55,7 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
                                               int lo, int hi, int *__restrict__ counter,
                                               bsb_ext_out_t *__restrict__ out, int64_t *__restrict__ cells)
 {
+    static_assert(C <= 32, "the non-zero columns of a lane are a 32-bit mask");
     const int lane = threadIdx.x & 31, gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);
     const int e_del = P.e_del, e_ins = P.e_ins;

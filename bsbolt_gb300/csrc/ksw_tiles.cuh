@@ -26,7 +26,7 @@ constexpr KswTile kTileList[] = {
     {32, 5},  {32, 6},  {32, 7},  {32, 8},  {32, 9},  {32, 10}, {32, 11}, {32, 12},    // 41..48
     {32, 13}, {32, 14}, {32, 15}, {32, 16},                                             // 49..52
     {32, 20}, {32, 24}, {32, 28}, {32, 32},                                             // 53..56
-    {4, 20},  {4, 24},  {4, 28},  {4, 32},  {4, 36}};                                   // 57..61
+    {4, 20},  {4, 24},  {4, 28},  {4, 32}};                                             // 57..60
 constexpr int kNumTiles = sizeof(kTileList) / sizeof(kTileList[0]);
 constexpr int kMaxNeed = BSB_TILE_MAP_LEN - 1;    // columns 0..qlen with qlen <= 1023
 constexpr int kKswBlock = 128;                      // threads per block (4 warps)
@@ -34,8 +34,9 @@ constexpr int kKswBlock = 128;                      // threads per block (4 warp
 static_assert(kNumTiles == BSB_NUM_TILES, "tile list and public header disagree");
 static_assert(kNumTiles <= 64, "tile sets are 64-bit masks");
 
-// Shapes with a 16-bit two-columns-per-register kernel: an even C of at most 32 (the
-// row-maximum key and the non-zero-column bits keep a column index in 4 bits per half).
+// Shapes with a 16-bit two-columns-per-register kernel: an even C (every shape has C <= 32:
+// a lane's non-zero columns are one 32-bit mask, and the 16-bit row-maximum key keeps a
+// column index in 4 bits per half).
 constexpr bool tile_has_pack16(int C) { return C % 2 == 0 && C <= 32; }
 
 constexpr int tile_index(int G, int C)

@@ -24,7 +24,6 @@ KswTileLaunch ksw_tiles_g4(int C)
     case 24: return ksw_tile_launch<24, 4>;
     case 28: return ksw_tile_launch<28, 4>;
     case 32: return ksw_tile_launch<32, 4>;
-    case 36: return ksw_tile_launch<36, 4>;
     default: return nullptr;
     }
 }

@@ -293,6 +293,15 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
                                 const uint8_t *seq, int64_t seq_bytes, bsb_kswr_t *out)
 {
     if (!ctx) return BSB_EINVAL;
+    return bsb_align2_run(ctx, p, jobs, n, seq, seq_bytes, out, &ctx->d_in, &ctx->d_in_bytes, &ctx->d_out,
+                          &ctx->d_out_bytes);
+}
+
+int bsb_align2_run(bsb_ctx *ctx, const bsb_ext_param_t *p, const bsb_sw_job_t *jobs, int64_t n, const uint8_t *seq,
+                   int64_t seq_bytes, bsb_kswr_t *out, void **in_buf, size_t *in_bytes, void **out_buf,
+                   size_t *out_bytes)
+{
+    if (!ctx) return BSB_EINVAL;
     if (!p || n < 0 || (n > 0 && (!jobs || !out)) || seq_bytes < 0 || (seq_bytes > 0 && !seq))
         return bsb_fail(ctx, BSB_EINVAL, "NULL argument");
     if (p->e_del < 0 || p->e_ins < 0 || p->o_del < 0 || p->o_ins < 0 || p->o_del > 65535 || p->o_ins > 65535 ||
@@ -397,8 +406,8 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t jb = al(sizeof(bsb_sw_job_t) * (size_t)n), sb = al((size_t)seq_bytes), ob = al(8 * (size_t)n);
     const size_t lb = al(sizeof(int32_t) * (size_t)n);
-    if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, jb + sb + ob + lb + 256, "SW input staging"))) return rc;
-    char *in = (char *)ctx->d_in;
+    if ((rc = bsb_ensure(ctx, in_buf, in_bytes, jb + sb + ob + lb + 256, "SW input staging"))) return rc;
+    char *in = (char *)*in_buf;
     bsb_sw_job_t *d_jobs = (bsb_sw_job_t *)in;
     uint8_t *d_seq = (uint8_t *)(in + jb);
     int64_t *d_boff = (int64_t *)(in + jb + sb);
@@ -413,9 +422,8 @@ extern "C" int bsb_align2_batch(bsb_ctx *ctx, const bsb_ext_param_t *p, const bs
     int *cnt = (int *)(a2 + lb + rb);
     int *ctr8 = cnt + 64, *ctr16 = cnt + 64 + kCtrInts;
     int2 *d_b = (int2 *)(a2 + lb + rb + kCtrBytes);
-    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, sizeof(bsb_kswr_t) * (size_t)n + 256, "SW output")))
-        return rc;
-    bsb_kswr_t *d_out = (bsb_kswr_t *)ctx->d_out;
+    if ((rc = bsb_ensure(ctx, out_buf, out_bytes, sizeof(bsb_kswr_t) * (size_t)n + 256, "SW output"))) return rc;
+    bsb_kswr_t *d_out = (bsb_kswr_t *)*out_buf;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_jobs, jobs, sizeof(bsb_sw_job_t) * n, cudaMemcpyHostToDevice, st),
                        "H2D jobs")) ||
         (seq_bytes && (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_seq, seq, seq_bytes, cudaMemcpyHostToDevice, st), "H2D seq"))) ||

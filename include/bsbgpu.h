@@ -113,7 +113,7 @@ float bsb_last_kernel_ms(const bsb_ctx *ctx);
  * query length.  The shape changes the time, never a result.  The library
  * ships a default map measured on GB300; an autotuner (bsbolt_gb300.autotune)
  * can measure the shapes on the caller's own jobs and install its map. */
-#define BSB_NUM_TILES 62
+#define BSB_NUM_TILES 61
 #define BSB_TILE_MAP_LEN 1025    /* entry [qlen + 1] for qlen = 0..1023; [0] unused */
 
 /* Fills G[t], C[t] for the compiled shapes t < min(max, BSB_NUM_TILES);
@@ -252,7 +252,7 @@ typedef struct {
  * mem_chain2aln with its ksw_extend2 calls.  Reads are nt4 codes (already
  * converted, as mem_align1_core sees them); read r's regions, in the
  * reference's order, are regs[regs_off[r] .. regs_off[r+1]).  Needs an index
- * with pac and contig table.  Supports reads up to 512 bp whose length keeps
+ * with pac and contig table.  Supports reads up to 1023 bp whose length keeps
  * mem_flt_chained_seeds a no-op (bwamem.c:606), indexes without ALT contigs
  * (BSBolt writes none).  Host buffers; synchronous.  When the batch has more
  * regions than max_regs (mem_chain samples up to max_occ rows per seed, so a

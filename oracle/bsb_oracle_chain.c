@@ -6,7 +6,8 @@
  *   mem_chain + test_and_merge   bwamem.c:203-319 (the kbtree of chains, kbtree.h)
  *   mem_chain_weight             bwamem.c:229-250
  *   mem_chain_flt                bwamem.c:331-389 (ks_introsort, ksort.h:146-226)
- *   mem_flt_chained_seeds        bwamem.c:602-619 (only its early return is supported)
+ *   mem_flt_chained_seeds        bwamem.c:602-619 (with mem_seed_sw, bwamem.c:574-598, on the
+ *                                ksw_align2 restatement of bsb_oracle_sw.c)
  *   cal_max_gap, mem_chain2aln   bwamem.c:625-790
  *   bns_pos2rid, bns_intv2rid    bntseq.c:364-394
  * Parity is pinned against the reference's own chains and regions
@@ -18,6 +19,7 @@
 
 #include "bsb_oracle.h"
 #include "bsb_oracle_chain.h"
+#include "bsb_oracle_sw.h"
 
 /* ------------------------------------------------------------- bns lookups */
 
@@ -486,6 +488,72 @@ int orc_seed_sw_filter_applies(const orc_opt_t *opt, int l_query)
     return !(min_l > 0.05f * l_query);
 }
 
+/* mem_seed_sw (bwamem.c:574-598): the best local score of the seed's neighbourhood, 50 bases
+ * each side, or -1 when the seed or the window is long enough to need none. */
+static int orc_mem_seed_sw(const orc_opt_t *opt, const orc_bns_t *bns, int l_query, const uint8_t *query,
+                           const orc_seed_t *s)
+{
+    int qb, qe, is_rev, rid, score;
+    int64_t rb, re, mid, l_pac = bns->l_pac, far_beg, far_end, k;
+    uint8_t *rseq;
+    orc_kswr_t x;
+    if (s->len >= 200) return -1;                               /* MEM_SHORT_LEN */
+    qb = s->qbeg, qe = s->qbeg + s->len;
+    rb = s->rbeg, re = s->rbeg + s->len;
+    mid = (rb + re) >> 1;
+    qb -= 50; qb = qb > 0 ? qb : 0;                             /* MEM_SHORT_EXT */
+    qe += 50; qe = qe < l_query ? qe : l_query;
+    rb -= 50; rb = rb > 0 ? rb : 0;
+    re += 50; re = re < l_pac << 1 ? re : l_pac << 1;
+    if (rb < l_pac && l_pac < re) {
+        if (mid < l_pac) re = l_pac;
+        else rb = l_pac;
+    }
+    if (qe - qb >= 200 || re - rb >= 200) return -1;
+    /* bns_fetch_seq (bntseq.c:436-461): the window clipped to the contig of its middle */
+    rid = pos2rid(bns, depos(bns, mid, &is_rev));
+    far_beg = bns->anns[rid].offset;
+    far_end = far_beg + bns->anns[rid].len;
+    if (is_rev) {
+        int64_t t = far_beg;
+        far_beg = (l_pac << 1) - far_end;
+        far_end = (l_pac << 1) - t;
+    }
+    rb = rb > far_beg ? rb : far_beg;
+    re = re < far_end ? re : far_end;
+    rseq = (uint8_t *)malloc((size_t)(re - rb) + 1);
+    for (k = rb; k < re; ++k) rseq[k - rb] = (uint8_t)text_base(bns, k);
+    x = orc_ksw_align2(qe - qb, query + qb, (int)(re - rb), rseq, opt->mat, opt->o_del, opt->e_del, opt->o_ins,
+                       opt->e_ins, ORC_KSW_XSTART);
+    score = x.score;
+    free(rseq);
+    return score;
+}
+
+/* mem_flt_chained_seeds (bwamem.c:602-619): each chain keeps, in order, the seeds whose
+ * neighbourhood scores at least min_HSP_score or that need no SW, rescored; a no-op for
+ * read lengths where the reference returns early. */
+void orc_flt_chained_seeds(const orc_opt_t *opt, const orc_bns_t *bns, int l_query, const uint8_t *query,
+                           int n_chn, orc_chain_t *a, orc_seed_t *seeds)
+{
+    double min_l = opt->min_chain_weight ? 1.1f * opt->min_chain_weight : 5.5f * log(l_query);
+    int i, j, k, min_HSP_score = (int)(opt->a * min_l + .499);
+    if (min_l > 0.05f * l_query) return;
+    for (i = 0; i < n_chn; ++i) {
+        orc_chain_t *c = &a[i];
+        orc_seed_t *cs = seeds + c->seed_off;
+        for (j = k = 0; j < c->n; ++j) {
+            orc_seed_t sd = cs[j];
+            sd.score = orc_mem_seed_sw(opt, bns, l_query, query, &sd);
+            if (sd.score < 0 || sd.score >= min_HSP_score) {
+                sd.score = sd.score < 0 ? sd.len * opt->a : sd.score;
+                cs[k++] = sd;
+            }
+        }
+        c->n = k;
+    }
+}
+
 /* cal_max_gap (bwamem.c:625-632) */
 static inline int cal_max_gap(const orc_opt_t *opt, int qlen)
 {
@@ -693,7 +761,9 @@ static void align_one(const orc_bwt_t *bwt, const orc_bns_t *bns, const orc_opt_
     rr->c1 = (orc_chain_t *)malloc(sizeof(orc_chain_t) * (rr->n0 ? rr->n0 : 1));
     memcpy(rr->c1, rr->c0, sizeof(orc_chain_t) * rr->n0);
     rr->n1 = orc_mem_chain_flt(opt, rr->n0, rr->c1, rr->s0);
-    if (rr->n1 > 0 && orc_seed_sw_filter_applies(opt, len)) { rr->err = -3; return; }
+    /* the filter rewrites the kept chains' seeds in place: the pre-filter chain list (c0)
+     * shares those seed ranges and is reported only for reads the filter leaves alone */
+    if (rr->n1 > 0) orc_flt_chained_seeds(opt, bns, len, q, rr->n1, rr->c1, rr->s0);
     max_regs = rr->ns + 1;
     rr->r = (orc_reg_t *)malloc(sizeof(orc_reg_t) * max_regs);
     for (i = 0; i < rr->n1; ++i)

@@ -53,6 +53,8 @@ int orc_mem_chain(const orc_bwt_t *bwt, const orc_bns_t *bns, const orc_opt_t *o
                   const orc_intv_t *mem, int n_mem, orc_chain_t **chains, orc_seed_t **seeds, int *n_seeds);
 int orc_mem_chain_flt(const orc_opt_t *opt, int n_chn, orc_chain_t *a, const orc_seed_t *seeds);
 int orc_seed_sw_filter_applies(const orc_opt_t *opt, int l_query);
+void orc_flt_chained_seeds(const orc_opt_t *opt, const orc_bns_t *bns, int l_query, const uint8_t *query,
+                           int n_chn, orc_chain_t *a, orc_seed_t *seeds);
 int orc_mem_chain2aln(const orc_opt_t *opt, const orc_bns_t *bns, int l_query, const uint8_t *query,
                       const orc_chain_t *c, const orc_seed_t *seeds, orc_reg_t *regs, int *n_regs, int max_regs,
                       int64_t *cells);

@@ -58,6 +58,26 @@ def pe_set(d, bwa):
     return fa, os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq"), os.path.join(d, "u1.fq"), os.path.join(d, "u2.fq")
 
 
+def long_set(d, bwa):
+    """Reads the seed-level Smith-Waterman filter runs on (mem_flt_chained_seeds,
+    bwamem.c:602-619): single-end reads of 513-1023 bases on the pe_set reference (at 5.5*ln(L)
+    <= 0.05*L, i.e. from ~724 bases, the filter runs with -W 0), and 2 x 150 pairs for runs with
+    -W (min_chain_weight), where it runs from 22*W bases.  Returns (fa, long.fq, p1.fq, p2.fq);
+    pe_set must have been built in d."""
+    contigs = synth.bs_genome(3, 200_000, seed=4242)
+    contigs[1][1][50_000:55_000] = contigs[0][1][10_000:15_000]
+    fa = os.path.join(d, "ref.fa")
+    reads = []
+    for k, L in enumerate((513, 600, 723, 724, 760, 900, 1023)):
+        r1, _ = synth.bs_reads_pe(contigs, 60, L, L + 200, 20, seed=4260 + k)
+        reads += r1
+    write_fastq(os.path.join(d, "long.fq"), reads, 1)
+    p1, p2 = synth.bs_reads_pe(contigs, 1500, 150, 400, 40, seed=4270)
+    write_fastq(os.path.join(d, "p150_1.fq"), p1, 1)
+    write_fastq(os.path.join(d, "p150_2.fq"), p2, 2)
+    return fa, os.path.join(d, "long.fq"), os.path.join(d, "p150_1.fq"), os.path.join(d, "p150_2.fq")
+
+
 def repeat_set(d, bwa, copies=700, n_pairs=40):
     """2 x 300 kb reference holding `copies` exact copies of one 300-base element, and read
     pairs from inside copies: every seed has more rows than max_occ (500), mem_chain samples

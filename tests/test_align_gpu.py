@@ -91,11 +91,54 @@ def test_regions_random_reads_vs_oracle(gpu_ctx, indexes, lmin, lmax):
         assert np.array_equal(regs[f], ref["regs"][f]), f"reg.{f}"
 
 
-def test_align_rejects_long_reads(gpu_ctx, indexes):
+def test_align_rejects_reads_over_1023(gpu_ctx, indexes):
     seed.load_index(gpu_ctx, indexes["plain"])
     with pytest.raises(_lib.BsbError) as e:
-        seed.align_regs(gpu_ctx, np.zeros(600, np.uint8), np.array([0, 600]))
+        seed.align_regs(gpu_ctx, np.zeros(1024, np.uint8), np.array([0, 1024]))
     assert e.value.code == _lib.BSB_ETOOLONG
+
+
+@pytest.mark.parametrize("mcw,lmin,lmax,n", [(0, 513, 1023, 600), (5, 100, 300, 1500), (0, 700, 760, 400)],
+                         ids=["long-reads", "W5", "filter-threshold"])
+def test_long_reads_and_seed_sw_filter_vs_oracle(gpu_ctx, indexes, mcw, lmin, lmax, n):
+    """Reads up to 1023 bases (the 32-column chain-extension width) and the seed-level
+    Smith-Waterman filter of mem_flt_chained_seeds (bwamem.c:602-619): it runs where
+    5.5*ln(L) <= 0.05*L (from ~724 bases) with -W 0, and from 22*W bases with -W W.  Regions
+    before and after mem_sort_dedup_patch against the oracle."""
+    prefix = indexes["rep"]
+    seed.load_index(gpu_ctx, prefix)
+    bi = index.BwaIndex(prefix)
+    pac = bi.pac_codes()
+    rng = np.random.Generator(np.random.PCG64(29 + mcw + lmin))
+    reads = []
+    for k in range(n):
+        L = int(rng.integers(lmin, lmax + 1))
+        st = int(rng.integers(0, len(pac) - L - 1))
+        r = pac[st:st + L].copy()
+        if k % 2:
+            r = (3 - r[::-1]).astype(np.uint8)
+        e = rng.random(L) < (0.03 if k % 3 else 0.12)          # some reads with weak seeds
+        r[e] = rng.integers(0, 5, int(e.sum()))
+        reads.append(r.astype(np.uint8))
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    seqs = np.concatenate(reads)
+    opt = _lib.AlignOpt.bwa_defaults()
+    opt.min_chain_weight = mcw
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    oo = oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000])
+    oo.min_chain_weight = mcw
+    ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oo, seqs, offs, n_threads=8)
+    regs, off = seed.align_regs(gpu_ctx, seqs, offs, opt)
+    assert np.array_equal(off, ref["regs_off"])
+    for f in REG_FIELDS + ["frac_rep"]:
+        assert np.array_equal(regs[f], ref["regs"][f]), f"reg.{f}"
+    dregs, doff = seed.align_regs(gpu_ctx, seqs, offs, opt, dedup=True)
+    dref, dref_off = oracle.sort_dedup_batch(oo, bi.l_pac, bi.pac, seqs, offs, ref["regs"], ref["regs_off"])
+    assert np.array_equal(doff, dref_off)
+    for f in dref.dtype.names:
+        assert np.array_equal(dregs[f], dref[f]), f"dedup.{f}"
 
 
 @pytest.mark.parametrize("fn,tag", GOLDEN_SETS)

@@ -156,3 +156,16 @@ def test_glue_repeat_family_over_max_occ(tmp_path):
     assert len(ref) >= 80 and run_mem(GLUE, fa, r1, r2, extra) == ref
     st = sam_sets.run_stats(GLUE, fa, [r1, r2], extra, "BSB_SHIM_STATS", "[bsb_glue]")
     assert st["regrown"] >= 1, st
+
+
+def test_glue_long_reads_and_seed_sw_filter(pe):
+    """Reads of 513-1023 bases (the seed-level SW filter of mem_flt_chained_seeds runs from ~724)
+    and 2 x 150 pairs under -W 5 (the filter runs on every read): the glue's regions and the
+    reference's SAM agree."""
+    fa, lf, p1, p2 = sam_sets.long_set(os.path.dirname(pe[0]), BWA)
+    for extra in (["-L", "5,5"], sam_sets.BSBOLT_ARGS):
+        ref = sam_sets.run_mem(BWA, fa, [lf], extra)
+        assert len(ref) >= 420 and sam_sets.run_mem(GLUE, fa, [lf], extra) == ref
+    extra = ["-W", "5", "-L", "5,5"]
+    ref = run_mem(BWA, fa, p1, p2, extra)
+    assert len(ref) >= 3000 and run_mem(GLUE, fa, p1, p2, extra) == ref

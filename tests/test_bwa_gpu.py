@@ -91,3 +91,12 @@ def test_gpu_repeat_family_over_max_occ(tmp_path):
     same(fa, [r1, r2], sam_sets.BSBOLT_ARGS, 80)
     st = sam_sets.run_stats(GPU, fa, [r1, r2], ["-L", "5,5"], "BSB_GPU_STATS", "[bsb_gpu]")
     assert st["regrown"] >= 1, st
+
+
+def test_gpu_long_reads_and_seed_sw_filter(pe):
+    """Reads of 513-1023 bases and 2 x 150 pairs under -W 5: the seed-level Smith-Waterman
+    filter (mem_flt_chained_seeds) runs on the GPU and the SAM is the reference's."""
+    fa, lf, p1, p2 = sam_sets.long_set(os.path.dirname(pe[0]), BWA)
+    same(fa, [lf], ["-L", "5,5"], 420)
+    same(fa, [lf], sam_sets.BSBOLT_ARGS, 420)
+    same(fa, [p1, p2], ["-W", "5", "-L", "5,5"], 3000)
