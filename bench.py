@@ -658,6 +658,76 @@ def sam_block(n_pairs_100mb=500_000, n_rrbs=1_000_000, threads=None):
     return res
 
 
+def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
+    """The learned read order of the alignment batches against the plain (chain-count) order on
+    the RRBS-like workload: per-read features and DP cells logged by the library from the first
+    batches train the 2x64 cost model on the GPU (bsb_mlp_* kernels); then every batch runs with
+    each order through bsb_mem_align1_batch (host buffers), regions compared."""
+    import torch
+    from bsbolt_gb300 import _lib, cost_model as cm, seed
+    prefix, reads, offs = rrbs_workload()
+    n_reads = len(offs) - 1
+    seed.load_index(ctx, prefix)
+    opt = _lib.AlignOpt.bwa_defaults()
+    batches, lo = [], 0
+    while lo < n_reads:
+        hi = int(np.searchsorted(offs, offs[lo] + batch_bases, side="left"))
+        hi = max(lo + 1, min(hi, n_reads))
+        batches.append((lo, hi))
+        lo = hi
+
+    def sub(a, b):
+        return reads[offs[a]:offs[b]], offs[a:b + 1] - offs[a]
+    # training logs: the first batches; evaluation logs: the last one
+    seed.read_cost_log(ctx, True)
+    feats, cells = [], []
+    for a, b in batches[:train_batches] + [batches[-1]]:
+        seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        f, c = seed.last_read_costs(ctx, b - a)
+        feats.append(f)
+        cells.append(c)
+    seed.read_cost_log(ctx, False)
+    ftr, ctr = np.concatenate(feats[:-1]), np.concatenate(cells[:-1])
+    fev, cev = feats[-1], cells[-1]
+    t0 = time.perf_counter()
+    model = cm.CostModel(ctx, seed=5)
+    losses = model.train(torch.from_numpy(ftr).cuda(), torch.from_numpy(np.log1p(ctr).astype(np.float32)).cuda(),
+                         epochs=8)
+    train_s = time.perf_counter() - t0
+    pred = model.forward(torch.from_numpy(fev).cuda()).cpu().numpy()
+
+    def run_all():
+        out = []
+        t = time.perf_counter()
+        for a, b in batches:
+            out.append(seed.align_regs(ctx, *sub(a, b), opt, dedup=True))
+        return time.perf_counter() - t, out
+    run_all()                                      # warm-up
+    plain_s, plain_out = run_all()
+    seed.set_read_cost_model(ctx, model)
+    try:
+        run_all()
+        learned_s, learned_out = run_all()
+    finally:
+        seed.set_read_cost_model(ctx, None)
+    same = all(np.array_equal(x[1], y[1]) and np.array_equal(x[0], y[0]) for x, y in zip(plain_out, learned_out))
+    # the plain order's key: chains per read (feature 1 is log1p(kept chains) / 4)
+    plain_key = np.expm1(fev[:, 1] * 4)
+    return {
+        "workload": f"RRBS-like, {n_reads} reads in {len(batches)} -K 10M batches (bsb_mem_align1_batch, host buffers)",
+        "model": "2x64 MLP, BF16 weights, FP32 accumulation, per-read features (read length, kept chains, their "
+                 "seeds, best chain weight, mean seed offset, reverse-strand share, C+G content, plain bound)",
+        "trained_on": f"{len(ftr)} reads of the first {train_batches} batches, target log1p(DP cells) logged by "
+                      "chain2aln_kernel", "train_s": round(train_s, 2),
+        "train_loss_per_epoch": [round(x, 4) for x in losses],
+        "spearman_model_eval_batch": round(cm.spearman(pred, cev), 4),
+        "spearman_chain_count_eval_batch": round(cm.spearman(plain_key, cev), 4),
+        "plain_reads_per_s": round(n_reads / plain_s, 1), "learned_reads_per_s": round(n_reads / learned_s, 1),
+        "plain_s": round(plain_s, 4), "learned_s": round(learned_s, 4),
+        "speedup_learned_vs_plain": round(plain_s / learned_s, 4), "regions_identical": bool(same),
+    }
+
+
 def pipeline_secondary(ctx, steps, rank):
     """Seeds -> chains -> regions on the 2 Mb-reference workload, GPU vs the CPU oracle."""
     import oracle
@@ -1035,6 +1105,13 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             rrbs = {"error": f"{type(e).__name__}: {e}"}
 
+    lp = None
+    if rank == 0 and not args.no_learned and not args.no_ref100mb:
+        try:
+            lp = learned_pipeline(ctx)
+        except Exception as e:   # reported, never hidden
+            lp = {"error": f"{type(e).__name__}: {e}"}
+
     tuned = None
     if rank == 0 and not args.no_autotune:
         try:
@@ -1108,6 +1185,7 @@ def run_ours(args, ws, rank, local):
             "clocks": clocks,
             "pipeline": secondary,
             "learned_schedule": learned,
+            "learned_read_order_rrbs": lp,
             "autotune": tuned,
             "pipeline_100mb_ref": big,
             "pipeline_rrbs_100mb_ref": rrbs,

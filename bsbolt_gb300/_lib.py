@@ -172,6 +172,12 @@ def load(path: str = LIB_PATH):
     L.bsb_align2_batch.argtypes = [P, P, P, I64, P, I64, P]
     L.bsb_last_seed_extensions.argtypes = [P, ctypes.POINTER(I64)]
     L.bsb_last_seed_extensions.restype = I32
+    L.bsb_read_cost_log.argtypes = [P, I32]
+    L.bsb_read_cost_log.restype = I32
+    L.bsb_last_read_costs.argtypes = [P, ctypes.c_int32, P, P]
+    L.bsb_last_read_costs.restype = I32
+    L.bsb_set_read_cost_model.argtypes = [P, P]
+    L.bsb_set_read_cost_model.restype = I32
     L.bsb_align2_batch.restype = I32
     _lib = L
     return L

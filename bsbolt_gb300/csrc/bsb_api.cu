@@ -128,6 +128,7 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
     if (ctx->flt_in) cudaFree(ctx->flt_in);
     if (ctx->flt_out) cudaFree(ctx->flt_out);
     if (ctx->flt_dev) cudaFree(ctx->flt_dev);
+    if (ctx->rc_buf) cudaFree(ctx->rc_buf);
     if (ctx->d_tile_map) cudaFree(ctx->d_tile_map);
     bsb_index_release(ctx);
     for (cudaStream_t s : {ctx->h2d, ctx->d2h, ctx->ms.aux[0], ctx->ms.aux[1], ctx->ms.aux[2]})

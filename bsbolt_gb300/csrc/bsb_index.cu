@@ -31,6 +31,8 @@ cudaError_t sa_full_build(const DevFM &F, int64_t n_sa, uint64_t *full, int *fai
 void bsb_index_release(bsb_ctx *ctx)
 {
     if (ctx->idx_bwt) cudaFree(ctx->idx_bwt);
+    if (ctx->idx_sb) cudaFree(ctx->idx_sb);
+    ctx->idx_sb = nullptr;
     if (ctx->idx_sa) cudaFree(ctx->idx_sa);
     if (ctx->idx_pac) cudaFree(ctx->idx_pac);
     if (ctx->idx_sa_full) cudaFree(ctx->idx_sa_full);
@@ -48,6 +50,8 @@ static DevFM dev_fm(const bsb_ctx *ctx)
 {
     DevFM F;
     F.blk = (const uint4 *)ctx->idx_bwt;
+    F.sb = (const uint64_t *)ctx->idx_sb;
+    F.sym64 = ctx->idx_sym64;
     F.sa = (const uint64_t *)ctx->idx_sa;
     F.sa_full = (const uint64_t *)ctx->idx_sa_full;
     F.primary = ctx->primary;
@@ -117,6 +121,34 @@ __global__ void occ_sectors_kernel(const uint32_t *__restrict__ ref, uint64_t n_
     out[2 * s + 1] = make_uint4((uint32_t)cg, (uint32_t)(cg >> 32), b[8 + 2 * q], b[9 + 2 * q]);
 }
 
+// The same re-cut into 64-symbol sectors: counts relative to the sector's 2^32-row
+// superblock (whose block starts at word ((s >> 26) << 25) * 16), four symbol words.
+__global__ void occ_sectors64_kernel(const uint32_t *__restrict__ ref, uint64_t n_sectors, uint4 *__restrict__ out)
+{
+    const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (s >= n_sectors) return;
+    const uint32_t *b = ref + (s >> 1) * 16;
+    const uint32_t *sbk = ref + ((s >> 26) << 25) * 16;
+    const int h = (int)(s & 1);
+    uint32_t a = 0, c = 0, g = 0;
+    for (int w = 0; w < 4 * h; ++w) word_counts(b[8 + w], 16, a, c, g);
+    const uint64_t ca = ((uint64_t)b[1] << 32 | b[0]) + a - ((uint64_t)sbk[1] << 32 | sbk[0]);
+    const uint64_t cc = ((uint64_t)b[3] << 32 | b[2]) + c - ((uint64_t)sbk[3] << 32 | sbk[2]);
+    const uint64_t cg = ((uint64_t)b[5] << 32 | b[4]) + g - ((uint64_t)sbk[5] << 32 | sbk[4]);
+    out[2 * s] = make_uint4((uint32_t)ca, (uint32_t)cc, (uint32_t)cg, 0u);
+    out[2 * s + 1] = make_uint4(b[8 + 4 * h], b[9 + 4 * h], b[10 + 4 * h], b[11 + 4 * h]);
+}
+
+// Occurrence layout for an index of seq_len rows: 64-symbol sectors once the 32-symbol
+// array (one byte per row) would take more than half of L2, where its misses start to set
+// the seeding time; BSB_OCC_SYM64=0/1 forces one layout (measurements, tests).
+static int occ_layout_sym64(uint64_t seq_len)
+{
+    const char *e = getenv("BSB_OCC_SYM64");
+    if (e && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
+    return seq_len > (64ull << 20);
+}
+
 extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
 {
     if (!ctx) return BSB_EINVAL;
@@ -135,20 +167,40 @@ extern "C" int bsb_index_upload(bsb_ctx *ctx, const bsb_index_view_t *v)
     bsb_index_release(ctx);
     {
         // the reference blocks go to a zero-padded staging buffer of whole blocks, then are re-cut
-        // into sectors (four per block, one extra block of padding past the last symbol)
+        // into sectors (four or two per block, one extra block of padding past the last symbol)
         const size_t ref_bytes = n_blocks * 64, copy = std::min<size_t>(v->bwt_size * 4, ref_bytes);
-        const uint64_t n_sectors = n_blocks * 4;
+        const int sym64 = occ_layout_sym64(seq_len);
+        const uint64_t n_sectors = n_blocks * (sym64 ? 2 : 4);
         void *stage = nullptr;
         if ((rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_bwt, n_sectors * 32), "index: occurrence array"))) return rc;
         if ((rc = bsb_cuda(ctx, cudaMalloc(&stage, ref_bytes), "index: occurrence staging"))) return rc;
         rc = bsb_cuda(ctx, cudaMemsetAsync(stage, 0, ref_bytes, ctx->stream), "index memset");
         if (!rc) rc = bsb_cuda(ctx, cudaMemcpyAsync(stage, v->bwt, copy, cudaMemcpyHostToDevice, ctx->stream),
                                "index: occurrence upload");
+        if (!rc && sym64) {
+            // the A, C, G counts before each 2^32-row superblock: the header of its first block
+            const uint64_t n_sb = (seq_len >> 32) + 1;
+            std::vector<uint64_t> sb(3 * n_sb, 0);
+            for (uint64_t k = 1; k < n_sb; ++k) {
+                const uint64_t w = (k << 25) * 16;
+                if (w + 6 > (uint64_t)v->bwt_size) break;
+                for (int c = 0; c < 3; ++c) sb[3 * k + c] = (uint64_t)v->bwt[w + 2 * c + 1] << 32 | v->bwt[w + 2 * c];
+            }
+            rc = bsb_cuda(ctx, cudaMalloc(&ctx->idx_sb, sb.size() * 8), "index: superblock counts");
+            if (!rc) rc = bsb_cuda(ctx, cudaMemcpyAsync(ctx->idx_sb, sb.data(), sb.size() * 8, cudaMemcpyHostToDevice,
+                                                        ctx->stream), "index: superblock counts");
+            if (!rc) rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "index: superblock counts");
+        }
         if (!rc) {
-            occ_sectors_kernel<<<(unsigned)((n_sectors + 255) / 256), 256, 0, ctx->stream>>>(
-                (const uint32_t *)stage, n_sectors, (uint4 *)ctx->idx_bwt);
+            if (sym64)
+                occ_sectors64_kernel<<<(unsigned)((n_sectors + 255) / 256), 256, 0, ctx->stream>>>(
+                    (const uint32_t *)stage, n_sectors, (uint4 *)ctx->idx_bwt);
+            else
+                occ_sectors_kernel<<<(unsigned)((n_sectors + 255) / 256), 256, 0, ctx->stream>>>(
+                    (const uint32_t *)stage, n_sectors, (uint4 *)ctx->idx_bwt);
             rc = bsb_cuda(ctx, cudaGetLastError(), "index: occurrence sectors");
         }
+        ctx->idx_sym64 = sym64;
         if (!rc) rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "index: occurrence sectors");
         cudaFree(stage);
         if (rc) return rc;

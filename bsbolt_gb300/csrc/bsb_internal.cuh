@@ -47,6 +47,8 @@ struct bsb_ctx {
     // device-resident FM-index (reference layout) and its scalars
     int has_index = 0;
     void *idx_bwt = nullptr, *idx_sa = nullptr, *idx_pac = nullptr;
+    void *idx_sb = nullptr;       // superblock counts of the 64-symbol occurrence layout
+    int idx_sym64 = 0;            // occurrence layout: 1 = 64 symbols per sector, 0 = 32
     void *idx_sa_full = nullptr;  // every row's SA value (built at upload when it fits), or NULL
     void *idx_opac = nullptr;     // original (unconverted) reference, 2-bit, for the methylation calls
     uint64_t primary = 0, seq_len = 0, n_sa = 0;
@@ -83,6 +85,13 @@ struct bsb_ctx {
     // batch's own reads and seeds occupy d_in / d_out meanwhile)
     void *flt_in = nullptr, *flt_out = nullptr, *flt_dev = nullptr;
     size_t flt_in_bytes = 0, flt_out_bytes = 0, flt_dev_bytes = 0;
+    // learned read order of the alignment batches: the cost model (caller's device memory,
+    // or NULL for the chain-count order), and the per-read features and extension cells of
+    // the last batch when logging
+    const void *read_model = nullptr;
+    int read_log = 0, rc_n = 0;
+    void *rc_buf = nullptr;
+    size_t rc_bytes = 0;
 };
 
 // bsb_align2_batch with explicit device staging buffers (grown as needed) in place of the

@@ -591,7 +591,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                  const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
                  const DevChain *__restrict__ chains, const int *__restrict__ n_chains, uint64_t *__restrict__ srt_buf,
                  bsb_reg_t *__restrict__ regs, int *__restrict__ n_regs, int *__restrict__ next,
-                 const int *__restrict__ order)
+                 const int *__restrict__ order, int64_t *__restrict__ read_cells)
 {
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -609,6 +609,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
         bsb_reg_t *av = regs + R0;
         uint64_t *srt = srt_buf + R0;
         int nav = 0;
+        long long cells = 0;           // DP cells of the read's ksw_extend2 calls, band retries included
         const int64_t l_pac = B.l_pac;
         for (int ci = 0; ci < nc; ++ci) {
             const DevChain c = chn[ci];
@@ -718,6 +719,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                         const int prev = a.score;
                         aw0 = opt.w << i;
                         x = extend_any<MaxC>(P, s.qbeg, tlen, s.len * opt.a, aw0, opt.pen_clip5, acc, lane);
+                        cells += x.cells;
                         a.score = x.score;
                         if (a.score == prev || x.max_off < (aw0 >> 1) + (aw0 >> 2)) break;
                     }
@@ -739,6 +741,7 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                         const int prev = a.score;
                         aw1 = opt.w << i;
                         x = extend_any<MaxC>(P, l_query - qe, tlen, sc0, aw1, opt.pen_clip3, acc, lane);
+                        cells += x.cells;
                         a.score = x.score;
                         if (a.score == prev || x.max_off < (aw1 >> 1) + (aw1 >> 2)) break;
                     }
@@ -764,7 +767,10 @@ chain2aln_kernel(AlnOpt opt, KswParams P, DevBns B, int n_reads, const uint8_t *
                 __syncwarp();
             }
         }
-        if (lane == 0) n_regs[r] = nav;
+        if (lane == 0) {
+            n_regs[r] = nav;
+            if (read_cells) read_cells[r] = cells;
+        }
     }
 }
 
@@ -902,6 +908,85 @@ __global__ void seed_sw_apply(AlnOpt opt, DevBns B, int n_reads, const int *__re
             }
             c.n = k;
         }
+    }
+}
+
+// ---------------------------------------------------------------- learned read order
+
+// Eight features per read for the learned extension-cost model (no reference counterpart:
+// they only order the read queue of chain2aln_kernel), from the kept chains after the seed
+// filter -- the inputs mem_chain2aln works from (bwamem.c:636-790):
+//   f0 read length / 256          f1 log1p(kept chains) / 4     f2 log1p(their seeds) / 6
+//   f3 best chain weight / length f4 mean seed offset / length  f5 chains on the reverse half
+//   f6 C+G fraction of the read   f7 log2(1 + plain bound of the extension cells) / 24
+// where the plain bound sums, over the seeds, the bases left and right of the seed times the
+// band they are extended in (2w + 1).
+__global__ void read_features_kernel(AlnOpt opt, DevBns B, int n_reads, const uint8_t *__restrict__ reads,
+                                     const int64_t *__restrict__ read_off, const int64_t *__restrict__ seed_off,
+                                     const int64_t *__restrict__ row_off_of_seed, const DevSeed *__restrict__ seeds,
+                                     const DevChain *__restrict__ chains, const int *__restrict__ n_chains,
+                                     float *__restrict__ feat)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        const int L = (int)(read_off[r + 1] - read_off[r]);
+        const uint8_t *q = reads + read_off[r];
+        const int64_t R0 = row_off_of_seed[seed_off[r]];
+        int ns = 0, wmax = 0, nrev = 0, kept = 0, cg = 0;
+        double qsum = 0., bound = 0.;
+        for (int ci = 0; ci < n_chains[r]; ++ci) {
+            const DevChain c = chains[R0 + ci];
+            if (c.n == 0) continue;
+            ++kept;
+            wmax = c.w > wmax ? c.w : wmax;
+            for (int i = 0; i < c.n; ++i) {
+                const DevSeed sd = seeds[R0 + c.seed_off + i];
+                ++ns;
+                qsum += sd.qbeg;
+                bound += (double)(L - sd.len) * (2 * opt.w + 1);
+                nrev += sd.rbeg >= B.l_pac;
+            }
+        }
+        for (int i = 0; i < L; ++i) cg += q[i] == 1 || q[i] == 2;
+        float *f = feat + (int64_t)r * 8;
+        const float l = L > 0 ? (float)L : 1.f;
+        f[0] = L / 256.f;
+        f[1] = log1pf((float)kept) / 4.f;
+        f[2] = log1pf((float)ns) / 6.f;
+        f[3] = wmax / l;
+        f[4] = ns ? (float)(qsum / ns) / l : 0.f;
+        f[5] = ns ? (float)nrev / ns : 0.f;
+        f[6] = cg / l;
+        f[7] = (float)(log2(1.0 + bound) / 24.0);
+    }
+}
+
+// The learned order: reads by predicted cost, most expensive first, in 64 bins of half an
+// octave of the predicted cells (key).
+__device__ __forceinline__ int key_bin(int32_t key)
+{
+    if (key <= 0) return 63;
+    const uint32_t k = (uint32_t)key;
+    const int msb = 31 - __clz(k);
+    const int half = 2 * msb + (msb > 0 ? (int)(k >> (msb - 1) & 1u) : 0);
+    return 63 - (half < 63 ? half : 63);
+}
+__global__ void order_hist_key(const int32_t *__restrict__ key, int n_reads, int *__restrict__ cnt)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x)
+        atomicAdd(&cnt[key_bin(key[r])], 1);
+}
+__global__ void order_scatter_key(const int32_t *__restrict__ key, int n_reads, const int *__restrict__ cnt,
+                                  int *__restrict__ cur, int *__restrict__ order)
+{
+    __shared__ int off[64];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < 64; ++b) off[b] = acc, acc += cnt[b];
+    }
+    __syncthreads();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        const int b = key_bin(key[r]);
+        order[off[b] + atomicAdd(&cur[b], 1)] = r;
     }
 }
 
@@ -1345,28 +1430,55 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         return rc;
     int *order = (int *)(A + o_order);
     int *ocnt = (int *)(A + o_order + al(sizeof(int) * (n_reads + 1)));
+    // per-read features / extension cells for the learned read order (kept for bsb_last_read_costs)
+    float *d_feat = nullptr;
+    int64_t *d_rcells = nullptr;
+    int32_t *d_rkey = nullptr;
+    const bool learned = ctx->read_model != nullptr, logging = ctx->read_log != 0;
+    if (learned || logging) {
+        const size_t nr = (size_t)n_reads;
+        if ((rc = bsb_ensure(ctx, &ctx->rc_buf, &ctx->rc_bytes, al(32 * nr) + al(8 * nr) + al(4 * nr) + 256,
+                             "read costs")))
+            return rc;
+        d_feat = (float *)ctx->rc_buf;
+        d_rcells = (int64_t *)((char *)ctx->rc_buf + al(32 * nr));
+        d_rkey = (int32_t *)((char *)ctx->rc_buf + al(32 * nr) + al(8 * nr));
+        const int fb = (int)std::min<int64_t>((n_reads + 127) / 128, (int64_t)ctx->n_sm * 8);
+        read_features_kernel<<<fb, 128, 0, st>>>(ao, B, n_reads, d_reads, d_read_off, d_seed_off, roff, cseeds, cchains,
+                                                 n_chains, d_feat);
+        ctx->rc_n = logging ? n_reads : 0;
+    }
     {
         const int ob = (int)((n_reads + 255) / 256) < ctx->n_sm * 4 ? (int)((n_reads + 255) / 256) : ctx->n_sm * 4;
         if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ocnt, 0, sizeof(int) * 2 * kOrderBins, st), "read order"))) return rc;
-        order_hist<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt);
-        order_scatter<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt, ocnt + kOrderBins, order);
+        if (learned) {       // predicted cells of every read, most expensive first
+            if ((rc = bsb_mlp_forward(ctx, (const bsb_mlp_weights_t *)ctx->read_model, d_feat, n_reads, nullptr,
+                                      d_rkey)))
+                return rc;
+            order_hist_key<<<ob, 256, 0, st>>>(d_rkey, n_reads, ocnt);
+            order_scatter_key<<<ob, 256, 0, st>>>(d_rkey, n_reads, ocnt, ocnt + kOrderBins, order);
+        } else {
+            order_hist<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt);
+            order_scatter<<<ob, 256, 0, st>>>(n_chains, n_reads, ocnt, ocnt + kOrderBins, order);
+        }
     }
+    int64_t *const rcells_out = logging ? d_rcells : nullptr;
     // every extension of these reads fits (max_len + 1) columns: the narrowest variant that holds them
     if (max_len <= 127)
         chain2aln_kernel<4><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
     else if (max_len <= 159)
         chain2aln_kernel<5><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
     else if (max_len <= 255)
         chain2aln_kernel<8><<<ctx->n_sm * 8, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+                                                            cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
     else if (max_len <= 511)
         chain2aln_kernel<16><<<ctx->n_sm * 4, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
     else
         chain2aln_kernel<32><<<ctx->n_sm * 2, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
-                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order);
+                                                             cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
     if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
     const int cgrid = (int)((n_reads + 3) / 4) < ctx->n_sm * 16 ? (int)((n_reads + 3) / 4) : ctx->n_sm * 16;
     compact_regs<<<cgrid, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
@@ -1494,4 +1606,36 @@ extern "C" int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
     if (o && !(o->mask_level_redun >= 0.f && o->mask_level_redun <= 1.f))
         return bsb_fail(ctx, BSB_EINVAL, "mask_level_redun must lie in [0, 1]");
     return align_batch(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, true);
+}
+
+extern "C" int bsb_read_cost_log(bsb_ctx *ctx, int enable)
+{
+    if (!ctx) return BSB_EINVAL;
+    ctx->read_log = enable != 0;
+    ctx->rc_n = 0;
+    return 0;
+}
+
+extern "C" int bsb_last_read_costs(bsb_ctx *ctx, int32_t n_reads, float *feat, int64_t *cells)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (!ctx->read_log || ctx->rc_n == 0) return bsb_fail(ctx, BSB_EINVAL, "no logged batch (bsb_read_cost_log)");
+    if (n_reads != ctx->rc_n) return bsb_fail(ctx, BSB_EINVAL, "the logged batch has %d reads, not %d", ctx->rc_n, n_reads);
+    int rc;
+    if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    const size_t nr = (size_t)n_reads;
+    const char *b = (const char *)ctx->rc_buf;
+    if (feat && (rc = bsb_cuda(ctx, cudaMemcpyAsync(feat, b, 32 * nr, cudaMemcpyDeviceToHost, ctx->stream), "D2H")))
+        return rc;
+    if (cells && (rc = bsb_cuda(ctx, cudaMemcpyAsync(cells, b + al(32 * nr), 8 * nr, cudaMemcpyDeviceToHost,
+                                                     ctx->stream), "D2H")))
+        return rc;
+    return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "read costs");
+}
+
+extern "C" int bsb_set_read_cost_model(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w)
+{
+    if (!ctx) return BSB_EINVAL;
+    ctx->read_model = d_w;
+    return 0;
 }

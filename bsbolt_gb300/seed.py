@@ -90,3 +90,24 @@ def align_regs(ctx: Context, seqs: np.ndarray, offs: np.ndarray, opt: "_lib.Alig
                 _ptr(regs_off))
     _lib.check(ctx.handle, rc)
     return regs[: regs_off[-1]].copy(), regs_off
+
+
+def read_cost_log(ctx: Context, enable: bool = True) -> None:
+    """bsb_read_cost_log: keep each later alignment batch's per-read features and DP cells."""
+    _lib.check(ctx.handle, ctx.L.bsb_read_cost_log(ctx.handle, int(enable)))
+
+
+def last_read_costs(ctx: Context, n_reads: int):
+    """(features[n, 8] float32, cells[n] int64) of the last logged alignment batch."""
+    feat = np.zeros((n_reads, 8), np.float32)
+    cells = np.zeros(n_reads, np.int64)
+    _lib.check(ctx.handle, ctx.L.bsb_last_read_costs(ctx.handle, n_reads, _ptr(feat), _ptr(cells)))
+    return feat, cells
+
+
+def set_read_cost_model(ctx: Context, model=None) -> None:
+    """Order the reads of later alignment batches by the cost model's prediction (a
+    cost_model.CostModel, whose device weights must stay alive meanwhile); None restores the
+    chain-count order."""
+    ptr = ctypes.c_void_p(model.w.data_ptr()) if model is not None else None
+    _lib.check(ctx.handle, ctx.L.bsb_set_read_cost_model(ctx.handle, ptr))

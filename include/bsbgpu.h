@@ -382,6 +382,25 @@ int bsb_mlp_backward(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w, const float *d_
 int bsb_mlp_adam(bsb_ctx *ctx, bsb_mlp_weights_t *d_w, float *d_master, float *d_m, float *d_v,
                  const float *d_grad, float lr, int32_t step);
 
+/* ---- learned read order of the alignment batches ------------------------- */
+
+/* No reference counterpart: BWA runs mem_chain2aln read by read on CPU threads.  Inside
+ * bsb_align_regs_batch / bsb_mem_align1_batch one warp extends one read's chains at a
+ * time, taking reads from a queue; by default the queue holds the reads with the most
+ * chains first.  A 2 x 64 cost model (the bsb_mlp_* kernels above, BSB_MLP_FEATURES
+ * features per read: read length, kept chains and their seeds, best chain weight, mean
+ * seed offset, reverse-strand share, C+G content, the plain bound of the extension cells)
+ * can order the queue by predicted DP cells instead.  The order never changes a result.
+ *   bsb_read_cost_log(ctx, 1): later batches keep, per read, the features and the DP cells
+ *     their ksw_extend2 calls visited (band retries included);
+ *   bsb_last_read_costs: copies them out for the last batch (n_reads must match; host
+ *     buffers of n_reads * BSB_MLP_FEATURES floats and n_reads int64);
+ *   bsb_set_read_cost_model(ctx, d_w): order later batches by the model's prediction
+ *     (weights in device memory, kept by the caller); NULL restores the chain-count order. */
+int bsb_read_cost_log(bsb_ctx *ctx, int enable);
+int bsb_last_read_costs(bsb_ctx *ctx, int32_t n_reads, float *feat, int64_t *cells);
+int bsb_set_read_cost_model(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w);
+
 /* ---- extension without any device allocation ---------------------------- */
 
 /* No counterpart in the reference: BWA allocates freely on the host and has

@@ -180,3 +180,38 @@ def test_dedup_random_indel_reads_vs_oracle(gpu_ctx, indexes):
             assert np.array_equal(regs[f], ref[f]), f"w={w}: dedup.{f}"
         merged += int((regs["n_comp"] > 1).sum())
     assert merged > 100
+
+
+def test_learned_read_order_changes_no_region(gpu_ctx, indexes):
+    """The per-read log (features, DP cells of the read's ksw_extend2 calls) and the learned
+    read order: the logged cells add up to the oracle's cell count of the same reads, a model
+    trained on the log orders the reads, and the regions stay the same."""
+    torch = pytest.importorskip("torch")
+    from bsbolt_gb300 import cost_model as cm
+    prefix = indexes["rep"]
+    seed.load_index(gpu_ctx, prefix)
+    g = np.load(os.path.join(GOLDEN, "reads_rep_L5.npz"))
+    reads, offs = g["reads"], g["read_off"]
+    n = len(offs) - 1
+    opt = opt_from(g["opts"])
+    seed.read_cost_log(gpu_ctx, True)
+    try:
+        plain, plain_off = seed.align_regs(gpu_ctx, reads, offs, opt, dedup=True)
+        feat, cells = seed.last_read_costs(gpu_ctx, n)
+    finally:
+        seed.read_cost_log(gpu_ctx, False)
+    bi = index.BwaIndex(prefix)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    ref = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oracle.Opt.from_list([int(x) for x in g["opts"]]), reads,
+                            offs, n_threads=8)
+    assert int(cells.sum()) == int(ref["cells"]) and np.isfinite(feat).all() and (cells >= 0).all()
+    model = cm.CostModel(gpu_ctx, seed=3)
+    model.train(torch.from_numpy(feat).cuda(), torch.from_numpy(np.log1p(cells).astype(np.float32)).cuda(),
+                epochs=3, batch=64)
+    seed.set_read_cost_model(gpu_ctx, model)
+    try:
+        learned, learned_off = seed.align_regs(gpu_ctx, reads, offs, opt, dedup=True)
+    finally:
+        seed.set_read_cost_model(gpu_ctx, None)
+    assert np.array_equal(plain_off, learned_off) and np.array_equal(plain, learned)

@@ -94,3 +94,35 @@ def test_seed_errors(gpu_ctx, ctx_idx):
     with pytest.raises(_lib.BsbError) as e:
         seed.sa_batch(ctx_idx, np.array([1 << 60], np.uint64))
     assert e.value.code == _lib.BSB_EINVAL
+
+
+@pytest.mark.parametrize("sym64", ["1", "0"], ids=["64-symbol-sectors", "32-symbol-sectors"])
+def test_occurrence_layouts_give_the_same_seeds_and_sa(gpu_ctx, idx, monkeypatch, sym64):
+    """The two device layouts of the occurrence array (32-symbol sectors, 64-symbol sectors with
+    2^32-row superblocks), forced at upload: seed lists against the reference's own (golden
+    L5 set) and the oracle, and every SA row through the LF walk and the full SA built from it."""
+    from bsbolt_gb300 import extend
+    monkeypatch.setenv("BSB_OCC_SYM64", sym64)
+    ctx = extend.Context(0)
+    try:
+        seed.load_index(ctx, idx)
+        d = np.load(os.path.join(GOLDEN, "reads_L5.npz"))
+        o = d["opts"]
+        got, off = seed.seed_batch(ctx, d["reads"], d["read_off"], min_seed_len=int(o[10]),
+                                   split_width=int(o[12]), max_mem_intv=int(o[13]))
+        ref, roff = d["smem"], d["smem_off"]
+        lens = d["read_off"][1:] - d["read_off"][:-1]
+        for r in range(len(lens)):
+            exp = ref[roff[r]:roff[r + 1]] if lens[r] >= int(o[10]) else ref[0:0]
+            assert np.array_equal(got[off[r]:off[r + 1]], exp), f"read {r}: seeds differ"
+        bi = index.BwaIndex(idx)
+        pac = bi.pac_codes()
+        text = np.concatenate([pac, 3 - pac[::-1]]).astype(np.uint8)
+        full = index.suffix_array(text).astype(np.int64)
+        want = np.where(full == len(text), -1, full)
+        rows = np.arange(0, len(full)).astype(np.uint64)
+        for resident in (1, 0):
+            _lib.check(ctx.handle, ctx.L.bsb_index_full_sa(ctx.handle, resident))
+            assert np.array_equal(seed.sa_batch(ctx, rows).astype(np.int64), want)
+    finally:
+        ctx.close()
