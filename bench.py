@@ -622,6 +622,29 @@ def sam_workloads(n_pairs_100mb, n_rrbs):
     return out
 
 
+def sam_compare(name, db, fqs, n_units, threads):
+    """One workload through the stock `bwa mem` and `bwa_gpu mem`: wall times, SAM and BSStat
+    identity, and bwa_gpu's own account of its time."""
+    stock = os.path.join(ROOT, "oracle", "_ref", "bwa")
+    gpu = os.path.join(ROOT, "bsbolt_gb300", "integration", "_build", "bwa_gpu")
+    tmp = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "sam")
+    os.makedirs(tmp, exist_ok=True)
+    sam_r, sam_g = os.path.join(tmp, name + ".ref.sam"), os.path.join(tmp, name + ".gpu.sam")
+    tr, st_r, _ = time_bwa_mem(stock, db, fqs, threads, sam_r)
+    tg, st_g, glog = time_bwa_mem(gpu, db, fqs, threads, sam_g, dict(os.environ, BSB_GPU_STATS="1"))
+    hr, nr = sam_sha(sam_r)
+    hg, ng = sam_sha(sam_g)
+    for f in (sam_r, sam_g):
+        os.unlink(f)
+    unit = "read pairs" if len(fqs) == 2 else "reads"
+    u = unit.replace(" ", "_")
+    return {unit: n_units, "sam_lines": nr,
+            f"stock_bwa_{u}_per_s": round(n_units / tr, 1), "stock_bwa_s": round(tr, 3),
+            f"bwa_gpu_{u}_per_s": round(n_units / tg, 1), "bwa_gpu_s": round(tg, 3),
+            "speedup": round(tr / tg, 3), "sam_identical": bool(hr == hg and nr == ng),
+            "bsstat_identical": st_r == st_g, "bsstat": st_g, "bwa_gpu_log": glog}
+
+
 def sam_block(n_pairs_100mb=500_000, n_rrbs=1_000_000, threads=None):
     """Aligned read pairs/s from SAM: the stock `bwa mem` (the reference BWA fork built from its
     own sources, oracle/Makefile.ref) against `bwa_gpu mem` (the same sources linked to
@@ -635,26 +658,130 @@ def sam_block(n_pairs_100mb=500_000, n_rrbs=1_000_000, threads=None):
     t0 = time.perf_counter()
     wl = sam_workloads(n_pairs_100mb, n_rrbs)
     prep_s = time.perf_counter() - t0
-    tmp = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "sam")
-    os.makedirs(tmp, exist_ok=True)
     res = {"argv": "bsbolt Align defaults (-Y -A1 -B4 -O6,6 -E1,1 -L30,30 -T10 -U17 -w100 -d100 -k19 -c500 "
                    "-h100,200 -e0.1 -l0.5 -n5 -Z0.95 ...) -t %d -K 10000000" % threads,
            "threads": threads, "workload_prep_s": round(prep_s, 1)}
-    env = dict(os.environ, BSB_GPU_STATS="1")
     for name, (db, fqs, n_units) in wl.items():
-        sam_r, sam_g = os.path.join(tmp, name + ".ref.sam"), os.path.join(tmp, name + ".gpu.sam")
-        tr, st_r, _ = time_bwa_mem(stock, db, fqs, threads, sam_r)
-        tg, st_g, glog = time_bwa_mem(gpu, db, fqs, threads, sam_g, env)
-        hr, nr = sam_sha(sam_r)
-        hg, ng = sam_sha(sam_g)
-        unit = "read pairs" if len(fqs) == 2 else "reads"
-        res[name] = {unit: n_units, "sam_lines": nr,
-                     f"stock_bwa_{unit.replace(' ', '_')}_per_s": round(n_units / tr, 1), "stock_bwa_s": round(tr, 3),
-                     f"bwa_gpu_{unit.replace(' ', '_')}_per_s": round(n_units / tg, 1), "bwa_gpu_s": round(tg, 3),
-                     "speedup": round(tr / tg, 3), "sam_identical": bool(hr == hg and nr == ng),
-                     "bsstat_identical": st_r == st_g, "bsstat": st_g, "bwa_gpu_log": glog}
-        for f in (sam_r, sam_g):
-            os.unlink(f)
+        res[name] = sam_compare(name, db, fqs, n_units, threads)
+    return res
+
+
+ADAPTER1 = "AGATCGGAAGAGCACACGTCTGAACTCCAGTCACATCACGATCTCGTATGCCGTCTTCTGCTTGAAAAAAAAAA"
+
+
+def ref1gb_reads(contigs, n_pairs, seed):
+    """The human-scale workload's read mix, scaled: 70 % 2x150 (insert N(400,50)) and 30 % 2x250
+    (insert N(550,60)) directional pairs; in 2 % of the pairs the fragment is shorter than the
+    read and the read runs into adapter.  Returns [(r1, r2)] per read length, bases as sequenced."""
+    from bsbolt_gb300 import synth
+    ad = synth.NT4[np.frombuffer(ADAPTER1.encode(), np.uint8)]
+    out = []
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for k, (rl, frac, ins, sd) in enumerate(((150, 0.7, 400, 50), (250, 0.3, 550, 60))):
+        r1, r2 = synth.bs_reads_pe_block(contigs, int(n_pairs * frac), rl, ins, sd, seed=seed + 1 + k)
+        for j in np.nonzero(rng.random(len(r1)) < 0.02)[0]:
+            c = int(rng.integers(rl // 2, rl))                 # fragment length below the read length
+            frag = r1[j, :c].copy()
+            r1[j, c:] = np.resize(ad, rl - c)
+            r2[j, :c] = synth.COMP[frag[::-1]]
+            r2[j, c:] = np.resize(ad[::-1], rl - c)
+        out.append((r1, r2))
+    return out
+
+
+def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
+    """The human-scale configuration at 1 Gb (the largest whose index text, 4e9 symbols with both
+    conversions and strands, keeps 32-bit suffix ranks): 8 contigs of 125 Mb, GC 41 %, CpG 1 %,
+    45 % interspersed repeats (families 300 bp - 6 kb, 2-20 % divergence).  The index is built
+    with the suffix array sorted on the GPU and held in HBM (64-symbol occurrence sectors, full
+    SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
+    every pair, parity against the oracle on a sample, and stock bwa against bwa_gpu from SAM."""
+    import oracle
+    from bsbolt_gb300 import _lib, index, seed, synth
+    res = {}
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "ref1gb")
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "ref")
+    t0 = time.perf_counter()
+    contigs = synth.bs_genome(8, 125_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 4)
+    synth.add_repeats(contigs, 0.45, fam_len=(300, 6000), div=(0.02, 0.20), n_families=500, seed=20261203 + 4)
+    res["genome_s"] = round(time.perf_counter() - t0, 1)
+    if not os.path.exists(prefix + ".sa"):
+        synth.write_fasta(prefix + ".fa", contigs)
+        t0 = time.perf_counter()
+        index.build_index(prefix + ".fa", prefix, ctx=ctx)
+        res["index_build_s"] = round(time.perf_counter() - t0, 1)
+    sets = ref1gb_reads(contigs, n_pairs, 20261203 + 40)
+    del contigs
+    fq = []
+    for k, (r1, r2) in enumerate(sets):
+        for e, r in ((1, r1), (2, r2)):
+            fn = os.path.join(d, f"pe{k}_{e}.fq")
+            synth.write_fastq_block(fn, r, e, first=sum(len(x[0]) for x in sets[:k]))
+            fq.append(fn)
+    for e in (1, 2):                                   # one FASTQ per end, both read lengths
+        with open(os.path.join(d, f"r{e}.fq"), "wb") as f:
+            for k in range(len(sets)):
+                with open(os.path.join(d, f"pe{k}_{e}.fq"), "rb") as g:
+                    f.write(g.read())
+    t0 = time.perf_counter()
+    seed.load_index(ctx, prefix)
+    res["index_upload_s"] = round(time.perf_counter() - t0, 1)
+    # the reads as the aligner sees them: read 1 C->T, read 2 G->A, pairs interleaved
+    reads, lens = [], []
+    for r1, r2 in sets:
+        c1, c2 = synth.bs_convert(r1, g2a=False), synth.bs_convert(r2, g2a=True)
+        reads.append(np.stack([c1, c2], axis=1).reshape(-1))
+        lens.append(np.full(2 * len(r1), r1.shape[1], np.int64))
+    reads = np.concatenate(reads)
+    offs = np.zeros(sum(len(x) for x in lens) + 1, np.int64)
+    offs[1:] = np.cumsum(np.concatenate(lens))
+    n_reads = len(offs) - 1
+    opt = _lib.AlignOpt.bwa_defaults()
+    batches, lo = [], 0
+    while lo < n_reads:
+        hi = int(np.searchsorted(offs, offs[lo] + batch_bases, side="left"))
+        hi = max(lo + 2, min(hi + (hi - lo) % 2, n_reads))
+        batches.append((lo, hi))
+        lo = hi
+
+    def sub(a, b):
+        return reads[offs[a]:offs[b]], offs[a:b + 1] - offs[a]
+    res["seeding_roofline_one_batch"] = seeding_roofline(ctx, reads, offs[batches[0][0]:batches[0][1] + 1])
+    seed.align_regs(ctx, *sub(*batches[0]), opt, dedup=True)       # warm-up
+    t0 = time.perf_counter()
+    first = None
+    for a, b in batches:
+        regs, roff = seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        if first is None:
+            first = (regs, roff)
+    gpu_s = time.perf_counter() - t0
+    bi = index.BwaIndex(prefix)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    oo = oracle.Opt.from_list([1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 19, 500, 10, 20, 10000])
+    ns = 1000
+    cr, co = sub(0, ns)
+    t0 = time.perf_counter()
+    pre = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oo, cr, co, n_threads=os.cpu_count() or 1)
+    ref, ref_off = oracle.sort_dedup_batch(oo, bi.l_pac, bi.pac, cr, co, pre["regs"], pre["regs_off"])
+    cpu_s = time.perf_counter() - t0
+    regs, roff = first
+    k = int(roff[ns])
+    exact = bool(np.array_equal(roff[:ns + 1], ref_off) and all(np.array_equal(regs[f][:k], ref[f])
+                                                                  for f in ref.dtype.names))
+    res.update({
+        "workload": f"1 Gb bisulfite reference (8x125 Mb, 45% repeats), {n_reads // 2} directional pairs: 70% 2x150, "
+                    f"30% 2x250, 2% adapter read-through; -K 10M batches ({len(batches)}); BWA defaults",
+        "seq_len": int(bi.l_pac) * 2, "occ_layout": "64-symbol sectors (0.5 B/row)",
+        "gpu_mem_align1_read_pairs_per_s": round(n_reads / 2 / gpu_s, 1),
+        "cpu_oracle_read_pairs_per_s": round(ns / 2 / cpu_s, 1), "cpu_oracle_sample_reads": ns,
+        "regions_bit_exact_vs_oracle_on_sample": exact})
+    del bi, ob
+    threads = os.cpu_count() or 1
+    if os.path.exists(os.path.join(ROOT, "bsbolt_gb300", "integration", "_build", "bwa_gpu")):
+        res["sam"] = sam_compare("pe_1gb", bsbolt_db(prefix), [os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq")],
+                                 n_reads // 2, threads)
     return res
 
 
@@ -1105,6 +1232,13 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             rrbs = {"error": f"{type(e).__name__}: {e}"}
 
+    big1g = None
+    if rank == 0 and args.ref1gb:
+        try:
+            big1g = pipeline_ref1gb(ctx, n_pairs=args.ref1gb_pairs)
+        except Exception as e:   # reported, never hidden
+            big1g = {"error": f"{type(e).__name__}: {e}"}
+
     lp = None
     if rank == 0 and not args.no_learned and not args.no_ref100mb:
         try:
@@ -1192,6 +1326,7 @@ def run_ours(args, ws, rank, local):
             "gen_cigar": cig,
             "mate_rescue_sw": msw,
             "sam_pipeline": sam,
+            "pipeline_1gb_ref": big1g,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -1217,6 +1352,9 @@ def main():
                     help="skip the 100 Mb-reference blocks, WGBS-like PE and RRBS-like SE (they build a 100 Mb "
                          "index: ~1 min the first time)")
     ap.add_argument("--no-sam", action="store_true", help="skip the stock bwa vs bwa_gpu SAM block")
+    ap.add_argument("--ref1gb", action="store_true",
+                    help="add the 1 Gb-reference block (index sorted on the GPU; a few minutes to build)")
+    ap.add_argument("--ref1gb-pairs", type=int, default=200_000)
     ap.add_argument("--sam-pairs", type=int, default=500_000,
                     help="2x150 pairs of the SAM block on the 100 Mb reference (the full workload is 4M)")
     ap.add_argument("--sam-rrbs", type=int, default=1_000_000,

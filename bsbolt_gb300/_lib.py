@@ -178,6 +178,8 @@ def load(path: str = LIB_PATH):
     L.bsb_last_read_costs.restype = I32
     L.bsb_set_read_cost_model.argtypes = [P, P]
     L.bsb_set_read_cost_model.restype = I32
+    L.bsb_build_suffix_array.argtypes = [P, P, I64, P]
+    L.bsb_build_suffix_array.restype = I32
     L.bsb_align2_batch.restype = I32
     _lib = L
     return L

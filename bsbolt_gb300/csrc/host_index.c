@@ -284,35 +284,34 @@ static int write_ann_amb(const char *prefix, const contig_t *c, int n, int64_t l
 
 /* --------------------------------------------------------- BWT + SA files */
 
-static int write_bwt_sa(const char *prefix, const uint8_t *pac, int64_t l_pac, int sa_intv)
+/* base at position p of the text bwa index sorts: the pac, then its reverse complement */
+static inline int text_at(const uint8_t *pac, int64_t l_pac, int64_t p)
 {
-    const int64_t n = 2 * l_pac;                /* text length without the sentinel */
-    int32_t *T, *SA;
+    return p < l_pac ? GETPAC(pac, p) : 3 - GETPAC(pac, 2 * l_pac - 1 - p);
+}
+
+/* .bwt and .sa from the suffix array of the text + '$' (n + 1 rows, in sa32 or sa64) */
+static int write_bwt_sa_from(const char *prefix, const uint8_t *pac, int64_t l_pac, int sa_intv, const int32_t *sa32,
+                             const int64_t *sa64)
+{
+    const int64_t n = 2 * l_pac;
     uint64_t L2[5] = {0, 0, 0, 0, 0}, primary = 0, cnt[4] = {0, 0, 0, 0};
     int64_t i, k, r, n_occ, bwt_words, n_sa;
     uint32_t *buf;
     char fn[4096];
     FILE *fp;
-    if (n + 1 > 0x7fffffffLL) return -2;       /* int32 SA-IS limit */
-    T = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
-    SA = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
-    if (!T || !SA) { free(T); free(SA); return -3; }
-    for (i = 0; i < l_pac; ++i) T[i] = GETPAC(pac, i) + 1;
-    for (i = 0; i < l_pac; ++i) T[l_pac + i] = 3 - GETPAC(pac, l_pac - 1 - i) + 1;
-    T[n] = 0;
-    for (i = 0; i < n; ++i) ++L2[T[i]];
+    for (i = 0; i < n; ++i) ++L2[text_at(pac, l_pac, i) + 1];
     for (i = 2; i <= 4; ++i) L2[i] += L2[i - 1];
-    if (sais(T, SA, n + 1, 5) != 0) { free(T); free(SA); return -3; }
-
     /* interleaved BWT: 4 x u64 counts then 8 words per 128 symbols, plus a final count block */
     n_occ = (n + 127) / 128 + 1;
     bwt_words = (n + 15) / 16 + n_occ * 8;
     buf = (uint32_t *)calloc((size_t)bwt_words, 4);
-    if (!buf) { free(T); free(SA); return -3; }
+    if (!buf) return -3;
     for (r = 0, i = 0, k = 0; r <= n; ++r) {
+        const int64_t s = sa32 ? (int64_t)sa32[r] : sa64[r];
         int c;
-        if (SA[r] == 0) { primary = (uint64_t)r; continue; }
-        c = T[SA[r] - 1] - 1;
+        if (s == 0) { primary = (uint64_t)r; continue; }
+        c = text_at(pac, l_pac, s - 1);
         if (i % 128 == 0) { memcpy(buf + k, cnt, 32); k += 8; }
         if (i % 16 == 0) ++k;
         buf[k - 1] |= (uint32_t)c << ((15 - (i & 15)) << 1);
@@ -322,7 +321,7 @@ static int write_bwt_sa(const char *prefix, const uint8_t *pac, int64_t l_pac, i
     memcpy(buf + k, cnt, 32);
     k += 8;
     snprintf(fn, sizeof fn, "%s.bwt", prefix);
-    if (!(fp = fopen(fn, "wb"))) { free(T); free(SA); free(buf); return -1; }
+    if (!(fp = fopen(fn, "wb"))) { free(buf); return -1; }
     fwrite(&primary, 8, 1, fp);
     fwrite(L2 + 1, 8, 4, fp);
     fwrite(buf, 4, (size_t)k, fp);
@@ -332,7 +331,7 @@ static int write_bwt_sa(const char *prefix, const uint8_t *pac, int64_t l_pac, i
     /* sampled suffix array: sa[r/intv] = SA[r] for r % intv == 0, sa[0] = -1 (not stored) */
     n_sa = (n + sa_intv) / sa_intv;
     snprintf(fn, sizeof fn, "%s.sa", prefix);
-    if (!(fp = fopen(fn, "wb"))) { free(T); free(SA); return -1; }
+    if (!(fp = fopen(fn, "wb"))) return -1;
     {
         uint64_t v = (uint64_t)sa_intv, sl = (uint64_t)n;
         fwrite(&primary, 8, 1, fp);
@@ -340,18 +339,56 @@ static int write_bwt_sa(const char *prefix, const uint8_t *pac, int64_t l_pac, i
         fwrite(&v, 8, 1, fp);
         fwrite(&sl, 8, 1, fp);
         for (i = 1; i < n_sa; ++i) {
-            uint64_t x = (uint64_t)SA[i * sa_intv];
+            uint64_t x = (uint64_t)(sa32 ? (int64_t)sa32[i * sa_intv] : sa64[i * sa_intv]);
             fwrite(&x, 8, 1, fp);
         }
     }
-    fclose(fp);
-    free(T);
-    free(SA);
-    return 0;
+    return fclose(fp);
 }
+
+static int write_bwt_sa(const char *prefix, const uint8_t *pac, int64_t l_pac, int sa_intv)
+{
+    const int64_t n = 2 * l_pac;                /* text length without the sentinel */
+    int32_t *T, *SA;
+    int64_t i;
+    int rc;
+    if (n + 1 > 0x7fffffffLL) return -2;       /* int32 SA-IS limit */
+    T = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    SA = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    if (!T || !SA) { free(T); free(SA); return -3; }
+    for (i = 0; i < n; ++i) T[i] = text_at(pac, l_pac, i) + 1;
+    T[n] = 0;
+    if (sais(T, SA, n + 1, 5) != 0) { free(T); free(SA); return -3; }
+    free(T);
+    rc = write_bwt_sa_from(prefix, pac, l_pac, sa_intv, SA, NULL);
+    free(SA);
+    return rc;
+}
+
+/* .bwt and .sa of <prefix> from a suffix array sorted elsewhere (the GPU's), 2*l_pac + 1 rows
+ * of int64, and the converted pac of <prefix>.pac. */
+int bsbh_write_bwt_sa64(const char *prefix, const uint8_t *pac, int64_t l_pac, const int64_t *sa, int sa_intv)
+{
+    if (!prefix || !pac || !sa || l_pac < 1 || sa_intv < 1) return -1;
+    return write_bwt_sa_from(prefix, pac, l_pac, sa_intv, NULL, sa);
+}
+
+static int index_fasta(const char *fasta, const char *prefix, int with_bwt, int64_t *l_pac_out);
 
 /* Build <prefix>.{pac,opac,ann,amb,bwt,sa} from a FASTA file.  Returns 0 or a negative code. */
 int bsbh_index_fasta(const char *fasta, const char *prefix)
+{
+    return index_fasta(fasta, prefix, 1, NULL);
+}
+
+/* The same without .bwt / .sa (their suffix array is sorted elsewhere); *l_pac receives the
+ * length of the converted pac. */
+int bsbh_index_fasta_nobwt(const char *fasta, const char *prefix, int64_t *l_pac)
+{
+    return index_fasta(fasta, prefix, 0, l_pac);
+}
+
+static int index_fasta(const char *fasta, const char *prefix, int with_bwt, int64_t *l_pac_out)
 {
     contig_t *c = NULL;
     int n = 0, nh = 0, nh2 = 0, k, rc;
@@ -370,7 +407,8 @@ int bsbh_index_fasta(const char *fasta, const char *prefix)
     snprintf(fn, sizeof fn, "%s.opac", prefix);
     if (!rc) rc = write_pac(fn, opac, l2);
     if (!rc) rc = write_ann_amb(prefix, c, n, l_pac, h, nh, na);
-    if (!rc) rc = write_bwt_sa(prefix, pac, l_pac, 32);
+    if (!rc && with_bwt) rc = write_bwt_sa(prefix, pac, l_pac, 32);
+    if (l_pac_out) *l_pac_out = l_pac;
     for (k = 0; k < n; ++k) { free(c[k].name); free(c[k].comment); free(c[k].seq); }
     free(c); free(h); free(h2); free(na); free(na2); free(pac); free(opac);
     return rc;

@@ -1,7 +1,10 @@
-"""FM-index files in BWA's formats: build (host C, SA-IS) and load.
+"""FM-index files in BWA's formats: build (host C, SA-IS; or the suffix array on the GPU) and load.
 
 ``build_index(fasta, prefix)`` writes <prefix>.{pac,opac,ann,amb,bwt,sa} exactly
-as BSBolt's ``bwa index -a bwtsw`` does (bsbolt/External/BWA/bwtindex.c:256-321).
+as BSBolt's ``bwa index -a bwtsw`` does (bsbolt/External/BWA/bwtindex.c:256-321);
+``build_index(fasta, prefix, ctx=ctx)`` sorts the suffix array on the GPU
+(bsb_build_suffix_array: prefix doubling, texts up to 2^32 - 2 symbols, where the
+host SA-IS stops at 2^31) and writes the same files.
 ``BwaIndex(prefix)`` reads them back into numpy arrays (bwt_restore_bwt,
 bwt_restore_sa, bns_restore: bwt.c:420-457, bntseq.c:99-176).
 """
@@ -27,14 +30,37 @@ def host_lib():
         L.bsbh_index_fasta.restype = ctypes.c_int
         L.bsbh_suffix_array.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
         L.bsbh_suffix_array.restype = ctypes.c_int
+        L.bsbh_index_fasta_nobwt.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
+        L.bsbh_index_fasta_nobwt.restype = ctypes.c_int
+        L.bsbh_write_bwt_sa64.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_int]
+        L.bsbh_write_bwt_sa64.restype = ctypes.c_int
         _host = L
     return _host
 
 
-def build_index(fasta: str, prefix: str) -> None:
-    rc = host_lib().bsbh_index_fasta(fasta.encode(), prefix.encode())
+def build_index(fasta: str, prefix: str, ctx=None) -> None:
+    """<prefix>.{pac,opac,ann,amb,bwt,sa} of a FASTA file; with ctx (an extend.Context) the
+    suffix array is sorted on that GPU."""
+    if ctx is None:
+        rc = host_lib().bsbh_index_fasta(fasta.encode(), prefix.encode())
+        if rc != 0:
+            raise RuntimeError(f"index build failed ({rc}) for {fasta}")
+        return
+    from . import _lib
+    l_pac = ctypes.c_int64()
+    rc = host_lib().bsbh_index_fasta_nobwt(fasta.encode(), prefix.encode(), ctypes.byref(l_pac))
     if rc != 0:
         raise RuntimeError(f"index build failed ({rc}) for {fasta}")
+    n = l_pac.value
+    pac = np.fromfile(prefix + ".pac", dtype=np.uint8)[: (n + 3) // 4].copy()
+    sa = np.empty(2 * n + 1, np.int64)
+    _lib.check(ctx.handle, ctx.L.bsb_build_suffix_array(ctx.handle, pac.ctypes.data_as(ctypes.c_void_p), n,
+                                                        sa.ctypes.data_as(ctypes.c_void_p)))
+    rc = host_lib().bsbh_write_bwt_sa64(prefix.encode(), pac.ctypes.data_as(ctypes.c_void_p), n,
+                                        sa.ctypes.data_as(ctypes.c_void_p), 32)
+    if rc != 0:
+        raise RuntimeError(f"writing {prefix}.bwt/.sa failed ({rc})")
 
 
 def suffix_array(text: np.ndarray) -> np.ndarray:

@@ -208,12 +208,17 @@ def add_repeats(contigs, frac: float = 0.15, fam_len=(300, 6000), div=(0.02, 0.1
 
 def write_fasta(path: str, contigs, width: int = 60) -> None:
     letters = np.frombuffer(b"ACGTN", np.uint8)
-    with open(path, "w") as f:
+    with open(path, "wb") as f:
         for name, codes in contigs:
-            f.write(f">{name}\n")
-            txt = letters[codes].tobytes().decode()
-            for i in range(0, len(txt), width):
-                f.write(txt[i:i + width] + "\n")
+            f.write(f">{name}\n".encode())
+            txt = letters[np.asarray(codes, np.uint8)]
+            full = len(txt) // width * width
+            lines = np.empty((full // width, width + 1), np.uint8)     # whole lines, newline last
+            lines[:, :width] = txt[:full].reshape(-1, width)
+            lines[:, width] = ord("\n")
+            f.write(lines.tobytes())
+            if full < len(txt):
+                f.write(txt[full:].tobytes() + b"\n")
 
 
 def bs_reads_pe(contigs, n_pairs: int, read_len: int = 100, insert_mean: float = 300,

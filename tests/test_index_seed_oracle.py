@@ -110,3 +110,24 @@ def test_oracle_ksw_matches_reference_job_stream(name):
     out, _ = oracle.ksw_batch(jobs, seq, synth.fill_scmat(int(o[0]), int(o[1])), int(o[2]), int(o[3]),
                               int(o[4]), int(o[5]), int(o[7]))
     assert np.array_equal(out, ref)
+
+
+def test_bwt_sa_writer_from_a_64bit_suffix_array(tmp_path):
+    """The writer the GPU-sorted suffix array goes through (bsbh_write_bwt_sa64), fed the host
+    SA-IS order as int64, gives the reference `bwa index` files byte for byte."""
+    import ctypes
+    fa = str(tmp_path / "ref.fa")
+    synth.write_fasta(fa, golden_data.golden_genome())
+    prefix = str(tmp_path / "ref")
+    L = index.host_lib()
+    l_pac = ctypes.c_int64()
+    assert L.bsbh_index_fasta_nobwt(fa.encode(), prefix.encode(), ctypes.byref(l_pac)) == 0
+    n = l_pac.value
+    pac = np.fromfile(prefix + ".pac", dtype=np.uint8)[: (n + 3) // 4].copy()
+    b = ((pac[np.arange(n) >> 2] >> ((~np.arange(n) & 3) << 1)) & 3).astype(np.uint8)
+    sa = index.suffix_array(np.concatenate([b, 3 - b[::-1]]).astype(np.uint8)).astype(np.int64)
+    assert L.bsbh_write_bwt_sa64(prefix.encode(), pac.ctypes.data_as(ctypes.c_void_p), n,
+                                 sa.ctypes.data_as(ctypes.c_void_p), 32) == 0
+    want = json.load(open(os.path.join(GOLDEN, "index_sha256.json")))["files"]
+    for ext, h in want.items():
+        assert sha(prefix + "." + ext) == h, f".{ext} differs from the reference bwa index"
