@@ -574,9 +574,13 @@ __device__ KswResult extend_any(const KswParams &P, int qlen, int tlen, int h0, 
     const int need = (qlen + 32) >> 5;
     if constexpr (MaxC <= 8) {
         return run_ext<MaxC>(P, qlen, tlen, h0, w, eb, acc, lane);
-    } else {
+    } else if constexpr (MaxC <= 16) {
         if (need <= 8) return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
         return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
+    } else {                 // reads of 512-1023 bases: extensions past 511 columns need 32 per lane
+        if (need <= 8) return run_ext<8>(P, qlen, tlen, h0, w, eb, acc, lane);
+        if (need <= 16) return run_ext<16>(P, qlen, tlen, h0, w, eb, acc, lane);
+        return run_ext<32>(P, qlen, tlen, h0, w, eb, acc, lane);
     }
 }
 

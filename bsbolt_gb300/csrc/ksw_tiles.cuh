@@ -50,9 +50,12 @@ struct KswTileMap {
     uint8_t tile[kMaxNeed + 1];    // [0] unused
 };
 
-// 4 lanes up to 64 columns, 8 lanes up to 144, 16 up to 256, then 32; the
-// narrowest even C that holds the query within each group size (even C runs
-// on 16-bit cells, two per register: cheaper than the next-narrower odd C).
+// 4 lanes up to 128 columns (even C up to 16, then 20, 24, 28, 32), 8 lanes up to
+// 144, 16 up to 256, then 32; the narrowest even C that holds the query within each
+// group size (even C runs on 16-bit cells, two per register: cheaper than the
+// next-narrower odd C).  Measured on GB300 with the autotuner on the 4M-job
+// distribution: 4x20..4x32 beat 8x10..8x16 by 1.11-1.23x on the bands they hold (fewer
+// lanes per job amortise a row's fixed work over more columns).
 constexpr int even_up(int c) { return c + (c & 1); }
 constexpr KswTileMap make_default_tile_map()
 {
@@ -60,6 +63,7 @@ constexpr KswTileMap make_default_tile_map()
     for (int need = 1; need <= kMaxNeed; ++need) {
         int t = 0;
         if (need <= 64) t = tile_index(4, even_up((need + 3) / 4));
+        else if (need <= 128) t = tile_index(4, ((need + 15) / 16) * 4);
         else if (need <= 144) t = tile_index(8, even_up((need + 7) / 8 < 9 ? 9 : (need + 7) / 8));
         else if (need <= 256) t = tile_index(16, even_up((need + 15) / 16 < 10 ? 10 : (need + 15) / 16));
         else if (need <= 512) t = tile_index(32, even_up((need + 31) / 32 < 9 ? 9 : (need + 31) / 32));
