@@ -14,6 +14,7 @@
  *       err_fatal(__func__, "%s", bsb_last_error(g_bsb));
  * and link with -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2.
  */
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
@@ -37,35 +38,126 @@ void mem_opt_to_bsb(const mem_opt_t *opt, bsb_align_opt_t *o)
     memcpy(o->mat, opt->mat, 25);
 }
 
+/* ---- the host work around each library call, on opt->n_threads threads ----
+ * BWA runs this work inside worker1/worker2 on its kt_for threads; here it is split the same
+ * way: items are handed out in chunks from a shared counter, and every item writes only its
+ * own slots, so the result does not depend on the thread count. */
+#define GLUE_MAX_THREADS 256
+#define GLUE_CHUNK 512
+typedef void (*glue_body_f)(void *data, int64_t i, int tid);
+typedef struct {
+    glue_body_f fn;
+    void *data;
+    int64_t n, next;
+} glue_loop_t;
+typedef struct {
+    glue_loop_t *L;
+    int tid;
+} glue_worker_t;
+
+static void *glue_worker(void *arg)
+{
+    const glue_worker_t *w = (const glue_worker_t *)arg;
+    glue_loop_t *L = w->L;
+    for (;;) {
+        int64_t b = __atomic_fetch_add(&L->next, GLUE_CHUNK, __ATOMIC_RELAXED), e, i;
+        if (b >= L->n) break;
+        e = b + GLUE_CHUNK < L->n ? b + GLUE_CHUNK : L->n;
+        for (i = b; i < e; ++i) L->fn(L->data, i, w->tid);
+    }
+    return 0;
+}
+
+/* fn(data, i, tid) for i in [0, n), tid < glue_threads(n_threads) */
+static int glue_threads(int n_threads) { return n_threads < 1 ? 1 : n_threads > GLUE_MAX_THREADS ? GLUE_MAX_THREADS : n_threads; }
+
+static void glue_for(int n_threads, int64_t n, glue_body_f fn, void *data)
+{
+    glue_loop_t L;
+    glue_worker_t w[GLUE_MAX_THREADS];
+    pthread_t th[GLUE_MAX_THREADS];
+    int64_t chunks = (n + GLUE_CHUNK - 1) / GLUE_CHUNK;
+    int t, started = 0;
+    n_threads = glue_threads(n_threads);
+    if (n_threads > chunks) n_threads = chunks < 1 ? 1 : (int)chunks;
+    L.fn = fn, L.data = data, L.n = n, L.next = 0;
+    for (t = 0; t < n_threads; ++t) w[t].L = &L, w[t].tid = t;
+    for (t = 1; t < n_threads; ++t) {                  /* a thread that fails to start leaves its share to the rest */
+        if (pthread_create(&th[t], 0, glue_worker, &w[t])) break;
+        started = t;
+    }
+    glue_worker(&w[0]);
+    for (t = 1; t <= started; ++t) pthread_join(th[t], 0);
+}
+
 static int64_t g_align_regrown;   /* batches whose region buffer had to grow */
 
 int64_t mem_align_regrown(void) { return __atomic_load_n(&g_align_regrown, __ATOMIC_RELAXED); }
+
+typedef struct {
+    bseq1_t *seqs;
+    const bntseq_t *bns;
+    mem_alnreg_v *regs;
+    const int64_t *offs, *roff;
+    uint8_t *buf;
+    const bsb_reg_t *out;
+} align_batch_t;
+
+/* nt4 in place, as mem_align1_core does (bwamem.c:1164-1166), and into the packed batch */
+static void align_encode(void *data, int64_t i, int tid)
+{
+    align_batch_t *B = (align_batch_t *)data;
+    char *s = B->seqs[i].seq;
+    int j;
+    (void)tid;
+    for (j = 0; j < B->seqs[i].l_seq; ++j) s[j] = s[j] < 4 ? s[j] : nst_nt4_table[(int)s[j]];
+    memcpy(B->buf + B->offs[i], s, B->seqs[i].l_seq);
+}
+
+/* read i's regions as mem_alnreg_t */
+static void align_convert(void *data, int64_t i, int tid)
+{
+    align_batch_t *B = (align_batch_t *)data;
+    mem_alnreg_v *v = &B->regs[i];
+    const int k = (int)(B->roff[i + 1] - B->roff[i]);
+    int j;
+    (void)tid;
+    v->n = v->m = k;
+    v->a = (mem_alnreg_t *)malloc(sizeof(mem_alnreg_t) * (k ? k : 1));
+    for (j = 0; j < k; ++j) {
+        const bsb_reg_t *r = &B->out[B->roff[i] + j];
+        mem_alnreg_t *a = &v->a[j];
+        memset(a, 0, sizeof(*a));         /* mem_chain2aln starts from zero (bwamem.c:713) */
+        a->rb = r->rb; a->re = r->re; a->qb = r->qb; a->qe = r->qe;
+        a->rid = r->rid; a->score = r->score; a->truesc = r->truesc; a->w = r->w;
+        a->seedcov = r->seedcov; a->seedlen0 = r->seedlen0; a->frac_rep = r->frac_rep;
+        a->n_comp = r->n_comp;
+        /* the ALT marking of mem_align1_core (bwamem.c:1189-1193) */
+        if (a->rid >= 0 && B->bns->anns[a->rid].is_alt) a->is_alt = 1;
+    }
+}
 
 int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, const uint8_t *pac,
                         int n, bseq1_t *seqs, mem_alnreg_v *regs)
 {
     bsb_align_opt_t o;
-    int64_t *offs, total = 0, *roff, cap;
+    align_batch_t B;
+    int64_t *offs, *roff, cap;
     uint8_t *buf;
     bsb_reg_t *out;
-    int i, j, rc;
+    int i, rc;
     mem_opt_to_bsb(opt, &o);
     offs = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
     roff = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
-    for (i = 0; i < n; ++i) total += seqs[i].l_seq;
-    buf = (uint8_t *)malloc(total + 1);
     offs[0] = 0;
-    for (i = 0; i < n; ++i) {
-        char *s = seqs[i].seq;
-        /* nt4 in place, as mem_align1_core does (bwamem.c:1164-1166) */
-        for (j = 0; j < seqs[i].l_seq; ++j) s[j] = s[j] < 4 ? s[j] : nst_nt4_table[(int)s[j]];
-        memcpy(buf + offs[i], s, seqs[i].l_seq);
-        offs[i + 1] = offs[i] + seqs[i].l_seq;
-    }
+    for (i = 0; i < n; ++i) offs[i + 1] = offs[i] + seqs[i].l_seq;
+    buf = (uint8_t *)malloc(offs[n] + 1);
+    B.seqs = seqs, B.bns = bns, B.regs = regs, B.offs = offs, B.roff = roff, B.buf = buf, B.out = 0;
+    glue_for(opt->n_threads, n, align_encode, &B);
     /* A first guess at the region count; a read in a family of many copies can have up to
      * max_occ regions per seed (bwamem.c:281-283), and then the library answers
      * BSB_ECAPACITY with the count it needs in roff[n], and the batch runs again. */
-    cap = 4 * total + 64 * (int64_t)n;
+    cap = 4 * offs[n] + 64 * (int64_t)n;
     out = (bsb_reg_t *)malloc(sizeof(bsb_reg_t) * (cap + 1));
     rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, cap, roff);
     if (rc == BSB_ECAPACITY && roff[n] > cap) {
@@ -76,24 +168,8 @@ int mem_align_batch_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns,
         rc = bsb_mem_align1_batch(ctx, &o, n, buf, offs, out, cap, roff);
     }
     if (rc == 0) {
-        for (i = 0; i < n; ++i) {
-            mem_alnreg_v *v = &regs[i];
-            int k = (int)(roff[i + 1] - roff[i]);
-            v->n = v->m = k;
-            v->a = (mem_alnreg_t *)malloc(sizeof(mem_alnreg_t) * (k ? k : 1));
-            for (j = 0; j < k; ++j) {
-                const bsb_reg_t *r = &out[roff[i] + j];
-                mem_alnreg_t *a = &v->a[j];
-                memset(a, 0, sizeof(*a));         /* mem_chain2aln starts from zero (bwamem.c:713) */
-                a->rb = r->rb; a->re = r->re; a->qb = r->qb; a->qe = r->qe;
-                a->rid = r->rid; a->score = r->score; a->truesc = r->truesc; a->w = r->w;
-                a->seedcov = r->seedcov; a->seedlen0 = r->seedlen0; a->frac_rep = r->frac_rep;
-                a->n_comp = r->n_comp;
-            }
-            /* the ALT marking of mem_align1_core (bwamem.c:1189-1193) */
-            for (j = 0; j < (int)v->n; ++j)
-                if (v->a[j].rid >= 0 && bns->anns[v->a[j].rid].is_alt) v->a[j].is_alt = 1;
-        }
+        B.out = out;
+        glue_for(opt->n_threads, n, align_convert, &B);
     }
     free(offs); free(roff); free(buf); free(out);
     return rc;
@@ -178,107 +254,150 @@ static int cig_eligible(const mem_opt_t *opt, const bseq1_t *s, const mem_alnreg
  * pair chose another hit -- is answered by the reference's own function; with -a
  * (MEM_F_ALL) every region is prepared. */
 #define CIG_PAIR_NEAR 16
+typedef struct {
+    const mem_opt_t *opt;
+    const bseq1_t *seqs;
+    const mem_alnreg_v *regs;
+    int64_t n_processed;
+    const int64_t *base;           /* read i's picks go to pick[base[i]..], at most regs[i].n */
+    int *n_of;                     /* and their count */
+    cig_pick_t *pick;
+    mem_alnreg_t *tmp;             /* per-thread copies of a read's regions ... */
+    int *cnt;                      /* ... and XA counts, tmax + 1 each */
+    int tmax;
+} cig_sel_t;
+
+static void cig_select1(void *data, int64_t i64, int tid)
+{
+    cig_sel_t *S = (cig_sel_t *)data;
+    const mem_opt_t *opt = S->opt;
+    const int i = (int)i64, k = (int)S->regs[i].n;
+    const mem_alnreg_t *a = S->regs[i].a;
+    mem_alnreg_t *tmp = S->tmp + (int64_t)tid * (S->tmax + 1);
+    int *cnt = S->cnt + (int64_t)tid * (S->tmax + 1);
+    cig_pick_t *pick = S->pick + S->base[i];
+    int near = 0, j, m = 0;
+    S->n_of[i] = 0;
+    if (k == 0 || !S->seqs[i].oseq) return;
+    if (!(opt->flag & MEM_F_ALL)) {
+        memcpy(tmp, a, sizeof(mem_alnreg_t) * k);
+        mem_mark_primary_se(opt, k, tmp, S->n_processed + i);
+        memset(cnt, 0, sizeof(int) * k);
+        for (j = 0; j < k; ++j) {
+            const int r = tmp[j].secondary_all;
+            if (r >= 0 && tmp[j].score >= tmp[r].score * opt->XA_drop_ratio) ++cnt[r];
+        }
+        a = tmp;
+        for (j = 0; j < k; ++j) near += a[j].score >= a[0].score * opt->XA_drop_ratio;
+    }
+    for (j = 0; j < k; ++j) {
+        const mem_alnreg_t *p = &a[j];
+        if (!cig_eligible(opt, &S->seqs[i], p)) continue;
+        if (!(opt->flag & MEM_F_ALL) && p->secondary >= 0) {
+            const int r = p->secondary_all;
+            const int xa = r >= 0 && p->score >= a[r].score * opt->XA_drop_ratio && cnt[r] <= opt->max_XA_hits;
+            const int pair = (opt->flag & MEM_F_PE) && near <= CIG_PAIR_NEAR &&
+                             p->score >= a[0].score * opt->XA_drop_ratio;
+            if (!xa && !pair) continue;
+        }
+        pick[m].rb = p->rb, pick[m].re = p->re, pick[m].qb = p->qb, pick[m].qe = p->qe;
+        pick[m].truesc = p->truesc, pick[m].w = p->w, pick[m].read = i;
+        ++m;
+    }
+    S->n_of[i] = m;
+}
+
 static cig_pick_t *cig_select(const mem_opt_t *opt, int n, const bseq1_t *seqs, const mem_alnreg_v *regs,
                               int64_t n_processed, int64_t *n_pick)
 {
-    int64_t m = 0, cap = 0;
-    cig_pick_t *pick = 0;
-    mem_alnreg_t *tmp = 0;
-    int *cnt = 0, i, j, tmax = 0;
+    cig_sel_t S;
+    int64_t *base = (int64_t *)malloc(sizeof(int64_t) * (n + 1)), m = 0;
+    int i, tmax = 0;
+    base[0] = 0;
     for (i = 0; i < n; ++i) {
-        cap += regs[i].n;
+        base[i + 1] = base[i] + regs[i].n;
         tmax = (int)regs[i].n > tmax ? (int)regs[i].n : tmax;
     }
-    pick = (cig_pick_t *)malloc(sizeof(cig_pick_t) * (cap + 1));
-    tmp = (mem_alnreg_t *)malloc(sizeof(mem_alnreg_t) * (tmax + 1));
-    cnt = (int *)malloc(sizeof(int) * (tmax + 1));
-    for (i = 0; i < n; ++i) {
-        const int k = (int)regs[i].n;
-        const mem_alnreg_t *a = regs[i].a;
-        int near = 0;
-        if (k == 0 || !seqs[i].oseq) continue;
-        if (!(opt->flag & MEM_F_ALL)) {
-            memcpy(tmp, a, sizeof(mem_alnreg_t) * k);
-            mem_mark_primary_se(opt, k, tmp, n_processed + i);
-            memset(cnt, 0, sizeof(int) * k);
-            for (j = 0; j < k; ++j) {
-                const int r = tmp[j].secondary_all;
-                if (r >= 0 && tmp[j].score >= tmp[r].score * opt->XA_drop_ratio) ++cnt[r];
-            }
-            a = tmp;
-            for (j = 0; j < k; ++j) near += a[j].score >= a[0].score * opt->XA_drop_ratio;
-        }
-        for (j = 0; j < k; ++j) {
-            const mem_alnreg_t *p = &a[j];
-            if (!cig_eligible(opt, &seqs[i], p)) continue;
-            if (!(opt->flag & MEM_F_ALL) && p->secondary >= 0) {
-                const int r = p->secondary_all;
-                const int xa = r >= 0 && p->score >= a[r].score * opt->XA_drop_ratio && cnt[r] <= opt->max_XA_hits;
-                const int pair = (opt->flag & MEM_F_PE) && near <= CIG_PAIR_NEAR &&
-                                 p->score >= a[0].score * opt->XA_drop_ratio;
-                if (!xa && !pair) continue;
-            }
-            pick[m].rb = p->rb, pick[m].re = p->re, pick[m].qb = p->qb, pick[m].qe = p->qe;
-            pick[m].truesc = p->truesc, pick[m].w = p->w, pick[m].read = i;
-            ++m;
-        }
+    S.opt = opt, S.seqs = seqs, S.regs = regs, S.n_processed = n_processed, S.base = base, S.tmax = tmax;
+    S.n_of = (int *)malloc(sizeof(int) * (n + 1));
+    S.pick = (cig_pick_t *)malloc(sizeof(cig_pick_t) * (base[n] + 1));
+    S.tmp = (mem_alnreg_t *)malloc(sizeof(mem_alnreg_t) * (tmax + 1) * glue_threads(opt->n_threads));
+    S.cnt = (int *)malloc(sizeof(int) * (tmax + 1) * glue_threads(opt->n_threads));
+    glue_for(opt->n_threads, n, cig_select1, &S);
+    for (i = 0; i < n; ++i) {                           /* in read order, as one pass would leave them */
+        if (S.n_of[i] && m != base[i]) memmove(&S.pick[m], &S.pick[base[i]], sizeof(cig_pick_t) * S.n_of[i]);
+        m += S.n_of[i];
     }
-    free(tmp);
-    free(cnt);
+    free(S.tmp); free(S.cnt); free(S.n_of); free(base);
     *n_pick = m;
-    return pick;
+    return S.pick;
+}
+
+typedef struct {
+    const mem_opt_t *opt;
+    const bseq1_t *seqs;
+    const cig_pick_t *pick;
+} cig_pack_t;
+
+/* job k: its band and its query bytes at the offsets set beforehand */
+static void cig_pack1(void *data, int64_t k, int tid)
+{
+    const cig_pack_t *P = (const cig_pack_t *)data;
+    const mem_opt_t *opt = P->opt;
+    const cig_pick_t *a = &P->pick[k];
+    const bseq1_t *s = &P->seqs[a->read];
+    bsb_cigar_job_t *jb = &g_cig.jobs[k];
+    uint8_t *q = g_cig.qbuf + jb->qoff, *oq = g_cig.obuf + jb->ooff;
+    const int l = a->qe - a->qb;
+    int w2, tmp, x;
+    (void)tid;
+    /* the band of mem_reg2aln's first bwa_gen_cigar2 call (bwamem.c:1219-1227) */
+    tmp = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_del, opt->e_del);
+    w2 = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_ins, opt->e_ins);
+    w2 = w2 > tmp ? w2 : tmp;
+    if (w2 > opt->w) w2 = w2 < a->w ? w2 : a->w;
+    w2 = w2 < opt->w << 2 ? w2 : opt->w << 2;
+    jb->rb = a->rb, jb->re = a->re, jb->l_query = l, jb->w = w2;
+    /* the nt4 query from qb and the original read from its start, as mem_reg2aln
+     * hands them over (bwamem.c:1211-1216, 1228) */
+    for (x = 0; x < l; ++x) {
+        const int c = (uint8_t)s->seq[a->qb + x];
+        q[x] = c < 5 ? c : nst_nt4_table[c];
+    }
+    for (x = 0; x < l; ++x) {
+        const int c = x < s->l_seq ? (uint8_t)s->oseq[x] : 4;
+        oq[x] = c < 5 ? c : nst_nt4_table[c];
+    }
 }
 
 int mem_gen_cigar_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *bns, int n, const bseq1_t *seqs,
                               const mem_alnreg_v *regs, int64_t n_processed)
 {
     bsb_align_opt_t o;
-    int64_t n_jobs = 0, qn = 0, on = 0, cap = 0, used = 0, k, t, n_pick = 0;
+    cig_pack_t P;
+    int64_t n_jobs, qn = 0, on = 0, cap = 0, used = 0, k, t, n_pick = 0;
     int rc;
     cig_pick_t *pick;
     cig_clear();
     pick = cig_select(opt, n, seqs, regs, n_processed, &n_pick);
-    for (k = 0; k < n_pick; ++k) {
-        const cig_pick_t *a = &pick[k];
-        ++n_jobs, qn += a->qe - a->qb, on += a->qe - a->qb;
-        cap += 14 * ((a->qe - a->qb) + (a->re - a->rb)) + 48;
-    }
+    n_jobs = n_pick;
     if (n_jobs == 0) {
         free(pick);
         return 0;
     }
     g_cig.jobs = (bsb_cigar_job_t *)malloc(sizeof(bsb_cigar_job_t) * n_jobs);
+    for (k = 0; k < n_pick; ++k) {
+        const cig_pick_t *a = &pick[k];
+        g_cig.jobs[k].qoff = qn, g_cig.jobs[k].ooff = on;
+        qn += a->qe - a->qb, on += a->qe - a->qb;
+        cap += 14 * ((a->qe - a->qb) + (a->re - a->rb)) + 48;
+    }
     g_cig.out = (bsb_cigar_out_t *)malloc(sizeof(bsb_cigar_out_t) * n_jobs);
     g_cig.qbuf = (uint8_t *)malloc(qn + 1);
     g_cig.obuf = (uint8_t *)malloc(on + 1);
     g_cig.blob = (uint8_t *)malloc(cap + 64);
-    qn = on = 0;
-    for (k = 0; k < n_pick; ++k) {
-        const cig_pick_t *a = &pick[k];
-        const bseq1_t *s = &seqs[a->read];
-        bsb_cigar_job_t *jb;
-        int l, w2, tmp, x;
-        l = a->qe - a->qb;
-        /* the band of mem_reg2aln's first bwa_gen_cigar2 call (bwamem.c:1219-1227) */
-        tmp = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_del, opt->e_del);
-        w2 = glue_infer_bw(l, (int)(a->re - a->rb), a->truesc, opt->a, opt->o_ins, opt->e_ins);
-        w2 = w2 > tmp ? w2 : tmp;
-        if (w2 > opt->w) w2 = w2 < a->w ? w2 : a->w;
-        w2 = w2 < opt->w << 2 ? w2 : opt->w << 2;
-        jb = &g_cig.jobs[k];
-        jb->rb = a->rb, jb->re = a->re, jb->l_query = l, jb->w = w2;
-        /* the nt4 query from qb and the original read from its start, as mem_reg2aln
-         * hands them over (bwamem.c:1211-1216, 1228) */
-        jb->qoff = qn, jb->ooff = on;
-        for (x = 0; x < l; ++x) {
-            const int c = (uint8_t)s->seq[a->qb + x];
-            g_cig.qbuf[qn++] = c < 5 ? c : nst_nt4_table[c];
-        }
-        for (x = 0; x < l; ++x) {
-            const int c = x < s->l_seq ? (uint8_t)s->oseq[x] : 4;
-            g_cig.obuf[on++] = c < 5 ? c : nst_nt4_table[c];
-        }
-    }
+    P.opt = opt, P.seqs = seqs, P.pick = pick;
+    glue_for(opt->n_threads, n_pick, cig_pack1, &P);
     free(pick);
     mem_opt_to_bsb(opt, &o);
     rc = bsb_gen_cigar_batch(ctx, &o, bns->crick_l, (int32_t)n_jobs, g_cig.jobs, g_cig.qbuf, qn, g_cig.obuf, on,
