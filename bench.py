@@ -395,8 +395,10 @@ def pipeline_rrbs(ctx, batch_bases=10_000_000, cpu_reads=4_000):
     seed.align_regs(ctx, *sub(*batches[0]), opt, dedup=True)     # warm-up
     t0 = time.perf_counter()
     first = None
+    stages = dict.fromkeys(seed.ALIGN_STAGES, 0.0)
     for a, b in batches:
         regs, roff = seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        add_stages(stages, ctx)
         if first is None:
             first = (regs, roff)
     gpu_s = time.perf_counter() - t0
@@ -427,6 +429,7 @@ def pipeline_rrbs(ctx, batch_bases=10_000_000, cpu_reads=4_000):
         "cpu_oracle_threads": threads, "cpu_sample_reads": cpu_reads,
         "regions_bit_exact_vs_oracle_on_sample": exact,
         "workload_prep_s": round(prep_s, 1),
+        "stage_ms_per_batch": {k: round(v / len(batches), 3) for k, v in stages.items()},
     }
 
 
@@ -489,6 +492,13 @@ def seeding_roofline(ctx, reads, offs, reps=5):
             "peak_source": f"HBM copy bandwidth, {src} (MEASURED_PEAKS.json hbm_gbs)"}
 
 
+def add_stages(acc, ctx):
+    """Adds the last alignment batch's device ms per stage (bsb_last_stage_ms) to acc."""
+    from bsbolt_gb300 import seed
+    for k, v in seed.last_stage_ms(ctx).items():
+        acc[k] += v
+
+
 def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
     """Seeds -> regions on the 100 Mb reference (200 MB BWT, larger than L2) in -K 10M-base
     batches, against the CPU oracle on a sample."""
@@ -508,8 +518,10 @@ def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
     seed.align_regs(ctx, *sub(*batches[0]))                      # warm-up
     t0 = time.perf_counter()
     first = None
+    stages = dict.fromkeys(seed.ALIGN_STAGES, 0.0)
     for lo, hi in batches:
         regs, roff = seed.align_regs(ctx, *sub(lo, hi))
+        add_stages(stages, ctx)
         if first is None:
             first = (regs, roff)
     gpu_s = time.perf_counter() - t0
@@ -544,6 +556,7 @@ def pipeline_ref100mb(ctx, batch_pairs=33_333, cpu_pairs=2_000):
         "cpu_oracle_threads": threads, "cpu_sample_pairs": cpu_pairs,
         "regions_bit_exact_vs_oracle_on_sample": exact,
         "workload_prep_s": round(prep_s, 1),
+        "stage_ms_per_batch": {k: round(v / len(batches), 3) for k, v in stages.items()},
         "seeding_roofline_one_batch": seeding,
     }
 
@@ -751,8 +764,10 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
     seed.align_regs(ctx, *sub(*batches[0]), opt, dedup=True)       # warm-up
     t0 = time.perf_counter()
     first = None
+    stages = dict.fromkeys(seed.ALIGN_STAGES, 0.0)
     for a, b in batches:
         regs, roff = seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        add_stages(stages, ctx)
         if first is None:
             first = (regs, roff)
     gpu_s = time.perf_counter() - t0
@@ -824,19 +839,25 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
     pred = model.forward(torch.from_numpy(fev).cuda()).cpu().numpy()
 
     def run_all():
-        out = []
+        out, stages = [], dict.fromkeys(seed.ALIGN_STAGES, 0.0)
         t = time.perf_counter()
         for a, b in batches:
             out.append(seed.align_regs(ctx, *sub(a, b), opt, dedup=True))
-        return time.perf_counter() - t, out
+            for k, v in seed.last_stage_ms(ctx).items():
+                stages[k] += v
+        return time.perf_counter() - t, out, stages
     run_all()                                      # warm-up
-    plain_s, plain_out = run_all()
+    plain_s, plain_out, plain_st = run_all()
     seed.set_read_cost_model(ctx, model)
     try:
         run_all()
-        learned_s, learned_out = run_all()
+        learned_s, learned_out, learned_st = run_all()
     finally:
         seed.set_read_cost_model(ctx, None)
+    # Amdahl: the read order changes only the chain2aln stage, so even a zero-time chain2aln
+    # caps the gain at total / (total - chain2aln)
+    tot = sum(plain_st.values())
+    cap = tot / max(tot - plain_st["chain2aln"], 1e-9)
     same = all(np.array_equal(x[1], y[1]) and np.array_equal(x[0], y[0]) for x, y in zip(plain_out, learned_out))
     # the plain order's key: chains per read (feature 1 is log1p(kept chains) / 4)
     plain_key = np.expm1(fev[:, 1] * 4)
@@ -852,6 +873,11 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
         "plain_reads_per_s": round(n_reads / plain_s, 1), "learned_reads_per_s": round(n_reads / learned_s, 1),
         "plain_s": round(plain_s, 4), "learned_s": round(learned_s, 4),
         "speedup_learned_vs_plain": round(plain_s / learned_s, 4), "regions_identical": bool(same),
+        "stage_ms_all_batches": {"plain": {k: round(v, 2) for k, v in plain_st.items()},
+                                 "learned": {k: round(v, 2) for k, v in learned_st.items()}},
+        "chain2aln_share_plain": round(plain_st["chain2aln"] / max(tot, 1e-9), 4),
+        "chain2aln_speedup_learned_vs_plain": round(plain_st["chain2aln"] / max(learned_st["chain2aln"], 1e-9), 4),
+        "max_gain_from_any_read_order": round(cap, 4),
     }
 
 

@@ -23,6 +23,7 @@ BSB_ENOINDEX = -7
 BSB_ECAPACITY = -8
 BSB_NOALLOC_MAX_JOBS = 1 << 18
 BSB_NUM_TILES = 61
+BSB_ALIGN_STAGES = 6
 BSB_TILE_MAP_LEN = 1025
 
 # every extern "C" symbol include/bsbgpu.h declares
@@ -36,6 +37,8 @@ EXPORTS = (
     "bsb_cost_features", "bsb_mlp_forward", "bsb_mlp_backward", "bsb_mlp_adam",
     "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
     "bsb_index_upload_opac", "bsb_gen_cigar_batch", "bsb_align2_batch",
+    "bsb_last_seed_extensions", "bsb_read_cost_log", "bsb_last_read_costs", "bsb_set_read_cost_model",
+    "bsb_build_suffix_array", "bsb_last_stage_ms",
 )
 
 
@@ -172,6 +175,8 @@ def load(path: str = LIB_PATH):
     L.bsb_align2_batch.argtypes = [P, P, P, I64, P, I64, P]
     L.bsb_last_seed_extensions.argtypes = [P, ctypes.POINTER(I64)]
     L.bsb_last_seed_extensions.restype = I32
+    L.bsb_last_stage_ms.argtypes = [P, P, I32]
+    L.bsb_last_stage_ms.restype = I32
     L.bsb_read_cost_log.argtypes = [P, I32]
     L.bsb_read_cost_log.restype = I32
     L.bsb_last_read_costs.argtypes = [P, ctypes.c_int32, P, P]

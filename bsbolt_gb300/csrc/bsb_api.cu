@@ -98,6 +98,7 @@ int bsb_ctx_create(int device, bsb_ctx **out)
     for (int t = 0; t < 4 * BSB_MAX_CHUNKS && ok; ++t)
         ok = cudaEventCreateWithFlags(&ctx->chunk_ev[t], (t & 3) < 2 ? cudaEventDisableTiming : cudaEventDefault) ==
              cudaSuccess;
+    for (int t = 0; t <= BSB_ALIGN_STAGES && ok; ++t) ok = cudaEventCreate(&ctx->stage_ev[t]) == cudaSuccess;
     for (int a = 0; a < BSB_AUX_STREAMS && ok; ++a)
         ok = cudaStreamCreateWithFlags(&ctx->ms.aux[a], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&ctx->ms.join[a], cudaEventDisableTiming) == cudaSuccess;
@@ -137,6 +138,8 @@ void bsb_ctx_destroy(bsb_ctx *ctx)
         if (ctx->tile_ev[t]) cudaEventDestroy(ctx->tile_ev[t]);
     for (int t = 0; t < 4 * BSB_MAX_CHUNKS; ++t)
         if (ctx->chunk_ev[t]) cudaEventDestroy(ctx->chunk_ev[t]);
+    for (int t = 0; t <= BSB_ALIGN_STAGES; ++t)
+        if (ctx->stage_ev[t]) cudaEventDestroy(ctx->stage_ev[t]);
     for (int a = 0; a < BSB_AUX_STREAMS; ++a) {
         if (ctx->ms.aux[a]) cudaStreamDestroy(ctx->ms.aux[a]);
         if (ctx->ms.join[a]) cudaEventDestroy(ctx->ms.join[a]);

@@ -78,6 +78,9 @@ struct bsb_ctx {
     // host entry chunks: copy-in done, extension done, extension start/end marks
     cudaEvent_t chunk_ev[4 * BSB_MAX_CHUNKS] = {};
     int n_chunks = 0;
+    // marks between the stages of the last alignment batch (bsb_last_stage_ms)
+    cudaEvent_t stage_ev[BSB_ALIGN_STAGES + 1] = {};
+    bool stage_valid = false;
     // chaining / chain-extension scratch
     void *arena0 = nullptr, *arena1 = nullptr, *arena2 = nullptr;
     size_t arena0_bytes = 0, arena1_bytes = 0, arena2_bytes = 0;

@@ -1407,6 +1407,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         cudaError_t e = bsb_sa_launch_ctx(ctx, rows, R, pos);
         if (e != cudaSuccess) return bsb_cuda(ctx, e, "SA rows");
     }
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->stage_ev[2], st), "stage mark"))) return rc;
     AlnOpt ao;
     ao.a = o->a; ao.o_del = o->o_del; ao.e_del = o->e_del; ao.o_ins = o->o_ins; ao.e_ins = o->e_ins;
     ao.w = o->w; ao.zdrop = o->zdrop; ao.pen_clip5 = o->pen_clip5; ao.pen_clip3 = o->pen_clip3;
@@ -1432,6 +1433,7 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         (rc = seed_sw_filter(ctx, o, B, n_reads, h_min_hsp, d_reads, d_read_off, d_seed_off, roff, cseeds, cchains,
                              n_chains, ao)))
         return rc;
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->stage_ev[3], st), "stage mark"))) return rc;
     int *order = (int *)(A + o_order);
     int *ocnt = (int *)(A + o_order + al(sizeof(int) * (n_reads + 1)));
     // per-read features / extension cells for the learned read order (kept for bsb_last_read_costs)
@@ -1483,7 +1485,9 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     else
         chain2aln_kernel<32><<<ctx->n_sm * 2, 128, 0, st>>>(ao, P, B, n_reads, d_reads, d_read_off, d_seed_off, roff,
                                                              cseeds, cchains, n_chains, srt, regs, n_regs, ctrl + 1, order, rcells_out);
-    if ((rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets"))) return rc;
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->stage_ev[4], st), "stage mark")) ||
+        (rc = bsb_cuda(ctx, scan_i32_i64(n_regs, n_reads, reg_off, scan_tmp, st), "region offsets")))
+        return rc;
     const int cgrid = (int)((n_reads + 3) / 4) < ctx->n_sm * 16 ? (int)((n_reads + 3) / 4) : ctx->n_sm * 16;
     compact_regs<<<cgrid, 128, 0, st>>>(regs, d_seed_off, roff, n_reads, n_regs, reg_off, regs_out);
     if (dedup) {
@@ -1505,7 +1509,8 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return bsb_cuda(ctx, e, "chain/extension launch");
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(n_regs_total, reg_off + n_reads, 8, cudaMemcpyDeviceToHost, st), "reg total")))
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(ctx->stage_ev[5], st), "stage mark")) ||
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(n_regs_total, reg_off + n_reads, 8, cudaMemcpyDeviceToHost, st), "reg total")))
         return rc;
     if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "chain/extension"))) return rc;
     *d_regs_out = regs_out;
@@ -1561,14 +1566,19 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
     bsb_intv_t *d_seeds = (bsb_intv_t *)ctx->d_out;
     std::vector<int64_t> rel(n_reads + 1);
     for (int r = 0; r <= n_reads; ++r) rel[r] = offs[r] - offs[0];
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_reads, seqs + offs[0], total, cudaMemcpyHostToDevice, ctx->stream), "H2D reads")))
+    ctx->stage_valid = false;
+    cudaEvent_t *const sev = ctx->stage_ev;
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(sev[0], ctx->stream), "stage mark")) ||
+        (rc = bsb_cuda(ctx, cudaMemcpyAsync(d_reads, seqs + offs[0], total, cudaMemcpyHostToDevice, ctx->stream), "H2D reads")))
         return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_offs, rel.data(), off_b, cudaMemcpyHostToDevice, ctx->stream), "H2D offsets")))
         return rc;
     bsb_seed_opt_t so;
     so.min_seed_len = o->min_seed_len; so.split_factor = o->split_factor;
     so.split_width = o->split_width; so.max_mem_intv = o->max_mem_intv;
-    if ((rc = bsb_seed_batch_device(ctx, &so, n_reads, d_reads, d_offs, total, max_len, d_seeds, d_seed_off))) return rc;
+    if ((rc = bsb_seed_batch_device(ctx, &so, n_reads, d_reads, d_offs, total, max_len, d_seeds, d_seed_off)) ||
+        (rc = bsb_cuda(ctx, cudaEventRecord(sev[1], ctx->stream), "stage mark")))
+        return rc;
     int64_t n_seeds = 0;
     int ctrl[2] = {0, 0};
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&n_seeds, d_seed_off + n_reads, 8, cudaMemcpyDeviceToHost, ctx->stream), "seed total")))
@@ -1594,7 +1604,11 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
         (rc = bsb_cuda(ctx, cudaMemcpyAsync(regs, d_regs, sizeof(bsb_reg_t) * n_regs, cudaMemcpyDeviceToHost, ctx->stream),
                        "D2H regions")))
         return rc;
-    return bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "align batch");
+    if ((rc = bsb_cuda(ctx, cudaEventRecord(sev[BSB_ALIGN_STAGES], ctx->stream), "stage mark")) ||
+        (rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "align batch")))
+        return rc;
+    ctx->stage_valid = true;
+    return 0;
 }
 
 extern "C" int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, const uint8_t *seqs,
@@ -1610,6 +1624,14 @@ extern "C" int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int3
     if (o && !(o->mask_level_redun >= 0.f && o->mask_level_redun <= 1.f))
         return bsb_fail(ctx, BSB_EINVAL, "mask_level_redun must lie in [0, 1]");
     return align_batch(ctx, o, n_reads, seqs, offs, regs, max_regs, regs_off, true);
+}
+
+extern "C" int bsb_last_stage_ms(const bsb_ctx *ctx, float *ms, int n)
+{
+    if (!ctx || !ms || n < 0 || !ctx->stage_valid) return BSB_EINVAL;
+    for (int k = 0; k < BSB_ALIGN_STAGES && k < n; ++k)
+        if (cudaEventElapsedTime(&ms[k], ctx->stage_ev[k], ctx->stage_ev[k + 1]) != cudaSuccess) return BSB_ECUDA;
+    return 0;
 }
 
 extern "C" int bsb_read_cost_log(bsb_ctx *ctx, int enable)

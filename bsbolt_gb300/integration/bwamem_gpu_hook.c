@@ -54,6 +54,8 @@ typedef struct {
 static bsb_ctx *g_hook_ctx;
 static long g_hook_calls;
 static double g_t_align, g_t_cigar, g_t_sw, g_t_worker2;
+static double g_t_start, g_t_load, g_t_ctx, g_t_upload;   /* index load, context, upload (wall) */
+static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
 static double hook_now(void)
@@ -81,6 +83,9 @@ static void hook_report(void)
             (long long)g_cig_served, (long long)g_cig_passed);
     fprintf(stderr, "[bsb_gpu] matesw jobs kept %lld served %lld\n", (long long)g_sw_kept, (long long)g_sw_served);
     fprintf(stderr, "[bsb_gpu] region buffer regrown %lld\n", (long long)mem_align_regrown());
+    fprintf(stderr, "[bsb_gpu] start-up: index load %.3f s, GPU context %.3f s (beside the load), index upload %.3f s; "
+            "%ld batches; %.3f s from the load to exit\n", g_t_load, g_t_ctx, g_t_upload, g_batches,
+            g_t_start > 0 ? hook_now() - g_t_start : 0.);
 }
 
 static void hook_fail(bsb_ctx *ctx, int rc, const char *what)
@@ -123,8 +128,10 @@ static int g_boot_rc;
 
 static void *hook_boot(void *arg)
 {
+    const double t0 = hook_now();
     (void)arg;
     g_boot_rc = bsb_ctx_create(hook_device(), &g_hook_ctx);
+    g_t_ctx = hook_now() - t0;
     return 0;
 }
 
@@ -135,12 +142,17 @@ bwaidx_t *__wrap_bwa_idx_load(const char *hint, int which)
     pthread_t boot;
     bwaidx_t *idx;
     const int full = (which & BWA_IDX_ALL) == BWA_IDX_ALL;   /* bwa mem's load (fastmap.c:321) */
+    const double t0 = hook_now();
     int started = full && !g_hook_ctx && pthread_create(&boot, 0, hook_boot, 0) == 0;
+    double t1;
     idx = __real_bwa_idx_load(hint, which);
     if (started) {
+        g_t_start = t0, g_t_load = hook_now() - t0;
         pthread_join(boot, 0);
         if (g_boot_rc) hook_fail(g_hook_ctx, g_boot_rc, "GPU context");
+        t1 = hook_now();
         if (idx) hook_upload(idx->bwt, idx->bns, idx->pac, idx->opac);
+        g_t_upload = hook_now() - t1;
     }
     return idx;
 }
@@ -171,7 +183,7 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
         t1 = hook_now();
         if ((rc = mem_gen_cigar_prepass_gpu(g_hook_ctx, w->opt, w->bns, n_reads, w->seqs, w->regs, w->n_processed)))
             hook_fail(g_hook_ctx, rc, "GPU CIGAR pre-pass");
-        g_t_align += t1 - t0, g_t_cigar += hook_now() - t1, g_reads += n_reads;
+        g_t_align += t1 - t0, g_t_cigar += hook_now() - t1, g_reads += n_reads, ++g_batches;
         return;
     }
     /* worker2: w->pes now holds mem_pestat's (or -I's) insert-size model */

@@ -49,6 +49,16 @@ def last_extensions(ctx: Context) -> int:
     return int(v.value)
 
 
+ALIGN_STAGES = ("seeding", "sa_rows", "chains", "chain2aln", "dedup", "d2h")
+
+
+def last_stage_ms(ctx: Context) -> dict:
+    """Device ms per stage of the context's last alignment batch (bsb_last_stage_ms)."""
+    ms = np.zeros(_lib.BSB_ALIGN_STAGES, np.float32)
+    _lib.check(ctx.handle, ctx.L.bsb_last_stage_ms(ctx.handle, _ptr(ms), len(ms)))
+    return dict(zip(ALIGN_STAGES, (float(x) for x in ms)))
+
+
 def sa_batch(ctx: Context, rows: np.ndarray) -> np.ndarray:
     rows = np.ascontiguousarray(rows, dtype=np.uint64)
     pos = np.zeros(len(rows), np.uint64)

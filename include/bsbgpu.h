@@ -261,9 +261,11 @@ typedef struct {
  * mem_chain2aln with its ksw_extend2 calls.  Reads are nt4 codes (already
  * converted, as mem_align1_core sees them); read r's regions, in the
  * reference's order, are regs[regs_off[r] .. regs_off[r+1]).  Needs an index
- * with pac and contig table.  Supports reads up to 1023 bp whose length keeps
- * mem_flt_chained_seeds a no-op (bwamem.c:606), indexes without ALT contigs
- * (BSBolt writes none).  Host buffers; synchronous.  When the batch has more
+ * with pac and contig table.  Supports reads up to 1023 bp (longer ones return
+ * BSB_ETOOLONG), with the seed-level Smith-Waterman filter of
+ * mem_flt_chained_seeds (bwamem.c:602-619) run for every read length it applies
+ * to, and indexes without ALT contigs (BSBolt writes none).  Host buffers;
+ * synchronous.  When the batch has more
  * regions than max_regs (mem_chain samples up to max_occ rows per seed, so a
  * read in a large repeat family can have hundreds), nothing is written to regs,
  * regs_off is filled all the same (regs_off[n_reads] = the regions needed) and
@@ -285,6 +287,16 @@ int bsb_align_regs_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_rea
 int bsb_mem_align1_batch(bsb_ctx *ctx, const bsb_align_opt_t *opt, int32_t n_reads,
                          const uint8_t *seqs, const int64_t *offs,
                          bsb_reg_t *regs, int64_t max_regs, int64_t *regs_off);
+
+/* Device time of the stages of the last bsb_align_regs_batch / bsb_mem_align1_batch
+ * call, in ms, between marks recorded on the library's stream: [0] read upload and
+ * seeding (mem_collect_intv), [1] suffix-array rows (bwt_sa), [2] chaining, chain
+ * filter and the seed-level SW filter, [3] read order and mem_chain2aln, [4] region
+ * compaction and mem_sort_dedup_patch, [5] region download.  Gaps where the stream
+ * waits for the host (the two count read-backs) fall into the stage after them.
+ * Writes min(n, BSB_ALIGN_STAGES) values; BSB_EINVAL before any batch. */
+#define BSB_ALIGN_STAGES 6
+int bsb_last_stage_ms(const bsb_ctx *ctx, float *ms, int n);
 
 /* ---- CIGAR, MD and methylation strings: bwa_gen_cigar2 ------------------ */
 

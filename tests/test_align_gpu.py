@@ -215,3 +215,18 @@ def test_learned_read_order_changes_no_region(gpu_ctx, indexes):
     finally:
         seed.set_read_cost_model(gpu_ctx, None)
     assert np.array_equal(plain_off, learned_off) and np.array_equal(plain, learned)
+
+
+def test_stage_times_of_the_last_batch(gpu_ctx, indexes):
+    """bsb_last_stage_ms: six non-negative stage times of the last alignment batch whose sum
+    is within the host's wall time of that call."""
+    import time
+    seed.load_index(gpu_ctx, indexes["plain"])
+    g = np.load(os.path.join(GOLDEN, "reads_L5.npz"))
+    t0 = time.perf_counter()
+    seed.align_regs(gpu_ctx, g["reads"], g["read_off"], opt_from(g["opts"]), dedup=True)
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    st = seed.last_stage_ms(gpu_ctx)
+    assert list(st) == list(seed.ALIGN_STAGES)
+    assert all(v >= 0 for v in st.values()) and st["seeding"] > 0 and st["chain2aln"] > 0
+    assert sum(st.values()) <= wall_ms + 1.0
