@@ -148,3 +148,11 @@ const uint8_t *ksw_default_tile_map();
 int ksw_tile_shape(int t, int *G, int *C);
 // Set of tile shapes a map uses (bit t).
 uint64_t ksw_map_tiles(const uint8_t *map);
+
+// (int)((double)num / e + 1.), the band caps of ksw.c:400-407, bwamem.c:627-628 and
+// bwa.c:234-235, in integer arithmetic (e >= 1, |num| < 2^30): (num + e) / e truncated
+// toward zero.  Where (num + e) / e
+// is an integer both forms are exact; elsewhere it lies at least 1/e from every integer, far
+// beyond the rounding of the two double operations, so truncation agrees.  (Double division
+// runs on the GPU's slow fp64 pipe.)
+__host__ __device__ __forceinline__ int band_cap(int num, int e) { return (num + e) / e; }

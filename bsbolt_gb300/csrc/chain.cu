@@ -546,8 +546,8 @@ struct ReadRefAcc {
 
 __device__ __forceinline__ int cal_max_gap(const AlnOpt &o, int qlen)         // bwamem.c:625-632
 {
-    const int l_del = (int)((double)(qlen * o.a - o.o_del) / o.e_del + 1.);
-    const int l_ins = (int)((double)(qlen * o.a - o.o_ins) / o.e_ins + 1.);
+    const int l_del = band_cap(qlen * o.a - o.o_del, o.e_del);
+    const int l_ins = band_cap(qlen * o.a - o.o_ins, o.e_ins);
     int l = l_del > l_ins ? l_del : l_ins;
     l = l > 1 ? l : 1;
     return l < o.w << 1 ? l : o.w << 1;

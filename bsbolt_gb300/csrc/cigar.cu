@@ -87,8 +87,8 @@ __device__ __forceinline__ JobPlan plan_job(const CigarParams &P, const bsb_ciga
     p.big = p.l > kSmemLen || p.rlen > kSmemLen;
     if (!p.ungapped) {
         const int l = p.l, m0 = P.mat[0];
-        const int max_ins = (int)((double)(((l + 1) >> 1) * m0 - P.o_ins) / P.e_ins + 1.);
-        const int max_del = (int)((double)(((l + 1) >> 1) * m0 - P.o_del) / P.e_del + 1.);
+        const int max_ins = band_cap(((l + 1) >> 1) * m0 - P.o_ins, P.e_ins);
+        const int max_del = band_cap(((l + 1) >> 1) * m0 - P.o_del, P.e_del);
         int max_gap = max_ins > max_del ? max_ins : max_del;
         max_gap = max_gap > 1 ? max_gap : 1;
         const int dl = abs(p.rlen - l);

@@ -86,13 +86,13 @@ __device__ __forceinline__ KswResult ksw_warp(const KswParams &P, int qlen, int 
         Es[s] = 0;
     }
 
-    // band clamp with the reference's double arithmetic (ksw.c:399-407)
+    // band clamp (ksw.c:399-407)
     int w = w_in;
     {
-        int max_ins = (int)((double)(qlen * P.mat_max + end_bonus - o_ins) / e_ins + 1.);
+        int max_ins = band_cap(qlen * P.mat_max + end_bonus - o_ins, e_ins);
         max_ins = max_ins > 1 ? max_ins : 1;
         w = w < max_ins ? w : max_ins;
-        int max_del = (int)((double)(qlen * P.mat_max + end_bonus - o_del) / e_del + 1.);
+        int max_del = band_cap(qlen * P.mat_max + end_bonus - o_del, e_del);
         max_del = max_del > 1 ? max_del : 1;
         w = w < max_del ? w : max_del;
     }

@@ -104,10 +104,10 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
                 }
                 w = jb.w;                                                                  // ksw.c:399-407
                 {
-                    int max_ins = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_ins) / e_ins + 1.);
+                    int max_ins = band_cap(qlen * P.mat_max + jb.end_bonus - P.o_ins, e_ins);
                     max_ins = max_ins > 1 ? max_ins : 1;
                     w = w < max_ins ? w : max_ins;
-                    int max_del = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_del) / e_del + 1.);
+                    int max_del = band_cap(qlen * P.mat_max + jb.end_bonus - P.o_del, e_del);
                     max_del = max_del > 1 ? max_del : 1;
                     w = w < max_del ? w : max_del;
                 }

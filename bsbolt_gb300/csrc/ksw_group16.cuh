@@ -113,10 +113,10 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                 for (int u = 0; u < C2; ++u) Hs[u] = pk16(h_init[u], h_init[u + C2]), Es[u] = 0;
                 w = jb.w;                                                                  // ksw.c:399-407
                 {
-                    int max_ins = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_ins) / e_ins + 1.);
+                    int max_ins = band_cap(qlen * P.mat_max + jb.end_bonus - P.o_ins, e_ins);
                     max_ins = max_ins > 1 ? max_ins : 1;
                     w = w < max_ins ? w : max_ins;
-                    int max_del = (int)((double)(qlen * P.mat_max + jb.end_bonus - P.o_del) / e_del + 1.);
+                    int max_del = band_cap(qlen * P.mat_max + jb.end_bonus - P.o_del, e_del);
                     max_del = max_del > 1 ? max_del : 1;
                     w = w < max_del ? w : max_del;
                 }
