@@ -185,7 +185,7 @@ __device__ __forceinline__ KswResult ksw_warp(const KswParams &P, int qlen, int 
             const int H = __vimax3_s32(Mv[s], Es[s], F);
             const bool lt = j < end;
             if (lt) kmax = max(kmax, H * 1024 + j);     // ties keep the later column (ksw.c:437)
-            const int nE = lt ? En[s] : (j == end ? 0 : Es[s]);
+            const int nE = lt ? En[s] : 0;     // E beyond end is 0 at every row (ksw_group16.cuh, pass 2)
             Es[s] = nE;
             if (s > 0) {
                 const int nH = j <= end ? prevH : Hs[s];

@@ -203,7 +203,7 @@ __device__ __forceinline__ void ksw_group_run(const KswParams &P, const bsb_ext_
             const int H = __vimax3_s32(Mv[s], Es[s], F);
             const bool lt = s < rend;
             if (lt) kmax = max(kmax, H * 1024 + s);     // ties keep the later column (ksw.c:437)
-            const int nE = lt ? En[s] : (s == rend ? 0 : Es[s]);
+            const int nE = lt ? En[s] : 0;     // E beyond end is 0 at every row (ksw_group16.cuh, pass 2)
             Es[s] = nE;
             if (s > 0) {
                 const int nH = s <= rend ? prevH : Hs[s];

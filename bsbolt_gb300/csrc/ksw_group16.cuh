@@ -44,6 +44,12 @@ __host__ __device__ __forceinline__ constexpr uint32_t sext2_selector(int b, int
     return (uint32_t)b | ((uint32_t)b | 8u) << 4 | (uint32_t)(4 + c) << 8 | ((uint32_t)(4 + c) | 8u) << 12;
 }
 
+// sext2_selector(b, b) for a base b in 0..3 as one multiply-add: b * 0x1111 + 0xC480.
+__host__ __device__ __forceinline__ constexpr uint32_t sext2_same(uint32_t b) { return b * 0x1111u + 0xC480u; }
+static_assert(sext2_same(0) == sext2_selector(0, 0) && sext2_same(1) == sext2_selector(1, 1) &&
+              sext2_same(2) == sext2_selector(2, 2) && sext2_same(3) == sext2_selector(3, 3),
+              "the selector of a base");
+
 // 1 in a half where u < the half of t (t - u >= 1), else 0.
 __device__ __forceinline__ uint32_t below16(uint32_t t, int u)
 {
@@ -172,7 +178,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         uint32_t Mv[C2];
         uint32_t local = 0;
         if (!__any_sync(act, tc >= 4)) {
-            const uint32_t sel = sext2_selector(tc, tc);
+            const uint32_t sel = sext2_same((uint32_t)tc);
 #pragma unroll
             for (int u = 0; u < C2; ++u) {
                 const uint32_t sc = prmt2(prof[u], prof[u + C2], sel);
@@ -182,7 +188,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
                 Mv[u] = M;
             }
         } else {                               // some group has an N in the target
-            const uint32_t sel = sext2_selector(tc < 4 ? tc : 0, tc < 4 ? tc : 0);
+            const uint32_t sel = sext2_same(tc < 4 ? (uint32_t)tc : 0u);
 #pragma unroll
             for (int u = 0; u < C2; ++u) {
                 const uint32_t sc = tc < 4 ? prmt2(prof[u], prof[u + C2], sel)
@@ -206,14 +212,18 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
 
         // pass 2: F (the recurrence F(i,j+1) = max(F(i,j) - e_ins, max(M - oe_ins, 0)) of
         // ksw.c:446-447 from each half's carry-in), H, E(i+1,j), the row maximum key, and the
-        // new eh[] -- E(i+1, j) inside the band, 0 at end, kept beyond; H shifted one column
-        // up to end, kept beyond -- and the non-zero cells.  Column 0's shifted H needs the
-        // left lane's last column and column C2-1 of this lane, so it is finished after the loop.
+        // new eh[] -- E(i+1, j) inside the band, 0 from end on; H shifted one column up to end,
+        // kept beyond -- and the non-zero cells.  E beyond end is 0 in ksw_extend2 at every
+        // row: eh[end].e is set to 0 (ksw.c:449), the columns the band shrinks off are those
+        // past the last non-zero one (ksw.c:468), and the band's right edge moves at most
+        // one column a row past them; so "kept beyond end" and "0" agree for E.  (H beyond
+        // end can hold the first row's insertion run and is kept.)  Column 0's shifted H needs
+        // the left lane's last column and column C2-1 of this lane, so it is finished after the loop.
         const int rend = end - base;               // |rend| <= 1023: exact in 16 bits
         // per half: ltm(u) = [column < rend]; lem(u) = [column <= rend] = ltm(u - 1)
         const uint32_t t_lt = pk16(rend, rend - C2);
         uint32_t ltm_prev = below16(t_lt, -1) * 0xffffu;
-        uint32_t kmx = 0;                          // per half: max of H*16 + u over band columns
+        uint32_t kmx = 0, kprev = 0;               // per half: max of H*16 + u over band columns
         uint32_t F = pk16(carry, max(carry - e_ins * C2, f_lo_end));   // F entering each half
         uint32_t Hprev = 0, nE0 = 0, lem0 = 0, nzw = 0;
 #pragma unroll
@@ -224,24 +234,29 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
             F = __viaddmax_s16x2(F, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
             const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = ltm_prev;
             ltm_prev = ltm;
-            kmx = __vimax_s16x2_relu(kmx, (H & ltm) * 16u + pk16(u, u));   // ties: the later column
-            const uint32_t nE = (En & ltm) | (Eo & ~lem);
+            const uint32_t key = (H & ltm) * 16u + pk16(u, u);             // ties: the later column
+            if (u & 1) kmx = __vimax3_s16x2(kmx, kprev, key);              // two registers a step
+            else kprev = key;
+            const uint32_t nE = En & ltm;
             Es[u] = nE;
             if (u > 0) {
                 const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);
                 Hs[u] = nH;
-                nzw += __vimin_s16x2_relu(nH | nE, 0x00010001u) << u;     // distinct bits: + is |, one shift-add
+                // 1 in a half where nH or nE is non-zero (both >= 0, their sum < 2^15); the
+                // halves' bits are distinct, so + is |: one shift-add
+                nzw += __viaddmin_s16x2_relu(nH, nE, 0x00010001u) << u;
             } else {
                 nE0 = nE, lem0 = lem;
             }
             Hprev = H;
         }
+        if (C2 & 1) kmx = __vimax_s16x2_relu(kmx, kprev);
         int Hleft = __shfl_up_sync(act, hi16(Hprev), 1, G);
         if (gl == 0) Hleft = h1_init;
         {
             const uint32_t nH = (pk16(Hleft, lo16(Hprev)) & lem0) | (Hs[0] & ~lem0);
             Hs[0] = nH;
-            nzw += __vimin_s16x2_relu(nH | nE0, 0x00010001u);
+            nzw += __viaddmin_s16x2_relu(nH, nE0, 0x00010001u);
         }
         uint32_t nzb = (nzw & 0xffffu) | (nzw >> 16) << C2;
         nzb &= rend < 0 ? 0u : rend >= C - 1 ? 0xffffffffu : (2u << rend) - 1u;   // columns s <= rend
@@ -256,10 +271,18 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         // query end reached: eh[qlen].h == H(i, qlen-1), or h1 for an empty band at qlen (ksw.c:450-453)
         int hq = h1_init;
         if (__any_sync(act, !empty && end == qlen)) {
+            // register qu by a select tree on its bits (C2 - 1 selects)
             const int qu = q_slot < C2 ? q_slot : q_slot - C2;
-            uint32_t wsel = 0;
+            uint32_t v[C2];
 #pragma unroll
-            for (int u = 0; u < C2; ++u) wsel = u == qu ? Hs[u] : wsel;
+            for (int u = 0; u < C2; ++u) v[u] = Hs[u];
+#pragma unroll
+            for (int l = 0; (1 << l) < C2; ++l) {
+                const bool b = (qu >> l) & 1;
+#pragma unroll
+                for (int a = 0; a + (1 << l) < C2; a += 2 << l) v[a] = b ? v[a + (1 << l)] : v[a];
+            }
+            const uint32_t wsel = v[0];
             const int hsel = q_slot < C2 ? lo16(wsel) : hi16(wsel);
             const int h1 = __shfl_sync(act, hsel, q_lane, G);
             hq = empty ? hq : h1;

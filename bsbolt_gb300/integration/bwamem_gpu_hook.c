@@ -23,7 +23,10 @@
  * A library error ends the run through err_fatal, as the reference ends on
  * its own errors.  BSB_GPU_DEVICE picks the CUDA device (default 0);
  * BSB_GPU_STATS=1 prints, at exit, how many CIGAR and rescue calls the GPU
- * results answered, and the time spent in the GPU passes.
+ * results answered, and the time spent in the GPU passes.  For that account,
+ * bseq_read (the input step of fastmap.c:process) and new_samSorter /
+ * samSorter_delete (which open and close its output step) are wrapped too,
+ * as pass-throughs that only take the time.
  */
 #include <pthread.h>
 #include <stdio.h>
@@ -55,6 +58,7 @@ static bsb_ctx *g_hook_ctx;
 static long g_hook_calls;
 static double g_t_align, g_t_cigar, g_t_sw, g_t_worker2;
 static double g_t_start, g_t_load, g_t_ctx, g_t_upload;   /* index load, context, upload (wall) */
+static double g_t_read, g_t_write, g_t_write0;             /* input and output steps of the pipeline */
 static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
@@ -86,6 +90,45 @@ static void hook_report(void)
     fprintf(stderr, "[bsb_gpu] start-up: index load %.3f s, GPU context %.3f s (beside the load), index upload %.3f s; "
             "%ld batches; %.3f s from the load to exit\n", g_t_load, g_t_ctx, g_t_upload, g_batches,
             g_t_start > 0 ? hook_now() - g_t_start : 0.);
+    fprintf(stderr, "[bsb_gpu] host steps: reading and converting the reads %.3f s, SAM output %.3f s "
+            "(each beside the other steps of the pipeline)\n", g_t_read, g_t_write);
+}
+
+/* ---- timing-only pass-throughs: the pipeline's input and output steps ---- */
+
+static int hook_stats(void)
+{
+    static int on = -1;
+    if (on < 0) on = getenv("BSB_GPU_STATS") != 0;
+    return on;
+}
+
+bseq1_t *__real_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
+                          int undirectional, float substitution_proportion);
+
+bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
+                          int undirectional, float substitution_proportion)
+{
+    const double t0 = hook_stats() ? hook_now() : 0.;
+    bseq1_t *r = __real_bseq_read(chunk_size, n_, ks1_, ks2_, s, conversion, undirectional, substitution_proportion);
+    if (t0 > 0.) g_t_read += hook_now() - t0;
+    return r;
+}
+
+struct samSorter;
+struct samSorter *__real_new_samSorter(bseq1_t *first_read);
+void __real_samSorter_delete(struct samSorter *ss);
+
+struct samSorter *__wrap_new_samSorter(bseq1_t *first_read)
+{
+    if (hook_stats()) g_t_write0 = hook_now();
+    return __real_new_samSorter(first_read);
+}
+
+void __wrap_samSorter_delete(struct samSorter *ss)
+{
+    __real_samSorter_delete(ss);
+    if (hook_stats() && g_t_write0 > 0.) g_t_write += hook_now() - g_t_write0;
 }
 
 static void hook_fail(bsb_ctx *ctx, int rc, const char *what)
