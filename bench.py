@@ -706,8 +706,7 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
     """The human-scale configuration at 1 Gb (the largest whose index text, 4e9 symbols with both
     conversions and strands, keeps 32-bit suffix ranks): 8 contigs of 125 Mb, GC 41 %, CpG 1 %,
     45 % interspersed repeats (families 300 bp - 6 kb, 2-20 % divergence).  The index is built
-    with the suffix array sorted on the GPU and held in HBM (64-symbol occurrence sectors, full
-    SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
+    with the suffix array sorted on the GPU and held in HBM (occurrence sectors, full SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
     every pair, parity against the oracle on a sample, and stock bwa against bwa_gpu from SAM."""
     import oracle
     from bsbolt_gb300 import _lib, index, seed, synth
@@ -788,7 +787,9 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
     res.update({
         "workload": f"1 Gb bisulfite reference (8x125 Mb, 45% repeats), {n_reads // 2} directional pairs: 70% 2x150, "
                     f"30% 2x250, 2% adapter read-through; -K 10M batches ({len(batches)}); BWA defaults",
-        "seq_len": int(bi.l_pac) * 2, "occ_layout": "64-symbol sectors (0.5 B/row)",
+        "seq_len": int(bi.l_pac) * 2,
+        "occ_layout": ("64-symbol sectors (0.5 B/row)" if os.environ.get("BSB_OCC_SYM64") == "1"
+                       else "32-symbol sectors (1 B/row)"),
         "gpu_mem_align1_read_pairs_per_s": round(n_reads / 2 / gpu_s, 1),
         "cpu_oracle_read_pairs_per_s": round(ns / 2 / cpu_s, 1), "cpu_oracle_sample_reads": ns,
         "regions_bit_exact_vs_oracle_on_sample": exact})
@@ -846,14 +847,22 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
             for k, v in seed.last_stage_ms(ctx).items():
                 stages[k] += v
         return time.perf_counter() - t, out, stages
-    run_all()                                      # warm-up
-    plain_s, plain_out, plain_st = run_all()
-    seed.set_read_cost_model(ctx, model)
-    try:
-        run_all()
-        learned_s, learned_out, learned_st = run_all()
-    finally:
-        seed.set_read_cost_model(ctx, None)
+    def with_model(m):
+        seed.set_read_cost_model(ctx, m)
+        try:
+            return run_all()
+        finally:
+            seed.set_read_cost_model(ctx, None)
+    run_all()                                      # warm-up of both orders
+    with_model(model)
+    # plain, learned, plain, learned: each order's time is the mean of its two passes, so a
+    # drift of the GPU or the host over the runs falls on both alike
+    runs = [run_all(), with_model(model), run_all(), with_model(model)]
+    plain_out, learned_out = runs[0][1], runs[1][1]
+    plain_s = (runs[0][0] + runs[2][0]) / 2
+    learned_s = (runs[1][0] + runs[3][0]) / 2
+    plain_st = {k: (runs[0][2][k] + runs[2][2][k]) / 2 for k in seed.ALIGN_STAGES}
+    learned_st = {k: (runs[1][2][k] + runs[3][2][k]) / 2 for k in seed.ALIGN_STAGES}
     # Amdahl: the read order changes only the chain2aln stage, so even a zero-time chain2aln
     # caps the gain at total / (total - chain2aln)
     tot = sum(plain_st.values())

@@ -67,6 +67,12 @@ int mem_matesw_prepass_gpu(bsb_ctx *ctx, const mem_opt_t *opt, const bntseq_t *b
 /* Jobs kept by the last mate-rescue pre-pass, and calls answered from them since. */
 void mem_matesw_stats(int64_t *kept, int64_t *served);
 
+/* bseq_read (bwa.c:73-143) with the same results, plain four-line FASTQ parsed with a line scan
+ * and the entries built on threads; anything else goes to the reference's bseq_read, reached
+ * as __real_bseq_read (link with -Wl,--wrap=bseq_read; bseq_fast.c). */
+bseq1_t *bseq_read_fast(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
+                        int undirectional, float substitution_proportion);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,10 +23,11 @@
  * A library error ends the run through err_fatal, as the reference ends on
  * its own errors.  BSB_GPU_DEVICE picks the CUDA device (default 0);
  * BSB_GPU_STATS=1 prints, at exit, how many CIGAR and rescue calls the GPU
- * results answered, and the time spent in the GPU passes.  For that account,
- * bseq_read (the input step of fastmap.c:process) and new_samSorter /
- * samSorter_delete (which open and close its output step) are wrapped too,
- * as pass-throughs that only take the time.
+ * results answered, and the time spent in the GPU passes.  bseq_read, the input
+ * step of fastmap.c:process, is answered by bseq_read_fast (bseq_fast.c: the same
+ * reads, parsed with a line scan and built on threads); it and new_samSorter /
+ * samSorter_delete (which open and close the output step) also take the time of
+ * those steps for the account.
  */
 #include <pthread.h>
 #include <stdio.h>
@@ -94,7 +95,7 @@ static void hook_report(void)
             "(each beside the other steps of the pipeline)\n", g_t_read, g_t_write);
 }
 
-/* ---- timing-only pass-throughs: the pipeline's input and output steps ---- */
+/* ---- the pipeline's input and output steps (timed for the account) ---- */
 
 static int hook_stats(void)
 {
@@ -103,14 +104,11 @@ static int hook_stats(void)
     return on;
 }
 
-bseq1_t *__real_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
-                          int undirectional, float substitution_proportion);
-
 bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
                           int undirectional, float substitution_proportion)
 {
     const double t0 = hook_stats() ? hook_now() : 0.;
-    bseq1_t *r = __real_bseq_read(chunk_size, n_, ks1_, ks2_, s, conversion, undirectional, substitution_proportion);
+    bseq1_t *r = bseq_read_fast(chunk_size, n_, ks1_, ks2_, s, conversion, undirectional, substitution_proportion);
     if (t0 > 0.) g_t_read += hook_now() - t0;
     return r;
 }
@@ -186,7 +184,12 @@ bwaidx_t *__wrap_bwa_idx_load(const char *hint, int which)
     bwaidx_t *idx;
     const int full = (which & BWA_IDX_ALL) == BWA_IDX_ALL;   /* bwa mem's load (fastmap.c:321) */
     const double t0 = hook_now();
-    int started = full && !g_hook_ctx && pthread_create(&boot, 0, hook_boot, 0) == 0;
+    int started;
+    /* SAM leaves through stdout (samSorter's fputs, bs_sorter.cpp:98-124): a 16 MB buffer instead
+     * of stdio's block-sized one, set before the header is printed (fastmap.c, after this load) */
+    static char *sam_buf;
+    if (full && !sam_buf && (sam_buf = (char *)malloc(1 << 24)) != 0) setvbuf(stdout, sam_buf, _IOFBF, 1 << 24);
+    started = full && !g_hook_ctx && pthread_create(&boot, 0, hook_boot, 0) == 0;
     double t1;
     idx = __real_bwa_idx_load(hint, which);
     if (started) {

@@ -205,3 +205,11 @@ void __wrap_kt_for(int n_threads, void (*func)(void *, long, int), void *data, l
     }
     __real_kt_for(n_threads, func, data, n);
 }
+
+/* The input step of fastmap.c:process through the glue's FASTQ reader (bseq_fast.c), so that
+ * the SAM tests run it against the stock reader's output. */
+bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
+                          int undirectional, float substitution_proportion)
+{
+    return bseq_read_fast(chunk_size, n_, ks1_, ks2_, s, conversion, undirectional, substitution_proportion);
+}

@@ -169,3 +169,74 @@ def test_glue_long_reads_and_seed_sw_filter(pe):
     extra = ["-W", "5", "-L", "5,5"]
     ref = run_mem(BWA, fa, p1, p2, extra)
     assert len(ref) >= 3000 and run_mem(GLUE, fa, p1, p2, extra) == ref
+
+
+def _records(path):
+    with open(path) as f:
+        lines = f.read().splitlines()
+    return [lines[i:i + 4] for i in range(0, len(lines), 4)]
+
+
+def _write(path, recs, eol="\n", final_eol=True, blank_after=None, header=None, fasta=False, opener=open):
+    out = []
+    for k, r in enumerate(recs):
+        h = header(k, r[0]) if header else r[0]
+        if fasta:
+            s = r[1]
+            out += [">" + h[1:]] + [s[i:i + 60] for i in range(0, len(s), 60)]
+        else:
+            out += [h, r[1], "+", r[3]]
+        if blank_after is not None and k == blank_after:
+            out.append("")
+    text = eol.join(out) + (eol if final_eol else "")
+    with opener(path, "wt") as f:
+        f.write(text)
+
+
+@pytest.mark.parametrize("variant", ["comments", "double_readno_undirectional", "crlf", "fasta_multiline",
+                                     "blank_line", "no_final_newline", "gzip", "small_batches_se_undirectional"])
+def test_glue_fastq_reader_matches_kseq(pe, tmp_path, variant):
+    """bwa_glue reads its input with the glue's FASTQ reader (bseq_fast.c: a line scan and entries
+    built on threads, the reference's bseq_read for anything else); the SAM must equal the stock
+    reader's for headers with comments (-C copies them into the SAM), names ending in /1/2 under
+    -z (bseq_read trims a duplicated read's name twice), CRLF line ends, multi-line FASTA, a blank
+    line between records, a file without its last newline, gzip input, and many small batches."""
+    import gzip
+    fa, r1, r2 = pe[:3]
+    a, b = _records(r1)[:1500], _records(r2)[:1500]
+    p1, p2 = str(tmp_path / "a.fq"), str(tmp_path / "b.fq")
+    extra = ["-L", "5,5"]
+    if variant == "comments":
+        hdr = lambda k, h: f"{h}\tBC:Z:ACGT{k % 7}  x"          # noqa: E731
+        _write(p1, a, header=hdr)
+        _write(p2, b, header=hdr)
+        extra += ["-C"]
+    elif variant == "double_readno_undirectional":
+        hdr = lambda k, h: h[:-2] + "/7" + h[-2:]                # noqa: E731  r1/7/1: trimmed to r1/7, then r1
+        _write(p1, a, header=hdr)
+        _write(p2, b, header=hdr)
+        extra += ["-z"]
+    elif variant == "crlf":
+        _write(p1, a, eol="\r\n")
+        _write(p2, b, eol="\r\n")
+    elif variant == "fasta_multiline":
+        _write(p1, a, fasta=True)
+        _write(p2, b, fasta=True)
+    elif variant == "blank_line":
+        _write(p1, a, blank_after=900)
+        _write(p2, b, blank_after=900)
+    elif variant == "no_final_newline":
+        _write(p1, a, final_eol=False)
+        _write(p2, b, final_eol=False)
+    elif variant == "gzip":
+        p1, p2 = p1 + ".gz", p2 + ".gz"
+        _write(p1, a, opener=gzip.open)
+        _write(p2, b, opener=gzip.open)
+    else:
+        _write(p1, a + b)
+        p2 = None
+        extra += ["-z", "-K", "20000"]
+    reads = [p1] + ([p2] if p2 else [])
+    ref = sam_sets.run_mem(BWA, fa, reads, extra)
+    glue = sam_sets.run_mem(GLUE, fa, reads, extra)
+    assert len(ref) >= 3000 and glue == ref
