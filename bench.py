@@ -839,13 +839,24 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
     train_s = time.perf_counter() - t0
     pred = model.forward(torch.from_numpy(fev).cuda()).cpu().numpy()
 
-    def run_all():
+    # every batch's logged cells: the keys of the exact-cost order (what a perfect model
+    # would predict), which bounds the gain of any learned order
+    seed.read_cost_log(ctx, True)
+    exact_keys = []
+    for a, b in batches:
+        seed.align_regs(ctx, *sub(a, b), opt, dedup=True)
+        exact_keys.append(seed.last_read_costs(ctx, b - a)[1])
+    seed.read_cost_log(ctx, False)
+
+    def run_all(exact=False):
         out, stages = [], dict.fromkeys(seed.ALIGN_STAGES, 0.0)
         t = time.perf_counter()
-        for a, b in batches:
+        for k, (a, b) in enumerate(batches):
+            if exact:
+                seed.set_read_order_keys(ctx, exact_keys[k])
             out.append(seed.align_regs(ctx, *sub(a, b), opt, dedup=True))
-            for k, v in seed.last_stage_ms(ctx).items():
-                stages[k] += v
+            for key, v in seed.last_stage_ms(ctx).items():
+                stages[key] += v
         return time.perf_counter() - t, out, stages
     def with_model(m):
         seed.set_read_cost_model(ctx, m)
@@ -853,21 +864,25 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
             return run_all()
         finally:
             seed.set_read_cost_model(ctx, None)
-    run_all()                                      # warm-up of both orders
+    run_all()                                      # warm-up of the three orders
     with_model(model)
-    # plain, learned, plain, learned: each order's time is the mean of its two passes, so a
-    # drift of the GPU or the host over the runs falls on both alike
-    runs = [run_all(), with_model(model), run_all(), with_model(model)]
-    plain_out, learned_out = runs[0][1], runs[1][1]
-    plain_s = (runs[0][0] + runs[2][0]) / 2
-    learned_s = (runs[1][0] + runs[3][0]) / 2
-    plain_st = {k: (runs[0][2][k] + runs[2][2][k]) / 2 for k in seed.ALIGN_STAGES}
-    learned_st = {k: (runs[1][2][k] + runs[3][2][k]) / 2 for k in seed.ALIGN_STAGES}
+    run_all(exact=True)
+    # plain, learned, exact, twice: each order's time is the mean of its two passes, so a
+    # drift of the GPU or the host over the runs falls on all alike
+    runs = [run_all(), with_model(model), run_all(exact=True), run_all(), with_model(model), run_all(exact=True)]
+    plain_out, learned_out, exact_out = runs[0][1], runs[1][1], runs[2][1]
+    plain_s = (runs[0][0] + runs[3][0]) / 2
+    learned_s = (runs[1][0] + runs[4][0]) / 2
+    exact_s = (runs[2][0] + runs[5][0]) / 2
+    plain_st = {k: (runs[0][2][k] + runs[3][2][k]) / 2 for k in seed.ALIGN_STAGES}
+    learned_st = {k: (runs[1][2][k] + runs[4][2][k]) / 2 for k in seed.ALIGN_STAGES}
+    exact_st = {k: (runs[2][2][k] + runs[5][2][k]) / 2 for k in seed.ALIGN_STAGES}
     # Amdahl: the read order changes only the chain2aln stage, so even a zero-time chain2aln
     # caps the gain at total / (total - chain2aln)
     tot = sum(plain_st.values())
     cap = tot / max(tot - plain_st["chain2aln"], 1e-9)
-    same = all(np.array_equal(x[1], y[1]) and np.array_equal(x[0], y[0]) for x, y in zip(plain_out, learned_out))
+    same = all(np.array_equal(x[1], y[1]) and np.array_equal(x[0], y[0]) and np.array_equal(x[1], z[1]) and
+               np.array_equal(x[0], z[0]) for x, y, z in zip(plain_out, learned_out, exact_out))
     # the plain order's key: chains per read (feature 1 is log1p(kept chains) / 4)
     plain_key = np.expm1(fev[:, 1] * 4)
     return {
@@ -886,6 +901,11 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
                                  "learned": {k: round(v, 2) for k, v in learned_st.items()}},
         "chain2aln_share_plain": round(plain_st["chain2aln"] / max(tot, 1e-9), 4),
         "chain2aln_speedup_learned_vs_plain": round(plain_st["chain2aln"] / max(learned_st["chain2aln"], 1e-9), 4),
+        "exact_cost_order": {"reads_per_s": round(n_reads / exact_s, 1), "s": round(exact_s, 4),
+                             "speedup_vs_plain": round(plain_s / exact_s, 4),
+                             "chain2aln_speedup_vs_plain": round(plain_st["chain2aln"] /
+                                                                 max(exact_st["chain2aln"], 1e-9), 4),
+                             "stage_ms_all_batches": {k: round(v, 2) for k, v in exact_st.items()}},
         "max_gain_from_any_read_order": round(cap, 4),
     }
 

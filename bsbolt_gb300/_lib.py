@@ -38,7 +38,7 @@ EXPORTS = (
     "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
     "bsb_index_upload_opac", "bsb_gen_cigar_batch", "bsb_align2_batch",
     "bsb_last_seed_extensions", "bsb_read_cost_log", "bsb_last_read_costs", "bsb_set_read_cost_model",
-    "bsb_build_suffix_array", "bsb_last_stage_ms",
+    "bsb_build_suffix_array", "bsb_last_stage_ms", "bsb_set_read_order_keys",
 )
 
 
@@ -175,6 +175,8 @@ def load(path: str = LIB_PATH):
     L.bsb_align2_batch.argtypes = [P, P, P, I64, P, I64, P]
     L.bsb_last_seed_extensions.argtypes = [P, ctypes.POINTER(I64)]
     L.bsb_last_seed_extensions.restype = I32
+    L.bsb_set_read_order_keys.argtypes = [P, P, I32]
+    L.bsb_set_read_order_keys.restype = I32
     L.bsb_last_stage_ms.argtypes = [P, P, I32]
     L.bsb_last_stage_ms.restype = I32
     L.bsb_read_cost_log.argtypes = [P, I32]

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/bsbgpu.h"
 
@@ -93,6 +94,7 @@ struct bsb_ctx {
     // the last batch when logging
     const void *read_model = nullptr;
     int read_log = 0, rc_n = 0;
+    std::vector<int32_t> order_keys;   // per-read order keys for the next alignment batch
     void *rc_buf = nullptr;
     size_t rc_bytes = 0;
 };

@@ -1440,8 +1440,10 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
     float *d_feat = nullptr;
     int64_t *d_rcells = nullptr;
     int32_t *d_rkey = nullptr;
-    const bool learned = ctx->read_model != nullptr, logging = ctx->read_log != 0;
-    if (learned || logging) {
+    const bool keyed = !ctx->order_keys.empty() && (int64_t)ctx->order_keys.size() == n_reads;
+    if (!keyed) ctx->order_keys.clear();          // keys for another batch size are dropped
+    const bool learned = ctx->read_model != nullptr && !keyed, logging = ctx->read_log != 0;
+    if (learned || logging || keyed) {
         const size_t nr = (size_t)n_reads;
         if ((rc = bsb_ensure(ctx, &ctx->rc_buf, &ctx->rc_bytes, al(32 * nr) + al(8 * nr) + al(4 * nr) + 256,
                              "read costs")))
@@ -1450,14 +1452,23 @@ static int bsb_align_regs_run(bsb_ctx *ctx, const bsb_align_opt_t *o, int n_read
         d_rcells = (int64_t *)((char *)ctx->rc_buf + al(32 * nr));
         d_rkey = (int32_t *)((char *)ctx->rc_buf + al(32 * nr) + al(8 * nr));
         const int fb = (int)std::min<int64_t>((n_reads + 127) / 128, (int64_t)ctx->n_sm * 8);
-        read_features_kernel<<<fb, 128, 0, st>>>(ao, B, n_reads, d_reads, d_read_off, d_seed_off, roff, cseeds, cchains,
-                                                 n_chains, d_feat);
+        if (learned || logging)
+            read_features_kernel<<<fb, 128, 0, st>>>(ao, B, n_reads, d_reads, d_read_off, d_seed_off, roff, cseeds,
+                                                     cchains, n_chains, d_feat);
         ctx->rc_n = logging ? n_reads : 0;
     }
     {
         const int ob = (int)((n_reads + 255) / 256) < ctx->n_sm * 4 ? (int)((n_reads + 255) / 256) : ctx->n_sm * 4;
         if ((rc = bsb_cuda(ctx, cudaMemsetAsync(ocnt, 0, sizeof(int) * 2 * kOrderBins, st), "read order"))) return rc;
-        if (learned) {       // predicted cells of every read, most expensive first
+        if (keyed) {         // the caller's keys, once (the copy is done before they are cleared)
+            if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_rkey, ctx->order_keys.data(), sizeof(int32_t) * (size_t)n_reads,
+                                                    cudaMemcpyHostToDevice, st), "read order keys")) ||
+                (rc = bsb_cuda(ctx, cudaStreamSynchronize(st), "read order keys")))
+                return rc;
+            ctx->order_keys.clear();
+            order_hist_key<<<ob, 256, 0, st>>>(d_rkey, n_reads, ocnt);
+            order_scatter_key<<<ob, 256, 0, st>>>(d_rkey, n_reads, ocnt, ocnt + kOrderBins, order);
+        } else if (learned) {   // predicted cells of every read, most expensive first
             if ((rc = bsb_mlp_forward(ctx, (const bsb_mlp_weights_t *)ctx->read_model, d_feat, n_reads, nullptr,
                                       d_rkey)))
                 return rc;
@@ -1663,5 +1674,13 @@ extern "C" int bsb_set_read_cost_model(bsb_ctx *ctx, const bsb_mlp_weights_t *d_
 {
     if (!ctx) return BSB_EINVAL;
     ctx->read_model = d_w;
+    return 0;
+}
+
+extern "C" int bsb_set_read_order_keys(bsb_ctx *ctx, const int32_t *keys, int32_t n)
+{
+    if (!ctx) return BSB_EINVAL;
+    if (n < 0 || (n > 0 && !keys)) return bsb_fail(ctx, BSB_EINVAL, "read order keys: NULL or negative count");
+    ctx->order_keys.assign(keys, keys + (n > 0 ? n : 0));
     return 0;
 }

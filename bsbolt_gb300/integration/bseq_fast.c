@@ -219,7 +219,29 @@ typedef struct {
     int64_t next, n;
 } fq_build_t;
 
-/* kseq2bseq1 (bwa.c:44-71) of entry i */
+/* The strings of entry i, allocated on the calling thread: BWA frees them in its output step
+ * (bs_sorter.cpp:152-156) on the pipeline thread that read the batch, and a free into another
+ * thread's heap arena takes that arena's lock, against the worker threads allocating there. */
+static void fq_alloc1(fq_build_t *B, int64_t i)
+{
+    const fq_entry_t *e = &B->ent[i];
+    const fq_rec_t *r = &B->rec[e->stream][e->rec];
+    bseq1_t *s = &B->seqs[i];
+    memset(s, 0, sizeof *s);
+    s->name = (char *)malloc((size_t)e->name_l + 1);
+    s->comment = r->cmt_l ? (char *)malloc((size_t)r->cmt_l + 1) : 0;
+    s->seq = (char *)malloc((size_t)r->seq_l + 1);
+    s->qual = r->seq_l ? (char *)malloc((size_t)r->seq_l + 1) : 0;
+    s->oseq = B->conversion ? (char *)malloc((size_t)r->seq_l + 1) : 0;
+}
+
+static void fq_copy(char *d, const char *src, int l)
+{
+    memcpy(d, src, (size_t)l);
+    d[l] = 0;
+}
+
+/* kseq2bseq1 (bwa.c:44-71) of entry i, into the strings fq_alloc1 made */
 static void fq_build1(fq_build_t *B, int64_t i)
 {
     const fq_entry_t *e = &B->ent[i];
@@ -227,11 +249,10 @@ static void fq_build1(fq_build_t *B, int64_t i)
     const char *b = B->st[e->stream]->buf;
     bseq1_t *s = &B->seqs[i];
     int k;
-    memset(s, 0, sizeof *s);
-    s->name = fq_dup(b + r->name, e->name_l);
-    s->comment = r->cmt_l ? fq_dup(b + r->cmt, r->cmt_l) : 0;
-    s->seq = fq_dup(b + r->seq, r->seq_l);
-    s->qual = r->seq_l ? fq_dup(b + r->qual, r->seq_l) : 0;
+    fq_copy(s->name, b + r->name, e->name_l);
+    if (s->comment) fq_copy(s->comment, b + r->cmt, r->cmt_l);
+    fq_copy(s->seq, b + r->seq, r->seq_l);
+    if (s->qual) fq_copy(s->qual, b + r->qual, r->seq_l);
     s->l_seq = r->seq_l;
     s->first = e->first;
     s->read_group = e->read_group;
@@ -239,7 +260,7 @@ static void fq_build1(fq_build_t *B, int64_t i)
     s->conversion = B->conversion;
     s->id = (int)i;
     if (B->conversion) {
-        s->oseq = fq_dup(b + r->seq, r->seq_l);
+        fq_copy(s->oseq, b + r->seq, r->seq_l);
         bsConversion(s->seq, s->subsitution_pattern, s->l_seq);
         for (k = 0; k < s->l_seq; ++k) s->oseq[k] = s->oseq[k] < 4 ? s->oseq[k] : nst_nt4_table[(int)s->oseq[k]];
     }
@@ -392,6 +413,10 @@ bseq1_t *bseq_read_fast(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int
     if (!seqs) goto undo;
     B.st[0] = st1, B.st[1] = st2, B.rec[0] = v1.a, B.rec[1] = v2.a, B.ent = ent, B.seqs = seqs;
     B.conversion = conversion, B.next = 0, B.n = n;
+    {
+        int64_t i;
+        for (i = 0; i < n; ++i) fq_alloc1(&B, i);
+    }
     fq_build_all(&B);
     free(v1.a); free(v2.a); free(ent);
     *n_ = (int)n;

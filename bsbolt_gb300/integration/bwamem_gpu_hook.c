@@ -25,9 +25,9 @@
  * BSB_GPU_STATS=1 prints, at exit, how many CIGAR and rescue calls the GPU
  * results answered, and the time spent in the GPU passes.  bseq_read, the input
  * step of fastmap.c:process, is answered by bseq_read_fast (bseq_fast.c: the same
- * reads, parsed with a line scan and built on threads); it and new_samSorter /
- * samSorter_delete (which open and close the output step) also take the time of
- * those steps for the account.
+ * reads, parsed with a line scan and built on threads), and the samSorter calls of its
+ * output step by sam_out.c (the same bytes, copied on threads, one write per batch);
+ * both also take the time of those steps for the account.
  */
 #include <pthread.h>
 #include <stdio.h>
@@ -115,17 +115,38 @@ bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, i
 
 struct samSorter;
 struct samSorter *__real_new_samSorter(bseq1_t *first_read);
+void __real_samSorter_processRead(struct samSorter *ss, bseq1_t *read);
+void __real_samSorter_processEnd(struct samSorter *ss);
 void __real_samSorter_delete(struct samSorter *ss);
+
+/* the output step: sam_out.c in place of samSorter (BSB_SAM_WRITER=0: the reference's) */
+static char g_sam_out_token;
 
 struct samSorter *__wrap_new_samSorter(bseq1_t *first_read)
 {
     if (hook_stats()) g_t_write0 = hook_now();
+    if (sam_out_enabled()) {
+        sam_out_begin(first_read);
+        return (struct samSorter *)&g_sam_out_token;
+    }
     return __real_new_samSorter(first_read);
+}
+
+void __wrap_samSorter_processRead(struct samSorter *ss, bseq1_t *read)
+{
+    if (ss == (struct samSorter *)&g_sam_out_token) sam_out_read(read);
+    else __real_samSorter_processRead(ss, read);
+}
+
+void __wrap_samSorter_processEnd(struct samSorter *ss)
+{
+    if (ss == (struct samSorter *)&g_sam_out_token) sam_out_end();
+    else __real_samSorter_processEnd(ss);
 }
 
 void __wrap_samSorter_delete(struct samSorter *ss)
 {
-    __real_samSorter_delete(ss);
+    if (ss != (struct samSorter *)&g_sam_out_token) __real_samSorter_delete(ss);
     if (hook_stats() && g_t_write0 > 0.) g_t_write += hook_now() - g_t_write0;
 }
 

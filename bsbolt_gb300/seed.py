@@ -49,6 +49,16 @@ def last_extensions(ctx: Context) -> int:
     return int(v.value)
 
 
+def set_read_order_keys(ctx: Context, keys) -> None:
+    """Orders the next alignment batch (of len(keys) reads) by these per-read keys, larger
+    first (bsb_set_read_order_keys); None clears."""
+    if keys is None:
+        _lib.check(ctx.handle, ctx.L.bsb_set_read_order_keys(ctx.handle, None, 0))
+        return
+    k = np.ascontiguousarray(np.minimum(np.asarray(keys, np.int64), 2**31 - 1), dtype=np.int32)
+    _lib.check(ctx.handle, ctx.L.bsb_set_read_order_keys(ctx.handle, _ptr(k), len(k)))
+
+
 ALIGN_STAGES = ("seeding", "sa_rows", "chains", "chain2aln", "dedup", "d2h")
 
 

@@ -417,10 +417,15 @@ int bsb_mlp_adam(bsb_ctx *ctx, bsb_mlp_weights_t *d_w, float *d_master, float *d
  *   bsb_last_read_costs: copies them out for the last batch (n_reads must match; host
  *     buffers of n_reads * BSB_MLP_FEATURES floats and n_reads int64);
  *   bsb_set_read_cost_model(ctx, d_w): order later batches by the model's prediction
- *     (weights in device memory, kept by the caller); NULL restores the chain-count order. */
+ *     (weights in device memory, kept by the caller); NULL restores the chain-count order;
+ *   bsb_set_read_order_keys(ctx, keys, n): order the next batch, which must hold n reads,
+ *     by the caller's per-read keys (host int32, larger first, in the model's half-octave
+ *     bins) -- e.g. the cells a log recorded, the order a perfect model would give, which
+ *     bounds what any learned order can gain; used once, over the model; n = 0 clears. */
 int bsb_read_cost_log(bsb_ctx *ctx, int enable);
 int bsb_last_read_costs(bsb_ctx *ctx, int32_t n_reads, float *feat, int64_t *cells);
 int bsb_set_read_cost_model(bsb_ctx *ctx, const bsb_mlp_weights_t *d_w);
+int bsb_set_read_order_keys(bsb_ctx *ctx, const int32_t *keys, int32_t n);
 
 /* ---- extension without any device allocation ---------------------------- */
 

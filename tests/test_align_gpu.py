@@ -215,6 +215,11 @@ def test_learned_read_order_changes_no_region(gpu_ctx, indexes):
     finally:
         seed.set_read_cost_model(gpu_ctx, None)
     assert np.array_equal(plain_off, learned_off) and np.array_equal(plain, learned)
+    # the exact-cost order (the logged cells as keys, once) and the reverse of it
+    for keys in (cells, -cells):
+        seed.set_read_order_keys(gpu_ctx, keys)
+        exact, exact_off = seed.align_regs(gpu_ctx, reads, offs, opt, dedup=True)
+        assert np.array_equal(plain_off, exact_off) and np.array_equal(plain, exact)
 
 
 def test_stage_times_of_the_last_batch(gpu_ctx, indexes):
