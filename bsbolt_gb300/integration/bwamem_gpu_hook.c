@@ -60,6 +60,7 @@ static long g_hook_calls;
 static double g_t_align, g_t_cigar, g_t_sw, g_t_worker2;
 static double g_t_start, g_t_load, g_t_ctx, g_t_upload;   /* index load, context, upload (wall) */
 static double g_t_read, g_t_write, g_t_write0;             /* input and output steps of the pipeline */
+static double g_t_first_read, g_t_last_write;              /* the pipeline's span */
 static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
@@ -93,6 +94,11 @@ static void hook_report(void)
             g_t_start > 0 ? hook_now() - g_t_start : 0.);
     fprintf(stderr, "[bsb_gpu] host steps: reading and converting the reads %.3f s, SAM output %.3f s "
             "(each beside the other steps of the pipeline)\n", g_t_read, g_t_write);
+    if (g_t_first_read > 0.)
+        fprintf(stderr, "[bsb_gpu] timeline: load to first read %.3f s, first read to last SAM output %.3f s "
+                "(alignment steps %.3f s of it), last output to exit %.3f s\n", g_t_first_read - g_t_start,
+                g_t_last_write - g_t_first_read, g_t_align + g_t_cigar + g_t_sw + g_t_worker2,
+                hook_now() - g_t_last_write);
 }
 
 /* ---- the pipeline's input and output steps (timed for the account) ---- */
@@ -108,6 +114,7 @@ bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, i
                           int undirectional, float substitution_proportion)
 {
     const double t0 = hook_stats() ? hook_now() : 0.;
+    if (t0 > 0. && g_t_first_read == 0.) g_t_first_read = t0;
     bseq1_t *r = bseq_read_fast(chunk_size, n_, ks1_, ks2_, s, conversion, undirectional, substitution_proportion);
     if (t0 > 0.) g_t_read += hook_now() - t0;
     return r;
@@ -147,7 +154,7 @@ void __wrap_samSorter_processEnd(struct samSorter *ss)
 void __wrap_samSorter_delete(struct samSorter *ss)
 {
     if (ss != (struct samSorter *)&g_sam_out_token) __real_samSorter_delete(ss);
-    if (hook_stats() && g_t_write0 > 0.) g_t_write += hook_now() - g_t_write0;
+    if (hook_stats() && g_t_write0 > 0.) g_t_last_write = hook_now(), g_t_write += g_t_last_write - g_t_write0;
 }
 
 static void hook_fail(bsb_ctx *ctx, int rc, const char *what)
