@@ -61,6 +61,7 @@ static double g_t_align, g_t_cigar, g_t_sw, g_t_worker2;
 static double g_t_start, g_t_load, g_t_ctx, g_t_upload;   /* index load, context, upload (wall) */
 static double g_t_read, g_t_write, g_t_write0;             /* input and output steps of the pipeline */
 static double g_t_first_read, g_t_last_write;              /* the pipeline's span */
+static double g_t_pipe_end, g_t_idx_free, g_t_out_close;    /* after it: index freed, SAM file closed */
 static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
@@ -96,9 +97,11 @@ static void hook_report(void)
             "(each beside the other steps of the pipeline)\n", g_t_read, g_t_write);
     if (g_t_first_read > 0.)
         fprintf(stderr, "[bsb_gpu] timeline: load to first read %.3f s, first read to last SAM output %.3f s "
-                "(alignment steps %.3f s of it), last output to exit %.3f s\n", g_t_first_read - g_t_start,
+                "(alignment steps %.3f s of it), last output to exit %.3f s (pipeline end %.3f s after it, "
+                "index freed in %.3f s, SAM file closed in %.3f s)\n", g_t_first_read - g_t_start,
                 g_t_last_write - g_t_first_read, g_t_align + g_t_cigar + g_t_sw + g_t_worker2,
-                hook_now() - g_t_last_write);
+                hook_now() - g_t_last_write, g_t_pipe_end > 0. ? g_t_pipe_end - g_t_last_write : 0., g_t_idx_free,
+                g_t_out_close);
 }
 
 /* ---- the pipeline's input and output steps (timed for the account) ---- */
@@ -109,6 +112,31 @@ static int hook_stats(void)
     if (on < 0) on = getenv("BSB_GPU_STATS") != 0;
     return on;
 }
+
+void __real_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps);
+void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps)
+{
+    __real_kt_pipeline(n_threads, func, shared_data, n_steps);
+    if (hook_stats()) g_t_pipe_end = hook_now();
+}
+
+void __real_bwa_idx_destroy(bwaidx_t *idx);
+void __wrap_bwa_idx_destroy(bwaidx_t *idx)
+{
+    const double t0 = hook_stats() ? hook_now() : 0.;
+    __real_bwa_idx_destroy(idx);
+    if (t0 > 0.) g_t_idx_free += hook_now() - t0;
+}
+
+int __real_err_fclose(FILE *stream);
+int __wrap_err_fclose(FILE *stream)
+{
+    const double t0 = hook_stats() ? hook_now() : 0.;
+    const int r = __real_err_fclose(stream);
+    if (t0 > 0.) g_t_out_close += hook_now() - t0;
+    return r;
+}
+
 
 bseq1_t *__wrap_bseq_read(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int64_t *s, int conversion,
                           int undirectional, float substitution_proportion)
