@@ -132,10 +132,10 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
 
     for (;;) {
         // ---- bookkeeping up to the next extension (or the end of the work)
-        DevIntv e_ik, p2;
+        DevIntv e_ik;
         bool e_back = false;
         int e_c = 0;
-        bool need = false, need2 = false;   // need2: a second backward entry of the same round (p2)
+        bool need = false;
         while (!need && st != kExit) {
             switch (st) {
             case kNeedRead: {
@@ -254,11 +254,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                     break;
                 }
                 p = pn;
-                // the entries of a round extend independently: two at a time, so that each
-                // thread has two occurrence fetches in flight; they are applied in order
-                need2 = c >= 0 && j + 1 < n_prev;
-                if (need2) p2 = prev[j + 1];
-                if (j + 1 + need2 < n_prev) pn = prev[j + 1 + need2];   // for the next step
+                if (j + 1 < n_prev) pn = prev[j + 1];       // for the next entry
                 if (c >= 0) {
                     e_ik = p; e_back = true; e_c = c;
                     need = true;
@@ -323,18 +319,11 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
             if (st == kExit) break;
             continue;
         }
-        n_ext += need + need2;
+        n_ext += need;
 
-        // ---- the extension(s), converged across the warp
-        DevIntv ok, ok2;
-        if (__any_sync(BSB_FULL_MASK, need2)) {      // warp-uniform: both in one block
-            if (need) {
-                ok = extend_one(F, e_ik, e_back, e_c);
-                ok2 = extend_one(F, need2 ? p2 : e_ik, e_back, e_c);
-            }
-        } else if (need) {
-            ok = extend_one(F, e_ik, e_back, e_c);
-        }
+        // ---- the extension, converged across the warp
+        DevIntv ok;
+        if (need) ok = extend_one(F, e_ik, e_back, e_c);
 
         // ---- apply it
         if (!need) continue;
@@ -349,23 +338,19 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
             ++i;
             break;
         case kBwdEntry:
-            for (int e = 0; e < 1 + need2; ++e) {    // entry j, then entry j + 1
-                const DevIntv &pe = e ? p2 : p;
-                DevIntv oe = e ? ok2 : ok;
-                if (oe.x2 < (uint64_t)min_intv) {
-                    if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
-                        DevIntv m = pe;
-                        m.info |= (uint64_t)(i + 1) << 32;
-                        mem[n_mem++] = m;
-                        last_mem_start = (uint64_t)(i + 1);
-                    }
-                } else if (n_curr == 0 || oe.x2 != last_x2) {
-                    oe.info = pe.info;
-                    curr[n_curr++] = oe;
-                    last_x2 = oe.x2;
+            if (ok.x2 < (uint64_t)min_intv) {
+                if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
+                    DevIntv m = p;
+                    m.info |= (uint64_t)(i + 1) << 32;
+                    mem[n_mem++] = m;
+                    last_mem_start = (uint64_t)(i + 1);
                 }
-                ++j;
+            } else if (n_curr == 0 || ok.x2 != last_x2) {
+                ok.info = p.info;
+                curr[n_curr++] = ok;
+                last_x2 = ok.x2;
             }
+            ++j;
             break;
         case kP3Fwd:
             if (ok.x2 < (uint64_t)opt.max_mem_intv && i - x0 >= opt.min_seed_len) {

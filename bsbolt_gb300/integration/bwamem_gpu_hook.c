@@ -62,6 +62,7 @@ static double g_t_start, g_t_load, g_t_ctx, g_t_upload;   /* index load, context
 static double g_t_read, g_t_write, g_t_write0;             /* input and output steps of the pipeline */
 static double g_t_first_read, g_t_last_write;              /* the pipeline's span */
 static double g_t_pipe_end, g_t_idx_free, g_t_out_close;    /* after it: index freed, SAM file closed */
+static double g_t_mem_end;                                  /* main_mem returned */
 static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
@@ -98,10 +99,11 @@ static void hook_report(void)
     if (g_t_first_read > 0.)
         fprintf(stderr, "[bsb_gpu] timeline: load to first read %.3f s, first read to last SAM output %.3f s "
                 "(alignment steps %.3f s of it), last output to exit %.3f s (pipeline end %.3f s after it, "
-                "index freed in %.3f s, SAM file closed in %.3f s)\n", g_t_first_read - g_t_start,
-                g_t_last_write - g_t_first_read, g_t_align + g_t_cigar + g_t_sw + g_t_worker2,
-                hook_now() - g_t_last_write, g_t_pipe_end > 0. ? g_t_pipe_end - g_t_last_write : 0., g_t_idx_free,
-                g_t_out_close);
+                "index freed in %.3f s, mem command returned %.3f s after it, SAM file closed in %.3f s)\n",
+                g_t_first_read - g_t_start, g_t_last_write - g_t_first_read,
+                g_t_align + g_t_cigar + g_t_sw + g_t_worker2, hook_now() - g_t_last_write,
+                g_t_pipe_end > 0. ? g_t_pipe_end - g_t_last_write : 0., g_t_idx_free,
+                g_t_mem_end > 0. ? g_t_mem_end - g_t_last_write : 0., g_t_out_close);
 }
 
 /* ---- the pipeline's input and output steps (timed for the account) ---- */
@@ -118,6 +120,14 @@ void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void 
 {
     __real_kt_pipeline(n_threads, func, shared_data, n_steps);
     if (hook_stats()) g_t_pipe_end = hook_now();
+}
+
+int __real_main_mem(int argc, char *argv[]);
+int __wrap_main_mem(int argc, char *argv[])
+{
+    const int r = __real_main_mem(argc, argv);
+    if (hook_stats()) g_t_mem_end = hook_now();
+    return r;
 }
 
 void __real_bwa_idx_destroy(bwaidx_t *idx);

@@ -240,3 +240,29 @@ def test_glue_fastq_reader_matches_kseq(pe, tmp_path, variant):
     ref = sam_sets.run_mem(BWA, fa, reads, extra)
     glue = sam_sets.run_mem(GLUE, fa, reads, extra)
     assert len(ref) >= 3000 and glue == ref
+
+
+def _bsstat(binary, fa, reads, extra):
+    cmd = [binary, "mem", "-Y", "-t", "4", "-K", "200000"] + extra + [fa] + list(reads)
+    err = subprocess.run(cmd, capture_output=True, check=True).stderr.decode()
+    tot = {}
+    for line in err.splitlines():
+        if line.startswith("BSStat "):
+            k, v = line.split()[1:3]
+            tot[k] = tot.get(k, 0) + int(v)
+    return tot
+
+
+@pytest.mark.parametrize("mode", ["pe", "se", "se_undirectional"])
+def test_glue_output_step_bsstat_matches_samsorter(pe, mode):
+    """The glue's output step (sam_out.c, in place of samSorter) prints the same BSStat counts
+    per batch as the reference's samSorter -- summed over many small batches (-K 200000) -- for
+    pairs, single ends, and -z, whose ambiguous reads take the unmapped rewrite."""
+    fa, r1, r2 = pe[:3]
+    reads = [r1, r2] if mode == "pe" else [r1]
+    extra = ["-L", "5,5"] + (["-z"] if mode == "se_undirectional" else [])
+    ref = _bsstat(BWA, fa, reads, extra)
+    glue = _bsstat(GLUE, fa, reads, extra)
+    assert ref and glue == ref
+    if mode == "se_undirectional":
+        assert ref["BSAmbiguous:"] > 0
