@@ -34,6 +34,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/time.h>
+#include <unistd.h>
 
 #include "bntseq.h"
 #include "bwa.h"
@@ -122,11 +123,31 @@ void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void 
     if (hook_stats()) g_t_pipe_end = hook_now();
 }
 
+/* At exit, after main has flushed and closed the SAM stream: leave without the CUDA runtime's
+ * own teardown (it frees every device allocation and the context one by one; the driver
+ * releases a process's context when it ends, as for any process that ends without it).
+ * Registered after main_mem returns, so it runs before every handler registered earlier --
+ * the runtime's among them.  BSB_GPU_FAST_EXIT=0 keeps the normal exit. */
+static void hook_report(void);
+static void hook_exit(int status, void *arg)
+{
+    const char *e = getenv("BSB_GPU_FAST_EXIT");
+    (void)arg;
+    if (!g_hook_ctx || (e && e[0] == '0')) return;
+    fflush(NULL);
+    if (hook_stats()) {
+        hook_report();
+        fflush(stderr);
+    }
+    _exit(status);
+}
+
 int __real_main_mem(int argc, char *argv[]);
 int __wrap_main_mem(int argc, char *argv[])
 {
     const int r = __real_main_mem(argc, argv);
     if (hook_stats()) g_t_mem_end = hook_now();
+    on_exit(hook_exit, 0);
     return r;
 }
 
