@@ -57,6 +57,45 @@ __device__ __forceinline__ uint32_t below16(uint32_t t, int u)
 }
 
 
+// Pass 2 of a row over the lane's C2 registers (see ksw_group16_run): F from each half's carry-in,
+// H, E(i+1,j), the row-maximum keys, the new eh[] and the non-zero bits.  Sym: o_del == o_ins and
+// e_del == e_ins, so E and F share their gap-open term max(M - oe, 0).
+template <int C2, bool Sym>
+__device__ __forceinline__ void ksw16_pass2(const uint32_t (&Mv)[C2], uint32_t (&Es)[C2], uint32_t (&Hs)[C2],
+                                            uint32_t &F, uint32_t t_lt, uint32_t &ltm_prev, uint32_t &kmx,
+                                            uint32_t &Hprev, uint32_t &nE0, uint32_t &lem0, uint32_t &nzw,
+                                            uint32_t ne_del, uint32_t noe_del, uint32_t ne_ins, uint32_t noe_ins)
+{
+    uint32_t kprev = 0;
+#pragma unroll
+    for (int u = 0; u < C2; ++u) {
+        const uint32_t M = Mv[u], Eo = Es[u];
+        const uint32_t H = __vimax3_s16x2(M, Eo, F);
+        const uint32_t td = __viaddmax_s16x2_relu(M, noe_del, 0);
+        const uint32_t ti = Sym ? td : __viaddmax_s16x2_relu(M, noe_ins, 0);
+        const uint32_t En = __viaddmax_s16x2(Eo, ne_del, td);
+        F = __viaddmax_s16x2(F, ne_ins, ti);
+        const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = ltm_prev;
+        ltm_prev = ltm;
+        const uint32_t key = (H & ltm) * 16u + pk16(u, u);             // ties: the later column
+        if (u & 1) kmx = __vimax3_s16x2(kmx, kprev, key);              // two registers a step
+        else kprev = key;
+        const uint32_t nE = En & ltm;
+        Es[u] = nE;
+        if (u > 0) {
+            const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);
+            Hs[u] = nH;
+            // 1 in a half where nH or nE is non-zero (both >= 0, their sum < 2^15); the
+            // halves' bits are distinct, so + is |: one shift-add
+            nzw += __viaddmin_s16x2_relu(nH, nE, 0x00010001u) << u;
+        } else {
+            nE0 = nE, lem0 = lem;
+        }
+        Hprev = H;
+    }
+    if (C2 & 1) kmx = __vimax_s16x2_relu(kmx, kprev);
+}
+
 template <int C2, int G>
 __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ext_job_t *__restrict__ jobs,
                                                 const uint8_t *__restrict__ seq, const int32_t *__restrict__ order,
@@ -73,6 +112,7 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
     const int eC = e_ins * C;
     const uint32_t ne_del = pk16(-e_del, -e_del), ne_ins = pk16(-e_ins, -e_ins);
     const uint32_t noe_del = pk16(-oe_del, -oe_del), noe_ins = pk16(-oe_ins, -oe_ins);
+    const bool sym_gaps = oe_del == oe_ins && e_del == e_ins;
 
     // per-group job state
     int qlen = 0, tlen = 0, h0 = 0, w = 0, job = -1;
@@ -223,34 +263,15 @@ __device__ __forceinline__ void ksw_group16_run(const KswParams &P, const bsb_ex
         // per half: ltm(u) = [column < rend]; lem(u) = [column <= rend] = ltm(u - 1)
         const uint32_t t_lt = pk16(rend, rend - C2);
         uint32_t ltm_prev = below16(t_lt, -1) * 0xffffu;
-        uint32_t kmx = 0, kprev = 0;               // per half: max of H*16 + u over band columns
+        uint32_t kmx = 0;                          // per half: max of H*16 + u over band columns
         uint32_t F = pk16(carry, max(carry - e_ins * C2, f_lo_end));   // F entering each half
         uint32_t Hprev = 0, nE0 = 0, lem0 = 0, nzw = 0;
-#pragma unroll
-        for (int u = 0; u < C2; ++u) {
-            const uint32_t M = Mv[u], Eo = Es[u];
-            const uint32_t H = __vimax3_s16x2(M, Eo, F);
-            const uint32_t En = __viaddmax_s16x2(Eo, ne_del, __viaddmax_s16x2_relu(M, noe_del, 0));
-            F = __viaddmax_s16x2(F, ne_ins, __viaddmax_s16x2_relu(M, noe_ins, 0));
-            const uint32_t ltm = below16(t_lt, u) * 0xffffu, lem = ltm_prev;
-            ltm_prev = ltm;
-            const uint32_t key = (H & ltm) * 16u + pk16(u, u);             // ties: the later column
-            if (u & 1) kmx = __vimax3_s16x2(kmx, kprev, key);              // two registers a step
-            else kprev = key;
-            const uint32_t nE = En & ltm;
-            Es[u] = nE;
-            if (u > 0) {
-                const uint32_t nH = (Hprev & lem) | (Hs[u] & ~lem);
-                Hs[u] = nH;
-                // 1 in a half where nH or nE is non-zero (both >= 0, their sum < 2^15); the
-                // halves' bits are distinct, so + is |: one shift-add
-                nzw += __viaddmin_s16x2_relu(nH, nE, 0x00010001u) << u;
-            } else {
-                nE0 = nE, lem0 = lem;
-            }
-            Hprev = H;
-        }
-        if (C2 & 1) kmx = __vimax_s16x2_relu(kmx, kprev);
+        if (sym_gaps)                          // deletions and insertions cost alike: one gap-open term
+            ksw16_pass2<C2, true>(Mv, Es, Hs, F, t_lt, ltm_prev, kmx, Hprev, nE0, lem0, nzw, ne_del, noe_del,
+                                  ne_ins, noe_ins);
+        else
+            ksw16_pass2<C2, false>(Mv, Es, Hs, F, t_lt, ltm_prev, kmx, Hprev, nE0, lem0, nzw, ne_del, noe_del,
+                                   ne_ins, noe_ins);
         int Hleft = __shfl_up_sync(act, hi16(Hprev), 1, G);
         if (gl == 0) Hleft = h1_init;
         {

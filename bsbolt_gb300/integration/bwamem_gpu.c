@@ -15,6 +15,7 @@
  * and link with -Wl,--wrap=bwa_gen_cigar2 -Wl,--wrap=ksw_align2.
  */
 #include <pthread.h>
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
@@ -88,6 +89,32 @@ static void glue_for(int n_threads, int64_t n, glue_body_f fn, void *data)
     }
     glue_worker(&w[0]);
     for (t = 1; t <= started; ++t) pthread_join(th[t], 0);
+}
+
+/* Counters that worker2's threads bump on every served call: one 64-byte line per shard and a
+ * shard per thread, so that no line is written by several threads or shared with the tables
+ * they read (a counter next to the CIGAR table's fields made every lookup miss). */
+#define GLUE_SHARDS 64
+typedef struct {
+    int64_t cig_served, cig_passed, sw_served;
+    char pad[64 - 3 * sizeof(int64_t)];
+} glue_shard_t;
+static glue_shard_t g_shard[GLUE_SHARDS] __attribute__((aligned(64)));
+static int g_shard_next;
+static __thread int t_shard = -1;
+
+static glue_shard_t *glue_shard(void)
+{
+    if (t_shard < 0) t_shard = __atomic_fetch_add(&g_shard_next, 1, __ATOMIC_RELAXED) % GLUE_SHARDS;
+    return &g_shard[t_shard];
+}
+
+static int64_t glue_shard_sum(size_t field)
+{
+    int64_t s = 0;
+    int k;
+    for (k = 0; k < GLUE_SHARDS; ++k) s += __atomic_load_n((int64_t *)((char *)&g_shard[k] + field), __ATOMIC_RELAXED);
+    return s;
 }
 
 static int64_t g_align_regrown;   /* batches whose region buffer had to grow */
@@ -204,7 +231,7 @@ static struct {
     int8_t mat[25];
     int o_del, e_del, o_ins, e_ins;
     int64_t l_pac, crick_l;
-    int64_t served, passed;
+    int64_t served0, passed0;      /* the shards' totals when this batch's table was made */
 } g_cig;
 
 static uint64_t cig_hash(int64_t rb, int64_t re, int l, int w)
@@ -219,15 +246,17 @@ static void cig_clear(void)
     free(g_cig.e); free(g_cig.slot); free(g_cig.jobs); free(g_cig.out);
     free(g_cig.qbuf); free(g_cig.obuf); free(g_cig.blob);
     memset(&g_cig, 0, sizeof g_cig);
+    g_cig.served0 = glue_shard_sum(offsetof(glue_shard_t, cig_served));
+    g_cig.passed0 = glue_shard_sum(offsetof(glue_shard_t, cig_passed));
 }
 
 void mem_gen_cigar_stats(int64_t *kept, int64_t *served)
 {
     if (kept) *kept = g_cig.n;
-    if (served) *served = __atomic_load_n(&g_cig.served, __ATOMIC_RELAXED);
+    if (served) *served = glue_shard_sum(offsetof(glue_shard_t, cig_served)) - g_cig.served0;
 }
 
-int64_t mem_gen_cigar_passed(void) { return __atomic_load_n(&g_cig.passed, __ATOMIC_RELAXED); }
+int64_t mem_gen_cigar_passed(void) { return glue_shard_sum(offsetof(glue_shard_t, cig_passed)) - g_cig.passed0; }
 
 int mem_mark_primary_se(const mem_opt_t *opt, int n, mem_alnreg_t *a, int64_t id);   /* bwamem.c:525 */
 
@@ -452,12 +481,12 @@ uint32_t *__wrap_bwa_gen_cigar2(const int8_t mat[25], int o_del, int e_del, int 
                 memcpy(c, g_cig.blob + r->off, r->bytes);
                 *score = r->score, *n_cigar = r->n_cigar, *NM = r->NM;
                 *cg_meth = r->cg_meth, *cg_unmeth = r->cg_unmeth, *ch_meth = r->ch_meth, *ch_unmeth = r->ch_unmeth;
-                __atomic_add_fetch(&g_cig.served, 1, __ATOMIC_RELAXED);
+                __atomic_add_fetch(&glue_shard()->cig_served, 1, __ATOMIC_RELAXED);
                 return c;
             }
         }
     }
-    if (n_cigar && oquery) __atomic_add_fetch(&g_cig.passed, 1, __ATOMIC_RELAXED);   /* a full call not served */
+    if (n_cigar && oquery) __atomic_add_fetch(&glue_shard()->cig_passed, 1, __ATOMIC_RELAXED);   /* not served */
     return __real_bwa_gen_cigar2(mat, o_del, e_del, o_ins, e_ins, w_, l_pac, pac, opac, l_query, query, rb, re, score,
                                  n_cigar, NM, crick_l, oquery, cg_meth, cg_unmeth, ch_meth, ch_unmeth);
 }
@@ -477,7 +506,7 @@ static struct {
     uint8_t *seq;
     int8_t mat[25];
     int o_del, e_del, o_ins, e_ins;
-    int64_t served;
+    int64_t served0;               /* the shards' total when this batch's table was made */
 } g_sw;
 
 /* content hash of one ksw_align2 call: lengths, flags and both sequences */
@@ -502,12 +531,13 @@ static void sw_clear(void)
 {
     free(g_sw.e); free(g_sw.slot); free(g_sw.seq);
     memset(&g_sw, 0, sizeof g_sw);
+    g_sw.served0 = glue_shard_sum(offsetof(glue_shard_t, sw_served));
 }
 
 void mem_matesw_stats(int64_t *kept, int64_t *served)
 {
     if (kept) *kept = g_sw.n;
-    if (served) *served = __atomic_load_n(&g_sw.served, __ATOMIC_RELAXED);
+    if (served) *served = glue_shard_sum(offsetof(glue_shard_t, sw_served)) - g_sw.served0;
 }
 
 /* mem_infer_dir (bwamem_pair.c:23-30) */
@@ -681,7 +711,7 @@ kswr_t __wrap_ksw_align2(int qlen, uint8_t *query, int tlen, uint8_t *target, in
                 kswr_t r;
                 r.score = e->r.score, r.te = e->r.te, r.qe = e->r.qe, r.score2 = e->r.score2, r.te2 = e->r.te2;
                 r.tb = e->r.tb, r.qb = e->r.qb;
-                __atomic_add_fetch(&g_sw.served, 1, __ATOMIC_RELAXED);
+                __atomic_add_fetch(&glue_shard()->sw_served, 1, __ATOMIC_RELAXED);
                 return r;
             }
         }

@@ -64,6 +64,7 @@ static double g_t_read, g_t_write, g_t_write0;             /* input and output s
 static double g_t_first_read, g_t_last_write;              /* the pipeline's span */
 static double g_t_pipe_end, g_t_idx_free, g_t_out_close;    /* after it: index freed, SAM file closed */
 static double g_t_mem_end;                                  /* main_mem returned */
+static double g_t_out_flush;                                /* the SAM stream flushed and synced to disk */
 static long g_batches;
 static int64_t g_cig_kept, g_cig_served, g_cig_passed, g_sw_kept, g_sw_served, g_reads;
 
@@ -100,11 +101,12 @@ static void hook_report(void)
     if (g_t_first_read > 0.)
         fprintf(stderr, "[bsb_gpu] timeline: load to first read %.3f s, first read to last SAM output %.3f s "
                 "(alignment steps %.3f s of it), last output to exit %.3f s (pipeline end %.3f s after it, "
-                "index freed in %.3f s, mem command returned %.3f s after it, SAM file closed in %.3f s)\n",
+                "index freed in %.3f s, mem command returned %.3f s after it, SAM stream flushed and synced to "
+                "disk (err_fflush, utils.c:233-258) in %.3f s, closed in %.3f s)\n",
                 g_t_first_read - g_t_start, g_t_last_write - g_t_first_read,
                 g_t_align + g_t_cigar + g_t_sw + g_t_worker2, hook_now() - g_t_last_write,
                 g_t_pipe_end > 0. ? g_t_pipe_end - g_t_last_write : 0., g_t_idx_free,
-                g_t_mem_end > 0. ? g_t_mem_end - g_t_last_write : 0., g_t_out_close);
+                g_t_mem_end > 0. ? g_t_mem_end - g_t_last_write : 0., g_t_out_flush, g_t_out_close);
 }
 
 /* ---- the pipeline's input and output steps (timed for the account) ---- */
@@ -123,31 +125,11 @@ void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void 
     if (hook_stats()) g_t_pipe_end = hook_now();
 }
 
-/* At exit, after main has flushed and closed the SAM stream: leave without the CUDA runtime's
- * own teardown (it frees every device allocation and the context one by one; the driver
- * releases a process's context when it ends, as for any process that ends without it).
- * Registered after main_mem returns, so it runs before every handler registered earlier --
- * the runtime's among them.  BSB_GPU_FAST_EXIT=0 keeps the normal exit. */
-static void hook_report(void);
-static void hook_exit(int status, void *arg)
-{
-    const char *e = getenv("BSB_GPU_FAST_EXIT");
-    (void)arg;
-    if (!g_hook_ctx || (e && e[0] == '0')) return;
-    fflush(NULL);
-    if (hook_stats()) {
-        hook_report();
-        fflush(stderr);
-    }
-    _exit(status);
-}
-
 int __real_main_mem(int argc, char *argv[]);
 int __wrap_main_mem(int argc, char *argv[])
 {
     const int r = __real_main_mem(argc, argv);
     if (hook_stats()) g_t_mem_end = hook_now();
-    on_exit(hook_exit, 0);
     return r;
 }
 
@@ -157,6 +139,15 @@ void __wrap_bwa_idx_destroy(bwaidx_t *idx)
     const double t0 = hook_stats() ? hook_now() : 0.;
     __real_bwa_idx_destroy(idx);
     if (t0 > 0.) g_t_idx_free += hook_now() - t0;
+}
+
+int __real_err_fflush(FILE *stream);
+int __wrap_err_fflush(FILE *stream)
+{
+    const double t0 = hook_stats() && stream == stdout ? hook_now() : 0.;
+    const int r = __real_err_fflush(stream);
+    if (t0 > 0.) g_t_out_flush += hook_now() - t0;
+    return r;
 }
 
 int __real_err_fclose(FILE *stream);

@@ -118,8 +118,8 @@ def test_autotune_map_is_valid_and_exact(gpu_ctx):
     assert np.array_equal(out, ref)
 
 
-@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 100), (16, 4, 6, 1, 6, 1, 100)],
-                         ids=["bwa_16bit_cells", "a16_32bit_cells"])
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 100), (1, 4, 5, 2, 7, 1, 80), (16, 4, 6, 1, 6, 1, 100)],
+                         ids=["bwa_16bit_cells", "asymmetric_gaps_16bit_cells", "a16_32bit_cells"])
 def test_every_shape_matches_oracle(gpu_ctx, scoring):
     """Each compiled shape, alone in the map for the query lengths it holds, on jobs of those
     lengths: tuples equal the oracle's.  With a = 16 the scores leave the 16-bit cells' range
