@@ -19,7 +19,7 @@
 size_t seed_scratch_bytes(int n_threads, int max_len);
 size_t seed_padded_entries(int64_t total_bases, int n_reads);
 size_t seed_queue_entries(int64_t total_bases, int n_reads);
-int seed_threads(int n_sm, int max_len, int n_reads);
+int seed_threads(int n_sm, int max_len, int n_reads, uint64_t seq_len);
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
@@ -344,7 +344,8 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     const size_t padded = seed_padded_entries(total_bases, n_reads) * sizeof(DevIntv);
     if (max_len > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "max_len %d > %d", max_len, BSB_SEED_MAX_LEN);
-    const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len, n_reads), max_len);
+    const DevFM F = dev_fm(ctx);
+    const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len, n_reads, F.seq_len), max_len);
     const size_t qn = seed_queue_entries(total_bases, n_reads);
     const size_t tot_b = (sizeof(int) * (size_t)n_reads + 255) & ~(size_t)255;
     const size_t need = padded + lists + 256 * 6 + sizeof(int) * (2 * (size_t)n_reads + 64) + 8 * qn + tot_b +
@@ -358,7 +359,6 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     void *d_queue = d_ctrl + 64;                              // pass-2 work items (int2)
     int *d_tot = (int *)((char *)d_queue + ((8 * qn + 255) & ~(size_t)255));     // seeds kept per read
     int64_t *d_scan_tmp = (int64_t *)((char *)d_tot + tot_b);
-    const DevFM F = dev_fm(ctx);
     cudaError_t e = seed_launch(F, opt->min_seed_len, opt->split_factor, opt->split_width, opt->max_mem_intv, n_reads,
                                 d_seqs, d_offs, max_len, d_padded, d_count, d_out_off, d_out, d_lists, d_ctrl,
                                 d_queue, (int64_t)qn, d_tot, d_scan_tmp, ctx->n_sm, ctx->stream);

@@ -10,7 +10,9 @@
 // substring and so the same interval, so the sort needs no tie rule.  The interval
 // lists of bwt_smem1 live in a per-thread slice of device scratch (they are short in
 // practice, but a repeat can make them as long as the read).  Every occurrence query
-// reads one 32-byte sector of the occurrence array (fm_index.cuh).
+// reads one 32-byte sector of the occurrence array (fm_index.cuh).  An index of fewer
+// than 2^32 - 2 rows runs the kernel on 32-bit intervals (96 registers, 5 blocks per SM,
+// 16-byte list entries); a larger one on 64-bit intervals (128 registers, 4 blocks).
 //
 // bwt_sa (bwt.c:86-96) is one thread per suffix-array row: one load from the full
 // suffix array when it is resident, else LF steps until a sampled row, each step
@@ -28,30 +30,73 @@ struct SeedOpt {
     int min_seed_len, split_len, split_width, max_mem_intv;
 };
 
-__device__ __forceinline__ int seed_len(const DevIntv &p)
+// The interval a seeding thread works with: bwtintv_t's fields in 64 bits (DevIntv), or, for
+// an index of fewer than 2^32 - 2 rows, in 32 bits (SeedIntv32, info = qbeg << 16 | qend with
+// read positions below 2^16), which halves the registers and the scratch bytes an interval
+// costs.  IvT gives the info field's parts and the conversions to the output's DevIntv.
+struct SeedIntv32 {
+    uint32_t x0, x1, x2, info;
+};
+
+template <class IV> struct IvT;
+template <> struct IvT<DevIntv> {
+    using pos_t = uint64_t;
+    static constexpr uint64_t kMaxRows = ~0ull;
+    __device__ static uint64_t info(int qb, int qe) { return (uint64_t)(uint32_t)qb << 32 | (uint32_t)qe; }
+    __device__ static int qbeg(const DevIntv &v) { return (int)(v.info >> 32); }
+    __device__ static int qend(const DevIntv &v) { return (int)(uint32_t)v.info; }
+    __device__ static DevIntv out(const DevIntv &v) { return v; }
+    __device__ static DevIntv in(const DevIntv &v) { return v; }
+};
+template <> struct IvT<SeedIntv32> {
+    using pos_t = uint32_t;
+    static constexpr uint64_t kMaxRows = 0xfffffffdull;
+    __device__ static uint32_t info(int qb, int qe) { return (uint32_t)qb << 16 | (uint32_t)qe; }
+    __device__ static int qbeg(const SeedIntv32 &v) { return (int)(v.info >> 16); }
+    __device__ static int qend(const SeedIntv32 &v) { return (int)(v.info & 0xffffu); }
+    __device__ static DevIntv out(const SeedIntv32 &v)
+    {
+        DevIntv d;
+        d.x0 = v.x0, d.x1 = v.x1, d.x2 = v.x2;
+        d.info = (uint64_t)(v.info >> 16) << 32 | (v.info & 0xffffu);
+        return d;
+    }
+    __device__ static SeedIntv32 in(const DevIntv &d)
+    {
+        SeedIntv32 v;
+        v.x0 = (uint32_t)d.x0, v.x1 = (uint32_t)d.x1, v.x2 = (uint32_t)d.x2;
+        v.info = (uint32_t)(d.info >> 32) << 16 | ((uint32_t)d.info & 0xffffu);
+        return v;
+    }
+};
+
+template <class IV>
+__device__ __forceinline__ int seed_len(const IV &p)
 {
-    return (int)((uint32_t)p.info - (uint32_t)(p.info >> 32));
+    return IvT<IV>::qend(p) - IvT<IV>::qbeg(p);
 }
 
 // bwt_extend (bwt.c:262-275) of ik by the single base c: the reference computes all
 // four extensions and its callers keep ok[c] only, so only that one is formed here.
-__device__ __forceinline__ DevIntv extend_one(const DevFM &F, const DevIntv &ik, bool is_back, int c)
+template <class IV>
+__device__ __forceinline__ IV extend_one(const DevFM &F, const IV &ik, bool is_back, int c)
 {
     const uint64_t xf = is_back ? ik.x0 : ik.x1;     // x[!is_back]
     const uint64_t xb = is_back ? ik.x1 : ik.x0;     // x[is_back]
+    const uint64_t x2 = ik.x2;
     Occ4 tk, tl;
-    occ4_pair(F, xf - 1, xf - 1 + ik.x2, tk, tl);
+    occ4_pair(F, xf - 1, xf - 1 + x2, tk, tl);        // in 64 bits whatever IV holds
     const uint64_t s0 = tl.c[0] - tk.c[0], s1 = tl.c[1] - tk.c[1], s2 = tl.c[2] - tk.c[2], s3 = tl.c[3] - tk.c[3];
     const uint64_t tkc = c == 0 ? tk.c[0] : c == 1 ? tk.c[1] : c == 2 ? tk.c[2] : tk.c[3];
     const uint64_t szc = c == 0 ? s0 : c == 1 ? s1 : c == 2 ? s2 : s3;
     const uint64_t above = c == 0 ? s1 + s2 + s3 : c == 1 ? s2 + s3 : c == 2 ? s3 : 0;   // bases > c
     const uint64_t l2c = l2_at(F, c);
     const uint64_t fw = l2c + 1 + tkc;
-    const uint64_t bk = xb + (xf <= F.primary && xf + ik.x2 - 1 >= F.primary) + above;
-    DevIntv o;
-    o.x0 = is_back ? fw : bk;
-    o.x1 = is_back ? bk : fw;
-    o.x2 = szc;
+    const uint64_t bk = xb + (xf <= F.primary && xf + x2 - 1 >= F.primary) + above;
+    IV o;
+    o.x0 = (typename IvT<IV>::pos_t)(is_back ? fw : bk);
+    o.x1 = (typename IvT<IV>::pos_t)(is_back ? bk : fw);
+    o.x2 = (typename IvT<IV>::pos_t)szc;
     o.info = 0;
     return o;
 }
@@ -94,19 +139,23 @@ enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrl
 __device__ __host__ __forceinline__ int part_cap1(int len) { return len / 2 + 8; }
 __device__ __host__ __forceinline__ int part_cap0(int len) { return 2 * len + 32 - part_cap1(len); }
 
-__global__ void __launch_bounds__(kSeedBlock, 4)
+// 4 blocks of 128 threads per SM on 64-bit intervals (128 registers), 5 on 32-bit ones.
+template <class IV>
+__global__ void __launch_bounds__(kSeedBlock, sizeof(IV) == sizeof(DevIntv) ? 4 : 5)
 seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restrict__ seqs,
             const int64_t *__restrict__ offs, DevIntv *__restrict__ out, int *__restrict__ count,
-            DevIntv *__restrict__ scratch, int list_cap, int *__restrict__ ctrl, int2 *__restrict__ queue,
+            IV *__restrict__ scratch, int list_cap, int *__restrict__ ctrl, int2 *__restrict__ queue,
             int queue_cap)
 {
+    using T = IvT<IV>;
+    using pos_t = typename T::pos_t;
     int *const next_item = ctrl + (mode ? kCtrlNext2 : kCtrlNext1);
     int *const overflow = ctrl + kCtrlOverflow;
     const int n_items = mode ? min(*(volatile int *)(ctrl + kCtrlQueued), queue_cap) : 2 * n_reads;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    DevIntv *const listA = scratch + (size_t)tid * 3 * list_cap;     // forward pushes / curr and prev rounds
-    DevIntv *const listB = listA + list_cap;
-    DevIntv *const mem = listB + list_cap;                           // SMEMs of one bwt_smem1 call
+    IV *const listA = scratch + (size_t)tid * 3 * list_cap;          // forward pushes / curr and prev rounds
+    IV *const listB = listA + list_cap;
+    IV *const mem = listB + list_cap;                                // SMEMs of one bwt_smem1 call
     const int64_t base_off = offs[0];
 
     int st = kNeedRead;
@@ -116,15 +165,16 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
     DevIntv *dst = nullptr;
     // bwt_smem1
     int pass = 1, x = 0, i = 0, min_intv = 1, n_curr = 0, n_prev = 0, n_mem = 0, j = 0, c = 0, ret = 0;
-    uint64_t last_mem_start = 0, last_x2 = 0;
-    DevIntv ik, p;
-    DevIntv *prev = listA, *curr = listB;
+    int last_mem_start = 0;
+    pos_t last_x2 = 0;
+    IV ik, p;
+    IV *prev = listA, *curr = listB;
     // bwt_seed_strategy1
     int x0 = 0;
     // values loaded one step ahead, so their latency overlaps the extension in flight:
     // qi = q[i] (forward phases), qb = q[i] of the next backward round, pn = prev[j]
     int qi = 4, qb = 4;
-    DevIntv pn;
+    IV pn;
     ik.x0 = ik.x1 = ik.x2 = ik.info = 0;
     p = ik;
     pn = ik;
@@ -132,7 +182,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
 
     for (;;) {
         // ---- bookkeeping up to the next extension (or the end of the work)
-        DevIntv e_ik;
+        IV e_ik;
         bool e_back = false;
         int e_c = 0;
         bool need = false;
@@ -205,8 +255,8 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                 goto smem_start;
             smem_start:
                 if (min_intv < 1) min_intv = 1;
-                ik = set_intv(F, q[x]);
-                ik.info = (uint64_t)(x + 1);
+                ik = T::in(set_intv(F, q[x]));
+                ik.info = T::info(0, x + 1);
                 n_curr = 0;
                 i = x + 1;
                 qi = i < len ? q[i] : 4;
@@ -226,7 +276,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                 prev = listA + list_cap - n_curr;            // reversed forward list
                 curr = listB;
                 n_prev = n_curr;
-                ret = (int)(uint32_t)prev[0].info;
+                ret = T::qend(prev[0]);
                 n_mem = 0;
                 i = x - 1;
                 qb = i >= 0 ? q[i] : 4;
@@ -245,7 +295,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                     if (n_curr == 0) { st = kSmemDone; break; }
                     // this round's curr becomes the next prev; the list the old prev lived in
                     // (the forward pushes sit at the top of A) takes the next curr
-                    DevIntv *const was_prev = prev;
+                    IV *const was_prev = prev;
                     prev = curr;
                     curr = was_prev < listB ? listA : listB;
                     n_prev = n_curr;
@@ -261,24 +311,24 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                     break;
                 }
                 // no base to extend by: p cannot grow, and is maximal if nothing survived yet
-                if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
-                    DevIntv m = p;
-                    m.info |= (uint64_t)(i + 1) << 32;
+                if (n_curr == 0 && (n_mem == 0 || i + 1 < last_mem_start)) {
+                    IV m = p;
+                    m.info |= T::info(i + 1, 0);
                     mem[n_mem++] = m;
-                    last_mem_start = (uint64_t)(i + 1);
+                    last_mem_start = i + 1;
                 }
                 ++j;
                 break;
             case kSmemDone:
                 for (int t = 0; t < n_mem; ++t) {
-                    const DevIntv m = mem[t];
+                    const IV m = mem[t];
                     if (seed_len(m) >= opt.min_seed_len) {
                         if (pass == 1) {
-                            if (n < cap) dst[n] = m;
+                            if (n < cap) dst[n] = T::out(m);
                             ++n;
                         } else {                            // re-seeds of one read arrive from many threads
                             const int slot = atomicAdd(&count[2 * r], 1);
-                            if (slot < cap) dst[slot] = m;
+                            if (slot < cap) dst[slot] = T::out(m);
                             else atomicMax(overflow, r + 1);
                         }
                     }
@@ -297,7 +347,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                     break;
                 }
                 if (q[x] > 3) { ++x; break; }
-                ik = set_intv(F, q[x]);
+                ik = T::in(set_intv(F, q[x]));
                 x0 = x;
                 i = x + 1;
                 qi = i < len ? q[i] : 4;
@@ -322,7 +372,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
         n_ext += need;
 
         // ---- the extension, converged across the warp
-        DevIntv ok;
+        IV ok;
         if (need) ok = extend_one(F, e_ik, e_back, e_c);
 
         // ---- apply it
@@ -331,19 +381,19 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
         case kFwd:
             if (ok.x2 != ik.x2) {
                 listA[list_cap - 1 - n_curr++] = ik;
-                if (ok.x2 < (uint64_t)min_intv) { st = kFwdEnd; break; }
+                if (ok.x2 < (pos_t)min_intv) { st = kFwdEnd; break; }
             }
             ik = ok;
-            ik.info = (uint64_t)(i + 1);
+            ik.info = T::info(0, i + 1);
             ++i;
             break;
         case kBwdEntry:
-            if (ok.x2 < (uint64_t)min_intv) {
-                if (n_curr == 0 && (n_mem == 0 || (uint64_t)(i + 1) < last_mem_start)) {
-                    DevIntv m = p;
-                    m.info |= (uint64_t)(i + 1) << 32;
+            if (ok.x2 < (pos_t)min_intv) {
+                if (n_curr == 0 && (n_mem == 0 || i + 1 < last_mem_start)) {
+                    IV m = p;
+                    m.info |= T::info(i + 1, 0);
                     mem[n_mem++] = m;
-                    last_mem_start = (uint64_t)(i + 1);
+                    last_mem_start = i + 1;
                 }
             } else if (n_curr == 0 || ok.x2 != last_x2) {
                 ok.info = p.info;
@@ -353,11 +403,11 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
             ++j;
             break;
         case kP3Fwd:
-            if (ok.x2 < (uint64_t)opt.max_mem_intv && i - x0 >= opt.min_seed_len) {
+            if (ok.x2 < (pos_t)opt.max_mem_intv && i - x0 >= opt.min_seed_len) {
                 if (ok.x2 > 0) {                            // an empty interval is not kept (bwamem.c:160)
-                    DevIntv m = ok;
-                    m.info = (uint64_t)x0 << 32 | (uint64_t)(i + 1);
-                    if (n < cap) dst[n] = m;
+                    IV m = ok;
+                    m.info = T::info(x0, i + 1);
+                    if (n < cap) dst[n] = T::out(m);
                     ++n;
                 }
                 x = i + 1;
@@ -497,19 +547,28 @@ size_t seed_scratch_bytes(int n_threads, int max_len)
     return (size_t)n_threads * 3 * (size_t)(max_len + 2) * sizeof(DevIntv);
 }
 
-// Persistent seeding threads: as many as fit on the GPU at once, no more than the
-// reads need, and fewer when long reads would make the per-thread interval lists
-// exceed ~1 GB of scratch.
-int seed_threads(int n_sm, int max_len, int n_reads)
+// The 32-bit interval variant serves indexes of fewer than 2^32 - 2 rows.
+static bool seed_narrow(uint64_t seq_len) { return seq_len < IvT<SeedIntv32>::kMaxRows; }
+
+// Persistent seeding threads for an index of seq_len rows: as many as fit on the GPU at once
+// (the variant the index runs sets the blocks per SM), no more than the reads need, and fewer
+// when long reads would make the per-thread interval lists exceed ~1 GB of scratch.  The
+// scratch of seed_scratch_bytes is sized by this count.
+int seed_threads(int n_sm, int max_len, int n_reads, uint64_t seq_len)
 {
-    static int resident = 0;
-    if (!resident) {
+    const bool narrow = seed_narrow(seq_len);
+    static int resident[2] = {0, 0};
+    if (!resident[narrow]) {
         int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, seed_kernel, kSeedBlock, 0) != cudaSuccess || b < 1) b = 4;
-        resident = b;
+        const cudaError_t e =
+            narrow ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, seed_kernel<SeedIntv32>, kSeedBlock, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, seed_kernel<DevIntv>, kSeedBlock, 0);
+        if (e != cudaSuccess || b < 1) b = 4;
+        resident[narrow] = b;
     }
+    const int res = resident[narrow];
     const size_t per_block = (size_t)kSeedBlock * 3 * (size_t)(max_len + 2) * sizeof(DevIntv);
-    size_t blocks = (size_t)n_sm * resident;
+    size_t blocks = (size_t)n_sm * res;
     const size_t want = ((size_t)2 * (n_reads > 0 ? n_reads : 1) + kSeedBlock - 1) / kSeedBlock;   // two items per read
     if (blocks > want) blocks = want;
     const size_t budget = (size_t)1 << 30;
@@ -540,11 +599,19 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
     o.max_mem_intv = max_mem_intv;
     cudaError_t e = cudaMemsetAsync(d_ctrl, 0, kCtrlWords * sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const int blocks = seed_threads(n_sm, max_len, n_reads) / kSeedBlock;
+    const bool narrow = seed_narrow(F.seq_len);
+    const int blocks = seed_threads(n_sm, max_len, n_reads, F.seq_len) / kSeedBlock;
     const int qcap = (int)(queue_cap < 0x7fffffff ? queue_cap : 0x7fffffff);
-    for (int mode = 0; mode < 2; ++mode)        // passes 1 and 3, then the pass-2 re-seeds
-        seed_kernel<<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs, (DevIntv *)d_padded, d_count,
-                                                   (DevIntv *)d_lists, max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+    for (int mode = 0; mode < 2; ++mode) {      // passes 1 and 3, then the pass-2 re-seeds
+        if (narrow)
+            seed_kernel<SeedIntv32><<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs,
+                                                                   (DevIntv *)d_padded, d_count, (SeedIntv32 *)d_lists,
+                                                                   max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+        else
+            seed_kernel<DevIntv><<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs,
+                                                                (DevIntv *)d_padded, d_count, (DevIntv *)d_lists,
+                                                                max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+    }
     read_totals<<<n_sm * 4, 256, 0, st>>>(d_count, d_offs, n_reads, d_tot);
     e = scan_i32_i64(d_tot, n_reads, d_out_off, d_scan_tmp, st);
     if (e != cudaSuccess) return e;
