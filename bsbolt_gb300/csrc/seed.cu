@@ -129,11 +129,9 @@ enum SeedState : int {
 enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrlExt = 4, kCtrlWords = 8 };
 
 // Persistent: each thread takes work items from a counter.
-//   mode 0: item r runs pass 1 of read r and queues its pass-2 re-seeds;
-//   mode 1: item w < queued runs the pass-2 re-seed queue[w] = (read, index of the SMEM),
-//           item queued + r runs pass 3 of read r (independent of passes 1-2), so that the
-//           two launches carry similar work (re-seeds alone left the second one a short,
-//           thin tail).
+//   mode 0: item r < n_reads runs pass 1 of read r and queues its pass-2 re-seeds;
+//           item n_reads + r runs pass 3 of read r (independent of passes 1-2);
+//   mode 1: item w runs the pass-2 re-seed queue[w] = (read, index of the SMEM).
 // out holds, per read r, 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r:
 // the first part_cap0(len) for passes 1-2 (pass 2 appends with an atomic counter),
 // the rest (at least len/2 + 8: pass 3 finds at most one seed per min_seed_len + 1 >= 2
@@ -153,8 +151,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
     using pos_t = typename T::pos_t;
     int *const next_item = ctrl + (mode ? kCtrlNext2 : kCtrlNext1);
     int *const overflow = ctrl + kCtrlOverflow;
-    const int n_queued = mode ? min(*(volatile int *)(ctrl + kCtrlQueued), queue_cap) : 0;
-    const int n_items = mode ? n_queued + n_reads : n_reads;
+    const int n_items = mode ? min(*(volatile int *)(ctrl + kCtrlQueued), queue_cap) : 2 * n_reads;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     IV *const listA = scratch + (size_t)tid * 3 * list_cap;          // forward pushes / curr and prev rounds
     IV *const listB = listA + list_cap;
@@ -192,20 +189,19 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
         while (!need && st != kExit) {
             switch (st) {
             case kNeedRead: {
-                // in the second launch all re-seeds first, then all pass-3 items: the warps
-                // that take them hold items of similar length, so fewer lanes idle behind a long one
+                // all pass-1 items first, then all pass-3 items: the warps that take
+                // them hold items of similar length, so fewer lanes idle behind a long one
                 const int w = atomicAdd(next_item, 1);
                 if (w >= n_items) { st = kExit; break; }
                 int k = 0;
-                const bool reseed = mode && w < n_queued;
-                if (reseed) {
+                if (mode) {
                     const int2 it = queue[w];
                     r = it.x;
                     k = it.y;
                     part = 0;
                 } else {
-                    part = mode;                             // pass 1 in the first launch, pass 3 in the second
-                    r = mode ? w - n_queued : w;
+                    part = w >= n_reads;
+                    r = part ? w - n_reads : w;
                 }
                 const int64_t o = offs[r];
                 const int64_t len64 = offs[r + 1] - o;
@@ -219,7 +215,7 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                 dst = out + 2 * (o - base_off) + 32 * (int64_t)r + (part ? part_cap0(len) : 0);
                 cap = part ? part_cap1(len) : part_cap0(len);
                 n = 0;
-                if (reseed) {                                // re-seed in the middle of a long, rare SMEM
+                if (mode) {                                  // re-seed in the middle of a long, rare SMEM
                     const DevIntv sm = dst[k];
                     pass = 2;
                     x = (int)(((sm.info >> 32) + (uint32_t)sm.info) >> 1);
@@ -573,7 +569,7 @@ int seed_threads(int n_sm, int max_len, int n_reads, uint64_t seq_len)
     const int res = resident[narrow];
     const size_t per_block = (size_t)kSeedBlock * 3 * (size_t)(max_len + 2) * sizeof(DevIntv);
     size_t blocks = (size_t)n_sm * res;
-    const size_t want = ((size_t)2 * (n_reads > 0 ? n_reads : 1) + kSeedBlock - 1) / kSeedBlock;   // re-seeds + pass 3
+    const size_t want = ((size_t)2 * (n_reads > 0 ? n_reads : 1) + kSeedBlock - 1) / kSeedBlock;   // two items per read
     if (blocks > want) blocks = want;
     const size_t budget = (size_t)1 << 30;
     if (blocks * per_block > budget) blocks = budget / per_block;
