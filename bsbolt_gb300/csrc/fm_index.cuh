@@ -111,65 +111,6 @@ __device__ __forceinline__ Occ4 occ4(const DevFM &F, uint64_t k)
     return occ_at(F, k - (k >= F.primary));
 }
 
-// In the first n (0..16) symbols of x: how many are base c (eq) and how many are above c (gt).
-// pat = c * 0x55555555 (c in every 2-bit field).
-__device__ __forceinline__ void word_cg(uint32_t x, int n, uint32_t pat, int c, uint32_t &eq, uint32_t &gt)
-{
-    const uint32_t keep = (n >= 16 ? 0xffffffffu : ~(0xffffffffu >> (2 * n))) & 0x55555555u;
-    const uint32_t y = x ^ pat, x1 = x >> 1;
-    eq += __popc(~(y | (y >> 1)) & keep);              // fields equal to c
-    gt += __popc((c == 0 ? (x | x1) : c == 1 ? x1 : c == 2 ? (x & x1) : 0u) & keep);   // fields above c
-}
-
-// Occurrences in rows [0, kk] of the $-free BWT of base c (eq) and of the bases above c (gt):
-// the two sums of occ_at's counts that a one-base bwt_extend uses, from the same sector.
-__device__ __forceinline__ void occ_cg_at(const DevFM &F, uint64_t kk, int c, uint32_t pat, uint64_t &eq,
-                                          uint64_t &gt)
-{
-    uint32_t e = 0, g = 0;
-    uint64_t ha, hc, hg, start;
-    if (F.sym64) {
-        const uint4 *p = F.blk + (kk >> 6) * 2;
-        const uint4 v0 = __ldg(p), v1 = __ldg(p + 1);
-        const int n = (int)(kk & 63) + 1;
-        word_cg(v1.x, n >= 16 ? 16 : n, pat, c, e, g);
-        word_cg(v1.y, n >= 32 ? 16 : n > 16 ? n - 16 : 0, pat, c, e, g);
-        word_cg(v1.z, n >= 48 ? 16 : n > 32 ? n - 32 : 0, pat, c, e, g);
-        word_cg(v1.w, n > 48 ? n - 48 : 0, pat, c, e, g);
-        uint64_t ba = 0, bc = 0, bg = 0;
-        if (kk >> 32) {
-            const uint64_t *b = F.sb + 3 * (kk >> 32);
-            ba = __ldg(b), bc = __ldg(b + 1), bg = __ldg(b + 2);
-        }
-        ha = ba + v0.x, hc = bc + v0.y, hg = bg + v0.z, start = kk & ~63ull;
-    } else {
-        const uint4 *p = F.blk + (kk >> 5) * 2;
-        const uint4 v0 = __ldg(p), v1 = __ldg(p + 1);
-        const int pos = (int)(kk & 31);
-        word_cg(v1.z, pos >= 16 ? 16 : pos + 1, pat, c, e, g);
-        word_cg(v1.w, pos >= 16 ? pos - 15 : 0, pat, c, e, g);
-        ha = (uint64_t)v0.y << 32 | v0.x, hc = (uint64_t)v0.w << 32 | v0.z, hg = (uint64_t)v1.y << 32 | v1.x;
-        start = kk & ~31ull;
-    }
-    const uint64_t ht = start - ha - hc - hg;          // T before the sector
-    eq = (c == 0 ? ha : c == 1 ? hc : c == 2 ? hg : ht) + e;
-    gt = (c == 0 ? hc + hg + ht : c == 1 ? hg + ht : c == 2 ? ht : 0) + g;
-}
-
-// occ_cg_at for BWT rows k and l (k <= l) with the $ adjustment and k or l = -1 counting
-// nothing, as occ4_pair does, branch-free.
-__device__ __forceinline__ void occ_cg_pair(const DevFM &F, uint64_t k, uint64_t l, int c, uint64_t &ek,
-                                            uint64_t &gk, uint64_t &el, uint64_t &gl)
-{
-    const bool kz = k == (uint64_t)-1, lz = l == (uint64_t)-1;
-    const uint64_t kk = kz ? 0 : k - (k >= F.primary), ll = lz ? 0 : l - (l >= F.primary);
-    const uint32_t pat = (uint32_t)c * 0x55555555u;
-    occ_cg_at(F, kk, c, pat, ek, gk);
-    occ_cg_at(F, ll, c, pat, el, gl);
-    if (kz) ek = gk = 0;
-    if (lz) el = gl = 0;
-}
-
 // bwt_2occ4 (bwt.c:189-220) without branches, so the threads of a warp never split over
 // whether k and l share a block.
 __device__ __forceinline__ void occ4_pair(const DevFM &F, uint64_t k, uint64_t l, Occ4 &ok, Occ4 &ol)

@@ -84,11 +84,12 @@ __device__ __forceinline__ IV extend_one(const DevFM &F, const IV &ik, bool is_b
     const uint64_t xf = is_back ? ik.x0 : ik.x1;     // x[!is_back]
     const uint64_t xb = is_back ? ik.x1 : ik.x0;     // x[is_back]
     const uint64_t x2 = ik.x2;
-    // only base c's count and the count of the bases above c are needed (bwt_2occ4 forms all
-    // four): tk[c], l's minus k's for the size, and the bases above c for the other end
-    uint64_t ek, gk, el, gl;
-    occ_cg_pair(F, xf - 1, xf - 1 + x2, c, ek, gk, el, gl);   // in 64 bits whatever IV holds
-    const uint64_t tkc = ek, szc = el - ek, above = gl - gk;
+    Occ4 tk, tl;
+    occ4_pair(F, xf - 1, xf - 1 + x2, tk, tl);        // in 64 bits whatever IV holds
+    const uint64_t s0 = tl.c[0] - tk.c[0], s1 = tl.c[1] - tk.c[1], s2 = tl.c[2] - tk.c[2], s3 = tl.c[3] - tk.c[3];
+    const uint64_t tkc = c == 0 ? tk.c[0] : c == 1 ? tk.c[1] : c == 2 ? tk.c[2] : tk.c[3];
+    const uint64_t szc = c == 0 ? s0 : c == 1 ? s1 : c == 2 ? s2 : s3;
+    const uint64_t above = c == 0 ? s1 + s2 + s3 : c == 1 ? s2 + s3 : c == 2 ? s3 : 0;   // bases > c
     const uint64_t l2c = l2_at(F, c);
     const uint64_t fw = l2c + 1 + tkc;
     const uint64_t bk = xb + (xf <= F.primary && xf + x2 - 1 >= F.primary) + above;
