@@ -38,7 +38,7 @@ EXPORTS = (
     "bsb_tile_shapes", "bsb_set_tile_map", "bsb_get_tile_map", "bsb_last_tile_ms", "bsb_index_full_sa",
     "bsb_index_upload_opac", "bsb_gen_cigar_batch", "bsb_align2_batch",
     "bsb_last_seed_extensions", "bsb_read_cost_log", "bsb_last_read_costs", "bsb_set_read_cost_model",
-    "bsb_build_suffix_array", "bsb_last_stage_ms", "bsb_set_read_order_keys",
+    "bsb_build_suffix_array", "bsb_last_stage_ms", "bsb_set_read_order_keys", "bsb_build_bwt",
 )
 
 
@@ -187,6 +187,8 @@ def load(path: str = LIB_PATH):
     L.bsb_set_read_cost_model.restype = I32
     L.bsb_build_suffix_array.argtypes = [P, P, I64, P]
     L.bsb_build_suffix_array.restype = I32
+    L.bsb_build_bwt.argtypes = [P, P, I64, I32, I64, P, P, P]
+    L.bsb_build_bwt.restype = I32
     L.bsb_align2_batch.restype = I32
     _lib = L
     return L

@@ -373,6 +373,54 @@ int bsbh_write_bwt_sa64(const char *prefix, const uint8_t *pac, int64_t l_pac, c
     return write_bwt_sa_from(prefix, pac, l_pac, sa_intv, NULL, sa);
 }
 
+/* .bwt and .sa of <prefix> from a BWT and sampled suffix array built elsewhere (the GPU's
+ * bsb_build_bwt): n = 2*l_pac symbols, bwt packed 16 to a word (first symbol in the top bits,
+ * the row of suffix 0 left out), primary = that row, sa[k] = SA[k * sa_intv] for k < n_sa =
+ * (n + sa_intv) / sa_intv.  The symbol counts L2 are the BWT's own (it permutes the text). */
+int bsbh_write_bwt_packed(const char *prefix, int64_t n, const uint32_t *bwt, uint64_t primary, const uint64_t *sa,
+                          int sa_intv)
+{
+    uint64_t L2[5] = {0, 0, 0, 0, 0}, cnt[4] = {0, 0, 0, 0};
+    const int64_t n_words = (n + 15) / 16, n_occ = (n + 127) / 128 + 1, n_sa = (n + sa_intv) / sa_intv;
+    int64_t w, k = 0, i;
+    uint32_t *buf;
+    char fn[4096];
+    FILE *fp;
+    if (!prefix || !bwt || !sa || n < 1 || sa_intv < 1 || primary > (uint64_t)n) return -1;
+    buf = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n_words + n_occ * 8));
+    if (!buf) return -3;
+    /* interleaved: the counts before every 128 symbols (4 x u64), then their 8 words */
+    for (w = 0; w < n_words; ++w) {
+        const uint32_t x = bwt[w];
+        const int valid = (int)(n - w * 16 < 16 ? n - w * 16 : 16);
+        int j;
+        if (w % 8 == 0) { memcpy(buf + k, cnt, 32); k += 8; }
+        buf[k++] = x;
+        for (j = 0; j < valid; ++j) ++cnt[x >> ((15 - j) << 1) & 3];
+    }
+    memcpy(buf + k, cnt, 32);
+    k += 8;
+    for (i = 0; i < 4; ++i) L2[i + 1] = L2[i] + cnt[i];
+    snprintf(fn, sizeof fn, "%s.bwt", prefix);
+    if (!(fp = fopen(fn, "wb"))) { free(buf); return -1; }
+    fwrite(&primary, 8, 1, fp);
+    fwrite(L2 + 1, 8, 4, fp);
+    if (fwrite(buf, 4, (size_t)k, fp) != (size_t)k) { fclose(fp); free(buf); return -1; }
+    free(buf);
+    if (fclose(fp)) return -1;
+    snprintf(fn, sizeof fn, "%s.sa", prefix);
+    if (!(fp = fopen(fn, "wb"))) return -1;
+    {
+        const uint64_t v = (uint64_t)sa_intv, sl = (uint64_t)n;
+        fwrite(&primary, 8, 1, fp);
+        fwrite(L2 + 1, 8, 4, fp);
+        fwrite(&v, 8, 1, fp);
+        fwrite(&sl, 8, 1, fp);
+        if (n_sa > 1 && fwrite(sa + 1, 8, (size_t)(n_sa - 1), fp) != (size_t)(n_sa - 1)) { fclose(fp); return -1; }
+    }
+    return fclose(fp);
+}
+
 static int index_fasta(const char *fasta, const char *prefix, int with_bwt, int64_t *l_pac_out);
 
 /* Build <prefix>.{pac,opac,ann,amb,bwt,sa} from a FASTA file.  Returns 0 or a negative code. */

@@ -2,9 +2,10 @@
 
 ``build_index(fasta, prefix)`` writes <prefix>.{pac,opac,ann,amb,bwt,sa} exactly
 as BSBolt's ``bwa index -a bwtsw`` does (bsbolt/External/BWA/bwtindex.c:256-321);
-``build_index(fasta, prefix, ctx=ctx)`` sorts the suffix array on the GPU
-(bsb_build_suffix_array: prefix doubling, texts up to 2^32 - 2 symbols, where the
-host SA-IS stops at 2^31) and writes the same files.
+``build_index(fasta, prefix, ctx=ctx)`` sorts the suffixes on the GPU
+(bsb_build_bwt: prefix doubling with 64-bit ranks in chunks that fit device memory,
+where the host SA-IS stops at 2^31 symbols), which returns the BWT and the sampled
+suffix array, and writes the same files.
 ``BwaIndex(prefix)`` reads them back into numpy arrays (bwt_restore_bwt,
 bwt_restore_sa, bns_restore: bwt.c:420-457, bntseq.c:99-176).
 """
@@ -35,13 +36,17 @@ def host_lib():
         L.bsbh_write_bwt_sa64.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_int]
         L.bsbh_write_bwt_sa64.restype = ctypes.c_int
+        L.bsbh_write_bwt_packed.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint64,
+                                            ctypes.c_void_p, ctypes.c_int]
+        L.bsbh_write_bwt_packed.restype = ctypes.c_int
         _host = L
     return _host
 
 
-def build_index(fasta: str, prefix: str, ctx=None) -> None:
+def build_index(fasta: str, prefix: str, ctx=None, chunk: int = 0, sa_intv: int = 32) -> None:
     """<prefix>.{pac,opac,ann,amb,bwt,sa} of a FASTA file; with ctx (an extend.Context) the
-    suffix array is sorted on that GPU."""
+    suffixes are sorted on that GPU (bsb_build_bwt; chunk > 0 caps the suffixes one device sort
+    takes, 0 lets the free device memory decide)."""
     if ctx is None:
         rc = host_lib().bsbh_index_fasta(fasta.encode(), prefix.encode())
         if rc != 0:
@@ -54,11 +59,14 @@ def build_index(fasta: str, prefix: str, ctx=None) -> None:
         raise RuntimeError(f"index build failed ({rc}) for {fasta}")
     n = l_pac.value
     pac = np.fromfile(prefix + ".pac", dtype=np.uint8)[: (n + 3) // 4].copy()
-    sa = np.empty(2 * n + 1, np.int64)
-    _lib.check(ctx.handle, ctx.L.bsb_build_suffix_array(ctx.handle, pac.ctypes.data_as(ctypes.c_void_p), n,
-                                                        sa.ctypes.data_as(ctypes.c_void_p)))
-    rc = host_lib().bsbh_write_bwt_sa64(prefix.encode(), pac.ctypes.data_as(ctypes.c_void_p), n,
-                                        sa.ctypes.data_as(ctypes.c_void_p), 32)
+    bwt = np.empty((2 * n + 15) // 16, np.uint32)
+    sa = np.empty((2 * n + sa_intv) // sa_intv, np.uint64)
+    primary = ctypes.c_uint64()
+    _lib.check(ctx.handle, ctx.L.bsb_build_bwt(ctx.handle, pac.ctypes.data_as(ctypes.c_void_p), n, sa_intv, chunk,
+                                               bwt.ctypes.data_as(ctypes.c_void_p), ctypes.byref(primary),
+                                               sa.ctypes.data_as(ctypes.c_void_p)))
+    rc = host_lib().bsbh_write_bwt_packed(prefix.encode(), 2 * n, bwt.ctypes.data_as(ctypes.c_void_p),
+                                          primary.value, sa.ctypes.data_as(ctypes.c_void_p), sa_intv)
     if rc != 0:
         raise RuntimeError(f"writing {prefix}.bwt/.sa failed ({rc})")
 

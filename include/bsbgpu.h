@@ -177,6 +177,18 @@ int bsb_index_load(bsb_ctx *ctx, const char *prefix);
  * No reference counterpart: bwa index sorts on the CPU. */
 int bsb_build_suffix_array(bsb_ctx *ctx, const uint8_t *pac, int64_t l_pac, int64_t *sa);
 
+/* The BWT and sampled suffix array of the same text, for texts of any length that fits device
+ * memory (ranks are 64-bit): the suffixes are sorted by prefix doubling in chunks of at most
+ * `chunk` suffixes (0: as many as the free device memory holds, ~44 bytes each, next to 9 bytes
+ * per symbol for the text and the ranks).  Outputs (host buffers): bwt, (2*l_pac + 15)/16 words
+ * of 2-bit symbols, 16 per word from the top bits, without the row of suffix 0 (bwt.h's
+ * layout before the occurrence counts are interleaved); *primary, that row; sa[k] = SA[k *
+ * sa_intv] for k < (2*l_pac + sa_intv)/sa_intv.  bsbolt_gb300.index.build_index writes
+ * BWA's .bwt/.sa from them (bwtindex.c:256-321).  BSB_ENOMEM when one 5-symbol bucket of
+ * suffixes does not fit a chunk.  No reference counterpart: bwa index sorts on the CPU. */
+int bsb_build_bwt(bsb_ctx *ctx, const uint8_t *pac, int64_t l_pac, int sa_intv, int64_t chunk, uint32_t *bwt,
+                  uint64_t *primary, uint64_t *sa);
+
 /* Full suffix array (no counterpart in the reference).  An uploaded index also gets
  * every row's SA value in device memory (8 bytes per row), built from the sampled SA,
  * so each bwt_sa is one load instead of an LF walk; results are identical.  When it

@@ -131,3 +131,34 @@ def test_bwt_sa_writer_from_a_64bit_suffix_array(tmp_path):
     want = json.load(open(os.path.join(GOLDEN, "index_sha256.json")))["files"]
     for ext, h in want.items():
         assert sha(prefix + "." + ext) == h, f".{ext} differs from the reference bwa index"
+
+
+def test_bwt_writer_from_a_packed_bwt(tmp_path):
+    """The writer bsb_build_bwt's output goes through (bsbh_write_bwt_packed): the BWT packed 16
+    symbols to a word without the row of suffix 0, that row, and every 32nd suffix-array row,
+    here derived from the host SA-IS order, give the reference `bwa index` files byte for byte."""
+    import ctypes
+    fa = str(tmp_path / "ref.fa")
+    synth.write_fasta(fa, golden_data.golden_genome())
+    prefix = str(tmp_path / "ref")
+    L = index.host_lib()
+    l_pac = ctypes.c_int64()
+    assert L.bsbh_index_fasta_nobwt(fa.encode(), prefix.encode(), ctypes.byref(l_pac)) == 0
+    n = l_pac.value
+    pac = np.fromfile(prefix + ".pac", dtype=np.uint8)[: (n + 3) // 4].copy()
+    b = ((pac[np.arange(n) >> 2] >> ((~np.arange(n) & 3) << 1)) & 3).astype(np.uint8)
+    text = np.concatenate([b, 3 - b[::-1]]).astype(np.uint8)
+    sa = index.suffix_array(text).astype(np.int64)
+    primary = int(np.nonzero(sa == 0)[0][0])
+    sym = text[sa[sa != 0] - 1].astype(np.uint32)
+    sym = np.concatenate([sym, np.zeros((-len(sym)) % 16, np.uint32)]).reshape(-1, 16)
+    words = np.zeros(len(sym), np.uint32)
+    for j in range(16):
+        words |= sym[:, j] << np.uint32((15 - j) * 2)
+    samples = sa[::32].astype(np.uint64)
+    assert len(samples) == (2 * n + 32) // 32
+    assert L.bsbh_write_bwt_packed(prefix.encode(), 2 * n, words.ctypes.data_as(ctypes.c_void_p), primary,
+                                   samples.ctypes.data_as(ctypes.c_void_p), 32) == 0
+    want = json.load(open(os.path.join(GOLDEN, "index_sha256.json")))["files"]
+    for ext, h in want.items():
+        assert sha(prefix + "." + ext) == h, f".{ext} differs from the reference bwa index"
