@@ -702,27 +702,49 @@ def ref1gb_reads(contigs, n_pairs, seed):
     return out
 
 
-def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
-    """The human-scale configuration at 1 Gb (the largest whose index text, 4e9 symbols with both
-    conversions and strands, keeps 32-bit suffix ranks): 8 contigs of 125 Mb, GC 41 %, CpG 1 %,
-    45 % interspersed repeats (families 300 bp - 6 kb, 2-20 % divergence).  The index is built
-    with the suffix array sorted on the GPU and held in HBM (occurrence sectors, full SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
+def human_contigs(tag):
+    """The human-scale references: "1gb", 8 contigs of 125 Mb; "3gb", 24 contigs of 250 down to
+    50 Mb (3.1 Gb); GC 41 %, CpG 1 %, 45 % interspersed repeats (families 300 bp - 6 kb, 2-20 %
+    divergence)."""
+    from bsbolt_gb300 import synth
+    if tag == "1gb":
+        contigs = synth.bs_genome(8, 125_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 4)
+    else:
+        x = np.linspace(1.0, 0.0, 24) ** 1.53
+        lens = np.round(50e6 + 200e6 * x).astype(np.int64)
+        lens[-1] += 3_100_000_000 - int(lens.sum())
+        assert 50e6 <= lens.min() and lens.max() <= 250e6
+        contigs = []
+        for k, ln in enumerate(lens):
+            (_, g), = synth.bs_genome(1, int(ln), gc=0.41, cpg_frac=0.01, seed=20261203 + 300 + k)
+            contigs.append((f"chr{k + 1}", g))
+    synth.add_repeats(contigs, 0.45, fam_len=(300, 6000), div=(0.02, 0.20), n_families=500, seed=20261203 + 4)
+    return contigs
+
+
+def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000, tag="1gb"):
+    """The human-scale configuration: a 1 Gb or the 3.1 Gb reference of human_contigs.  The index
+    is built with the suffixes sorted on the GPU (bsb_build_bwt: 64-bit ranks, the 3.1 Gb text
+    has 12.4e9 symbols with both conversions and strands) and held in HBM (occurrence sectors,
+    full SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
     every pair, parity against the oracle on a sample, and stock bwa against bwa_gpu from SAM."""
     import oracle
     from bsbolt_gb300 import _lib, index, seed, synth
     res = {}
-    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "ref1gb")
+    d = os.path.join(tempfile.gettempdir(), "bsbgpu_cache", "ref" + tag)
     os.makedirs(d, exist_ok=True)
     prefix = os.path.join(d, "ref")
     t0 = time.perf_counter()
-    contigs = synth.bs_genome(8, 125_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 4)
-    synth.add_repeats(contigs, 0.45, fam_len=(300, 6000), div=(0.02, 0.20), n_families=500, seed=20261203 + 4)
+    contigs = human_contigs(tag)
     res["genome_s"] = round(time.perf_counter() - t0, 1)
     if not os.path.exists(prefix + ".sa"):
-        synth.write_fasta(prefix + ".fa", contigs)
         t0 = time.perf_counter()
-        index.build_index(prefix + ".fa", prefix, ctx=ctx)
+        synth.write_fasta(prefix + ".fa", contigs)
+        res["fasta_write_s"] = round(time.perf_counter() - t0, 1)
+        t0 = time.perf_counter()
+        res["index_build"] = index.build_index(prefix + ".fa", prefix, ctx=ctx)
         res["index_build_s"] = round(time.perf_counter() - t0, 1)
+        os.unlink(prefix + ".fa")
     sets = ref1gb_reads(contigs, n_pairs, 20261203 + 40)
     del contigs
     fq = []
@@ -785,7 +807,9 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
     exact = bool(np.array_equal(roff[:ns + 1], ref_off) and all(np.array_equal(regs[f][:k], ref[f])
                                                                   for f in ref.dtype.names))
     res.update({
-        "workload": f"1 Gb bisulfite reference (8x125 Mb, 45% repeats), {n_reads // 2} directional pairs: 70% 2x150, "
+        "workload": ("1 Gb bisulfite reference (8x125 Mb" if tag == "1gb" else
+                     "3.1 Gb bisulfite reference (24 contigs of 250-50 Mb") +
+                    f", 45% repeats), {n_reads // 2} directional pairs: 70% 2x150, "
                     f"30% 2x250, 2% adapter read-through; -K 10M batches ({len(batches)}); BWA defaults",
         "seq_len": int(bi.l_pac) * 2,
         "occ_layout": ("64-symbol sectors (0.5 B/row)" if os.environ.get("BSB_OCC_SYM64") == "1"
@@ -796,7 +820,9 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000):
     del bi, ob
     threads = os.cpu_count() or 1
     if os.path.exists(os.path.join(ROOT, "bsbolt_gb300", "integration", "_build", "bwa_gpu")):
-        res["sam"] = sam_compare("pe_1gb", bsbolt_db(prefix), [os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq")],
+        # this process's full SA leaves the device first: bwa_gpu uploads the index again
+        _lib.check(ctx.handle, ctx.L.bsb_index_full_sa(ctx.handle, 0))
+        res["sam"] = sam_compare("pe_" + tag, bsbolt_db(prefix), [os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq")],
                                  n_reads // 2, threads)
     return res
 
@@ -1287,12 +1313,17 @@ def run_ours(args, ws, rank, local):
         except Exception as e:   # reported, never hidden
             rrbs = {"error": f"{type(e).__name__}: {e}"}
 
-    big1g = None
+    big1g = big3g = None
     if rank == 0 and args.ref1gb:
         try:
             big1g = pipeline_ref1gb(ctx, n_pairs=args.ref1gb_pairs)
         except Exception as e:   # reported, never hidden
             big1g = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0 and args.ref3gb:
+        try:
+            big3g = pipeline_ref1gb(ctx, n_pairs=args.ref3gb_pairs, tag="3gb")
+        except Exception as e:   # reported, never hidden
+            big3g = {"error": f"{type(e).__name__}: {e}"}
 
     lp = None
     if rank == 0 and not args.no_learned and not args.no_ref100mb:
@@ -1382,6 +1413,7 @@ def run_ours(args, ws, rank, local):
             "mate_rescue_sw": msw,
             "sam_pipeline": sam,
             "pipeline_1gb_ref": big1g,
+            "pipeline_3gb_ref": big3g,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -1410,6 +1442,10 @@ def main():
     ap.add_argument("--ref1gb", action="store_true",
                     help="add the 1 Gb-reference block (index sorted on the GPU; a few minutes to build)")
     ap.add_argument("--ref1gb-pairs", type=int, default=200_000)
+    ap.add_argument("--ref3gb", action="store_true",
+                    help="add the 3.1 Gb human-scale block (24 contigs, 45%% repeats; the index is sorted on the "
+                         "GPU with 64-bit ranks: ~10 min and ~200 GB of device memory the first time)")
+    ap.add_argument("--ref3gb-pairs", type=int, default=200_000)
     ap.add_argument("--sam-pairs", type=int, default=500_000,
                     help="2x150 pairs of the SAM block on the 100 Mb reference (the full workload is 4M)")
     ap.add_argument("--sam-rrbs", type=int, default=1_000_000,

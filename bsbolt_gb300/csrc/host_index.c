@@ -387,8 +387,14 @@ int bsbh_write_bwt_packed(const char *prefix, int64_t n, const uint32_t *bwt, ui
     char fn[4096];
     FILE *fp;
     if (!prefix || !bwt || !sa || n < 1 || sa_intv < 1 || primary > (uint64_t)n) return -1;
+    uint32_t by4[256];           /* the symbol counts of a byte (4 symbols), one per byte lane */
     buf = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n_words + n_occ * 8));
     if (!buf) return -3;
+    for (i = 0; i < 256; ++i) {
+        int j;
+        by4[i] = 0;
+        for (j = 0; j < 4; ++j) by4[i] += 1u << ((i >> (j << 1) & 3) << 3);
+    }
     /* interleaved: the counts before every 128 symbols (4 x u64), then their 8 words */
     for (w = 0; w < n_words; ++w) {
         const uint32_t x = bwt[w];
@@ -396,7 +402,12 @@ int bsbh_write_bwt_packed(const char *prefix, int64_t n, const uint32_t *bwt, ui
         int j;
         if (w % 8 == 0) { memcpy(buf + k, cnt, 32); k += 8; }
         buf[k++] = x;
-        for (j = 0; j < valid; ++j) ++cnt[x >> ((15 - j) << 1) & 3];
+        if (valid == 16) {       /* at most 16 of a symbol: the byte lanes do not carry */
+            const uint32_t c = by4[x & 255] + by4[x >> 8 & 255] + by4[x >> 16 & 255] + by4[x >> 24];
+            for (j = 0; j < 4; ++j) cnt[j] += c >> (j << 3) & 255;
+        } else {
+            for (j = 0; j < valid; ++j) ++cnt[x >> ((15 - j) << 1) & 3];
+        }
     }
     memcpy(buf + k, cnt, 32);
     k += 8;

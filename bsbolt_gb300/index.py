@@ -43,16 +43,19 @@ def host_lib():
     return _host
 
 
-def build_index(fasta: str, prefix: str, ctx=None, chunk: int = 0, sa_intv: int = 32) -> None:
+def build_index(fasta: str, prefix: str, ctx=None, chunk: int = 0, sa_intv: int = 32):
     """<prefix>.{pac,opac,ann,amb,bwt,sa} of a FASTA file; with ctx (an extend.Context) the
     suffixes are sorted on that GPU (bsb_build_bwt; chunk > 0 caps the suffixes one device sort
-    takes, 0 lets the free device memory decide)."""
+    takes, 0 lets the free device memory decide) and the seconds of each step are returned:
+    reading and packing the FASTA, the GPU sort with its copies, writing .bwt/.sa."""
+    import time
     if ctx is None:
         rc = host_lib().bsbh_index_fasta(fasta.encode(), prefix.encode())
         if rc != 0:
             raise RuntimeError(f"index build failed ({rc}) for {fasta}")
-        return
+        return None
     from . import _lib
+    t0 = time.perf_counter()
     l_pac = ctypes.c_int64()
     rc = host_lib().bsbh_index_fasta_nobwt(fasta.encode(), prefix.encode(), ctypes.byref(l_pac))
     if rc != 0:
@@ -62,13 +65,17 @@ def build_index(fasta: str, prefix: str, ctx=None, chunk: int = 0, sa_intv: int 
     bwt = np.empty((2 * n + 15) // 16, np.uint32)
     sa = np.empty((2 * n + sa_intv) // sa_intv, np.uint64)
     primary = ctypes.c_uint64()
+    t1 = time.perf_counter()
     _lib.check(ctx.handle, ctx.L.bsb_build_bwt(ctx.handle, pac.ctypes.data_as(ctypes.c_void_p), n, sa_intv, chunk,
                                                bwt.ctypes.data_as(ctypes.c_void_p), ctypes.byref(primary),
                                                sa.ctypes.data_as(ctypes.c_void_p)))
+    t2 = time.perf_counter()
     rc = host_lib().bsbh_write_bwt_packed(prefix.encode(), 2 * n, bwt.ctypes.data_as(ctypes.c_void_p),
                                           primary.value, sa.ctypes.data_as(ctypes.c_void_p), sa_intv)
     if rc != 0:
         raise RuntimeError(f"writing {prefix}.bwt/.sa failed ({rc})")
+    return {"text_symbols": 2 * n, "pack_s": round(t1 - t0, 1), "gpu_sort_s": round(t2 - t1, 1),
+            "write_s": round(time.perf_counter() - t2, 1)}
 
 
 def suffix_array(text: np.ndarray) -> np.ndarray:
