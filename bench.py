@@ -710,7 +710,7 @@ def human_contigs(tag):
     if tag == "1gb":
         contigs = synth.bs_genome(8, 125_000_000, gc=0.41, cpg_frac=0.01, seed=20261203 + 4)
     else:
-        x = np.linspace(1.0, 0.0, 24) ** 1.56
+        x = np.linspace(1.0, 0.0, 24) ** 1.53
         lens = np.round(50e6 + 200e6 * x).astype(np.int64)
         lens[0] += 3_100_000_000 - int(lens.sum())           # the total, on the longest contig
         assert 50e6 <= lens.min() and lens.max() <= 250e6
