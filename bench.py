@@ -722,12 +722,14 @@ def human_contigs(tag):
     return contigs
 
 
-def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000, tag="1gb"):
+def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000, tag="1gb", learned=False):
     """The human-scale configuration: a 1 Gb or the 3.1 Gb reference of human_contigs.  The index
     is built with the suffixes sorted on the GPU (bsb_build_bwt: 64-bit ranks, the 3.1 Gb text
     has 12.4e9 symbols with both conversions and strands) and held in HBM (occurrence sectors,
     full SA); then seeding's roofline on one -K batch, the regions pass (bsb_mem_align1_batch) over
-    every pair, parity against the oracle on a sample, and stock bwa against bwa_gpu from SAM."""
+    every pair, parity against the oracle on a sample, with `learned` the learned read order
+    against the plain one (learned_order_compare, trained on the first quarter of the batches),
+    and stock bwa against bwa_gpu from SAM."""
     import oracle
     from bsbolt_gb300 import _lib, index, seed, synth
     res = {}
@@ -818,6 +820,10 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000, tag="1gb"):
         "cpu_oracle_read_pairs_per_s": round(ns / 2 / cpu_s, 1), "cpu_oracle_sample_reads": ns,
         "regions_bit_exact_vs_oracle_on_sample": exact})
     del bi, ob
+    if learned:
+        res["learned_read_order"] = learned_order_compare(
+            ctx, reads, offs, batches, max(1, len(batches) // 4),
+            f"{res['workload'].split(',')[0]}, {n_reads} reads in {len(batches)} -K 10M batches")
     threads = os.cpu_count() or 1
     if os.path.exists(os.path.join(ROOT, "bsbolt_gb300", "integration", "_build", "bwa_gpu")):
         # this process's full SA leaves the device first: bwa_gpu uploads the index again
@@ -829,21 +835,30 @@ def pipeline_ref1gb(ctx, n_pairs=200_000, batch_bases=10_000_000, tag="1gb"):
 
 def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
     """The learned read order of the alignment batches against the plain (chain-count) order on
-    the RRBS-like workload: per-read features and DP cells logged by the library from the first
-    batches train the 2x64 cost model on the GPU (bsb_mlp_* kernels); then every batch runs with
-    each order through bsb_mem_align1_batch (host buffers), regions compared."""
-    import torch
-    from bsbolt_gb300 import _lib, cost_model as cm, seed
+    the RRBS-like workload (learned_order_compare)."""
+    from bsbolt_gb300 import seed
     prefix, reads, offs = rrbs_workload()
     n_reads = len(offs) - 1
     seed.load_index(ctx, prefix)
-    opt = _lib.AlignOpt.bwa_defaults()
     batches, lo = [], 0
     while lo < n_reads:
         hi = int(np.searchsorted(offs, offs[lo] + batch_bases, side="left"))
         hi = max(lo + 1, min(hi, n_reads))
         batches.append((lo, hi))
         lo = hi
+    return learned_order_compare(ctx, reads, offs, batches, train_batches,
+                                 f"RRBS-like, {n_reads} reads in {len(batches)} -K 10M batches")
+
+
+def learned_order_compare(ctx, reads, offs, batches, train_batches, label):
+    """Per-read features and DP cells logged by the library from the first batches train the
+    2x64 cost model on the GPU (bsb_mlp_* kernels); then every batch runs with the plain
+    (chain-count), the learned and the exact-cost read order through bsb_mem_align1_batch (host
+    buffers), regions compared.  The index is the one loaded."""
+    import torch
+    from bsbolt_gb300 import _lib, cost_model as cm, seed
+    n_reads = int(batches[-1][1] - batches[0][0])
+    opt = _lib.AlignOpt.bwa_defaults()
 
     def sub(a, b):
         return reads[offs[a]:offs[b]], offs[a:b + 1] - offs[a]
@@ -912,7 +927,7 @@ def learned_pipeline(ctx, batch_bases=10_000_000, train_batches=6):
     # the plain order's key: chains per read (feature 1 is log1p(kept chains) / 4)
     plain_key = np.expm1(fev[:, 1] * 4)
     return {
-        "workload": f"RRBS-like, {n_reads} reads in {len(batches)} -K 10M batches (bsb_mem_align1_batch, host buffers)",
+        "workload": f"{label} (bsb_mem_align1_batch, host buffers)",
         "model": "2x64 MLP, BF16 weights, FP32 accumulation, per-read features (read length, kept chains, their "
                  "seeds, best chain weight, mean seed offset, reverse-strand share, C+G content, plain bound)",
         "trained_on": f"{len(ftr)} reads of the first {train_batches} batches, target log1p(DP cells) logged by "
@@ -1321,7 +1336,7 @@ def run_ours(args, ws, rank, local):
             big1g = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and args.ref3gb:
         try:
-            big3g = pipeline_ref1gb(ctx, n_pairs=args.ref3gb_pairs, tag="3gb")
+            big3g = pipeline_ref1gb(ctx, n_pairs=args.ref3gb_pairs, tag="3gb", learned=not args.no_learned)
         except Exception as e:   # reported, never hidden
             big3g = {"error": f"{type(e).__name__}: {e}"}
 

@@ -100,3 +100,14 @@ def test_gpu_long_reads_and_seed_sw_filter(pe):
     same(fa, [lf], ["-L", "5,5"], 420)
     same(fa, [lf], sam_sets.BSBOLT_ARGS, 420)
     same(fa, [p1, p2], ["-W", "5", "-L", "5,5"], 3000)
+
+
+@pytest.mark.parametrize("workers", ["2", "3", "5"])
+def test_gpu_sam_many_batches_and_pipeline_workers(pe, workers):
+    """-K 30000 cuts the pairs into ~20 batches; with 2 (the reference's), 3 (bwa_gpu's default)
+    and 5 workers in mem's read -> align -> write pipeline the SAM is the stock one."""
+    fa, r1, r2 = pe[:3]
+    extra = sam_sets.BSBOLT_ARGS + ["-K", "30000"]
+    ref = sam_sets.run_mem(BWA, fa, [r1, r2], extra)
+    got = sam_sets.run_mem(GPU, fa, [r1, r2], extra, env=dict(os.environ, BSB_PIPELINE_WORKERS=workers))
+    assert len(ref) > 6000 and got == ref
