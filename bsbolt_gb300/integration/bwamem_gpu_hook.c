@@ -132,7 +132,6 @@ void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void 
     int n = n_threads == 2 ? 3 : n_threads;
     if (e && atoi(e) >= 1) n = atoi(e) < 8 ? atoi(e) : 8;
     __real_kt_pipeline(n, func, shared_data, n_steps);
-    if (sam_out_enabled()) sam_out_drain();          /* the last batches' SAM bytes are out */
     if (hook_stats()) g_t_pipe_end = hook_now();
 }
 
@@ -156,7 +155,6 @@ int __real_err_fflush(FILE *stream);
 int __wrap_err_fflush(FILE *stream)
 {
     const double t0 = hook_stats() && stream == stdout ? hook_now() : 0.;
-    if (stream == stdout && sam_out_enabled()) sam_out_drain();
     const int r = __real_err_fflush(stream);
     if (t0 > 0.) g_t_out_flush += hook_now() - t0;
     return r;
@@ -166,7 +164,6 @@ int __real_err_fclose(FILE *stream);
 int __wrap_err_fclose(FILE *stream)
 {
     const double t0 = hook_stats() ? hook_now() : 0.;
-    if (stream == stdout && sam_out_enabled()) sam_out_drain();
     const int r = __real_err_fclose(stream);
     if (t0 > 0.) g_t_out_close += hook_now() - t0;
     return r;

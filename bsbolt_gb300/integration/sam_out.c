@@ -10,11 +10,8 @@
  * counted as bisulfite-ambiguous (setUnmapped, bs_sorter.cpp:51-82).  Each written read is
  * counted by its mapping class; the other queue is dropped.  Here the same decisions are made
  * in one pass over the reads (it is sequential, and cheap), then the records are measured and
- * copied into one buffer on threads.  The write of that buffer and the frees of the reads'
- * strings go to a background thread, one batch after another in batch order, so the pipeline's
- * output step ends when the buffer is built; at most two batches wait there, and
- * sam_out_drain (called by the pipeline's end and before stdout is flushed or closed) waits for
- * all of them.
+ * copied into one buffer on threads and written with one fwrite, and the reads' strings are
+ * freed on the calling thread (the pipeline thread that read the batch allocated them).
  *
  * The hook links this in place of the samSorter calls (-Wl,--wrap=new_samSorter,
  * --wrap=samSorter_processRead, --wrap=samSorter_processEnd, --wrap=samSorter_delete);
@@ -37,78 +34,6 @@ typedef struct {
 } so_batch_t;
 
 static so_batch_t g_so;      /* kt_pipeline runs one output step at a time */
-
-/* ---- the background writer: batches' SAM bytes to stdout, then their reads freed ---- */
-
-typedef struct so_job {
-    char *buf;
-    size_t len;
-    void **strs;             /* the reads' strings (the read structs themselves are the caller's) */
-    int64_t n_strs;
-    struct so_job *next;
-} so_job_t;
-
-static pthread_mutex_t g_fl_mu = PTHREAD_MUTEX_INITIALIZER;
-static pthread_cond_t g_fl_cv = PTHREAD_COND_INITIALIZER;
-static so_job_t *g_fl_head, *g_fl_tail;
-static int g_fl_pending, g_fl_started;
-
-static void *so_flusher(void *arg)
-{
-    (void)arg;
-    for (;;) {
-        so_job_t *j;
-        int64_t i;
-        pthread_mutex_lock(&g_fl_mu);
-        while (!g_fl_head) pthread_cond_wait(&g_fl_cv, &g_fl_mu);
-        j = g_fl_head;
-        g_fl_head = j->next;
-        if (!g_fl_head) g_fl_tail = 0;
-        pthread_mutex_unlock(&g_fl_mu);
-        if (j->len && fwrite(j->buf, 1, j->len, stdout) != j->len) {
-            fprintf(stderr, "[sam_out] write error\n");
-            exit(1);
-        }
-        free(j->buf);
-        for (i = 0; i < j->n_strs; ++i) free(j->strs[i]);
-        free(j->strs);
-        free(j);
-        pthread_mutex_lock(&g_fl_mu);
-        --g_fl_pending;
-        pthread_cond_broadcast(&g_fl_cv);
-        pthread_mutex_unlock(&g_fl_mu);
-    }
-    return 0;
-}
-
-static void so_enqueue(so_job_t *j)
-{
-    pthread_mutex_lock(&g_fl_mu);
-    if (!g_fl_started) {
-        pthread_t t;
-        if (pthread_create(&t, 0, so_flusher, 0)) {
-            fprintf(stderr, "[sam_out] cannot start the writer thread\n");
-            abort();
-        }
-        pthread_detach(t);
-        g_fl_started = 1;
-    }
-    while (g_fl_pending >= 2) pthread_cond_wait(&g_fl_cv, &g_fl_mu);
-    j->next = 0;
-    if (g_fl_tail) g_fl_tail->next = j;
-    else g_fl_head = j;
-    g_fl_tail = j;
-    ++g_fl_pending;
-    pthread_cond_broadcast(&g_fl_cv);
-    pthread_mutex_unlock(&g_fl_mu);
-}
-
-void sam_out_drain(void)
-{
-    pthread_mutex_lock(&g_fl_mu);
-    while (g_fl_pending) pthread_cond_wait(&g_fl_cv, &g_fl_mu);
-    pthread_mutex_unlock(&g_fl_mu);
-}
 
 int sam_out_enabled(void)
 {
@@ -215,14 +140,12 @@ static void so_parallel(so_write_t *W, int phase)
     for (t = 1; t <= started; ++t) pthread_join(th[t], 0);
 }
 
-/* a read's strings into the writer's free list (the reference frees the read structs right
- * after the output step, fastmap.c:70-72) */
-static void **so_take_strings(bseq1_t *r, void **p)
+static void so_free_read(bseq1_t *r)
 {
-    *p++ = r->name, *p++ = r->comment, *p++ = r->seq;
-    *p++ = r->qual, *p++ = r->sam, *p++ = r->oseq;
+    free(r->name); free(r->comment);
+    free(r->seq); free(r->qual);
+    free(r->sam); free(r->oseq);
     r->name = r->comment = r->seq = r->qual = r->sam = r->oseq = 0;
-    return p;
 }
 
 /* processEnd and the reads before it: the reference's decisions over the batch, then the
@@ -290,6 +213,10 @@ void sam_out_end(void)
             abort();
         }
         so_parallel(&W, 1);
+        if (acc && fwrite(W.buf, 1, acc, stdout) != acc) {
+            fprintf(stderr, "[sam_out] write error\n");
+            exit(1);
+        }
     }
     /* the reference prints the batch's counts from processEnd (bs_sorter_wrapper.cpp) */
     fprintf(stderr, "BSStat TotalReads: %d\n", reads_observed);
@@ -300,24 +227,8 @@ void sam_out_end(void)
     fprintf(stderr, "BSStat C_G2A: %d\n", cg2a);
     fprintf(stderr, "BSStat Unaligned: %d\n", unaligned);
     fprintf(stderr, "BSStat BSAmbiguous: %d\n", bs_ambiguous);
-    {   /* the bytes and the reads to the writer thread; the next batch gets a new read list */
-        so_job_t *j = (so_job_t *)malloc(sizeof *j);
-        if (!j) {
-            fprintf(stderr, "[sam_out] out of memory\n");
-            abort();
-        }
-        void **p;
-        j->buf = W.buf, j->len = W.off[n_out];
-        j->n_strs = 6 * g_so.n;
-        j->strs = p = (void **)malloc(sizeof(void *) * (size_t)(j->n_strs + 1));
-        if (!j->strs) {
-            fprintf(stderr, "[sam_out] out of memory\n");
-            abort();
-        }
-        for (i = 0; i < g_so.n; ++i) p = so_take_strings(g_so.r[i], p);
-        so_enqueue(j);
-    }
-    free(W.out); free(W.unmapped); free(W.off); free(g1); free(g2);
+    for (i = 0; i < g_so.n; ++i) so_free_read(g_so.r[i]);
+    free(W.buf); free(W.out); free(W.unmapped); free(W.off); free(g1); free(g2);
     g_so.n = 0;
     g_so.active = 0;
 }

@@ -227,11 +227,3 @@ struct samSorter *__wrap_new_samSorter(bseq1_t *first_read)
 void __wrap_samSorter_processRead(struct samSorter *ss, bseq1_t *read) { (void)ss; sam_out_read(read); }
 void __wrap_samSorter_processEnd(struct samSorter *ss) { (void)ss; sam_out_end(); }
 void __wrap_samSorter_delete(struct samSorter *ss) { (void)ss; }
-
-/* the pipeline's end: the writer thread has written every batch before main flushes stdout */
-void __real_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps);
-void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps)
-{
-    __real_kt_pipeline(n_threads, func, shared_data, n_steps);
-    sam_out_drain();
-}
