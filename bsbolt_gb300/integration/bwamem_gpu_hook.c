@@ -118,18 +118,17 @@ static int hook_stats(void)
     return on;
 }
 
-/* mem's read -> align -> write pipeline (fastmap.c:352, kthread.c:119-147) runs with three
- * workers where the reference starts two: each worker takes one batch through the three steps,
- * every step still runs one batch at a time and in batch order (ktp_worker), so the SAM stream is
- * unchanged; the third worker lets the next batch's input run beside the current batch's
- * alignment and the previous batch's output, which with two workers wait for one another once
- * input + alignment + output exceed two alignment steps.  BSB_PIPELINE_WORKERS=n sets the count
- * (2: the reference's; mem -1 asks for one and keeps it). */
+/* mem's read -> align -> write pipeline (fastmap.c:352, kthread.c:119-147): each worker takes
+ * one batch through the three steps and every step runs one batch at a time, in batch order
+ * (ktp_worker), so the worker count changes only what overlaps.  BSB_PIPELINE_WORKERS=n sets
+ * it; the default is the reference's (two; one with mem -1).  Measured on the GB300 machine, three
+ * workers gained nothing (100 Mb PE: 0.61 s from the first read to the last SAM output either
+ * way; RRBS: 0.69 s with two, 0.71 s with three). */
 void __real_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps);
 void __wrap_kt_pipeline(int n_threads, void *(*func)(void *, int, void *), void *shared_data, int n_steps)
 {
     const char *e = getenv("BSB_PIPELINE_WORKERS");
-    int n = n_threads == 2 ? 3 : n_threads;
+    int n = n_threads;
     if (e && atoi(e) >= 1) n = atoi(e) < 8 ? atoi(e) : 8;
     __real_kt_pipeline(n, func, shared_data, n_steps);
     if (hook_stats()) g_t_pipe_end = hook_now();

@@ -104,7 +104,7 @@ def test_gpu_long_reads_and_seed_sw_filter(pe):
 
 @pytest.mark.parametrize("workers", ["2", "3", "5"])
 def test_gpu_sam_many_batches_and_pipeline_workers(pe, workers):
-    """-K 30000 cuts the pairs into ~20 batches; with 2 (the reference's), 3 (bwa_gpu's default)
+    """-K 30000 cuts the pairs into ~20 batches; with 2 (the reference's, bwa_gpu's default), 3
     and 5 workers in mem's read -> align -> write pipeline the SAM is the stock one."""
     fa, r1, r2 = pe[:3]
     extra = sam_sets.BSBOLT_ARGS + ["-K", "30000"]
