@@ -17,14 +17,14 @@
 #include "scan.cuh"
 
 size_t seed_scratch_bytes(int n_threads, int max_len);
-size_t seed_padded_entries(int64_t total_bases, int n_reads);
-size_t seed_queue_entries(int64_t total_bases, int n_reads);
+size_t seed_padded_entries(int64_t total_bases, int n_reads, int mult);
+size_t seed_queue_entries(int64_t total_bases, int n_reads, int mult);
 int seed_threads(int n_sm, int max_len, int n_reads, uint64_t seq_len);
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
                         void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int *d_tot,
-                        int64_t *d_scan_tmp, int n_sm, cudaStream_t st);
+                        int64_t *d_scan_tmp, int mult, int n_sm, cudaStream_t st);
 cudaError_t sa_launch(const DevFM &F, const uint64_t *d_rows, int64_t n, uint64_t *d_pos, int n_sm, cudaStream_t st);
 cudaError_t sa_full_build(const DevFM &F, int64_t n_sa, uint64_t *full, int *failed, int n_sm, cudaStream_t st);
 
@@ -334,6 +334,15 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
                                      const int64_t *d_offs, int64_t total_bases, int32_t max_len,
                                      bsb_intv_t *d_out, int64_t *d_out_off)
 {
+    return bsb_seed_batch_device_m(ctx, opt, n_reads, d_seqs, d_offs, total_bases, max_len, d_out, d_out_off, 1);
+}
+
+// With mult times the per-read seed slots (seed.cu): d_out must hold seed_padded_entries(total,
+// n, mult) entries.  The overflow word (bsb_seed_overflow) tells whether a read needed more.
+int bsb_seed_batch_device_m(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *d_seqs,
+                            const int64_t *d_offs, int64_t total_bases, int32_t max_len, bsb_intv_t *d_out,
+                            int64_t *d_out_off, int mult)
+{
     if (!ctx) return BSB_EINVAL;
     if (!ctx->has_index) return bsb_fail(ctx, BSB_ENOINDEX, "no index loaded");
     if (!opt || n_reads < 0 || max_len < 0 || total_bases < 0) return bsb_fail(ctx, BSB_EINVAL, "bad seed arguments");
@@ -342,11 +351,11 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     if (n_reads == 0) return 0;
     int rc;
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
-    const size_t padded = seed_padded_entries(total_bases, n_reads) * sizeof(DevIntv);
+    const size_t padded = seed_padded_entries(total_bases, n_reads, mult) * sizeof(DevIntv);
     if (max_len > BSB_SEED_MAX_LEN) return bsb_fail(ctx, BSB_ETOOLONG, "max_len %d > %d", max_len, BSB_SEED_MAX_LEN);
     const DevFM F = dev_fm(ctx);
     const size_t lists = seed_scratch_bytes(seed_threads(ctx->n_sm, max_len, n_reads, F.seq_len), max_len);
-    const size_t qn = seed_queue_entries(total_bases, n_reads);
+    const size_t qn = seed_queue_entries(total_bases, n_reads, mult);
     const size_t tot_b = (sizeof(int) * (size_t)n_reads + 255) & ~(size_t)255;
     const size_t need = padded + lists + 256 * 6 + sizeof(int) * (2 * (size_t)n_reads + 64) + 8 * qn + tot_b +
                         sizeof(int64_t) * (size_t)scan_tmp_words(n_reads);
@@ -361,7 +370,7 @@ extern "C" int bsb_seed_batch_device(bsb_ctx *ctx, const bsb_seed_opt_t *opt, in
     int64_t *d_scan_tmp = (int64_t *)((char *)d_tot + tot_b);
     cudaError_t e = seed_launch(F, opt->min_seed_len, opt->split_factor, opt->split_width, opt->max_mem_intv, n_reads,
                                 d_seqs, d_offs, max_len, d_padded, d_count, d_out_off, d_out, d_lists, d_ctrl,
-                                d_queue, (int64_t)qn, d_tot, d_scan_tmp, ctx->n_sm, ctx->stream);
+                                d_queue, (int64_t)qn, d_tot, d_scan_tmp, mult, ctx->n_sm, ctx->stream);
     ctx->seed_ctrl = d_ctrl;
     return bsb_cuda(ctx, e, "seed launch");
 }
@@ -404,9 +413,7 @@ extern "C" int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     const size_t off_b = sizeof(int64_t) * ((size_t)n_reads + 1);
     const size_t seq_b = ((size_t)total + 255) & ~(size_t)255;
-    const size_t out_b = seed_padded_entries(total, n_reads) * sizeof(bsb_intv_t);
     if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, seq_b + 2 * off_b + 512, "seed input staging"))) return rc;
-    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, out_b + 256, "seed output staging"))) return rc;
     uint8_t *d_seqs = (uint8_t *)ctx->d_in;
     int64_t *d_offs = (int64_t *)((char *)ctx->d_in + seq_b);
     int64_t *d_out_off = (int64_t *)((char *)d_offs + ((off_b + 255) & ~(size_t)255));
@@ -417,15 +424,26 @@ extern "C" int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n
         return rc;
     if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(d_offs, rel.data(), off_b, cudaMemcpyHostToDevice, ctx->stream), "H2D offsets")))
         return rc;
-    if ((rc = bsb_seed_batch_device(ctx, opt, n_reads, d_seqs, d_offs, total, max_len, (bsb_intv_t *)ctx->d_out, d_out_off)))
-        return rc;
-    int ctrl[2] = {0, 0};
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out_off, d_out_off, off_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H offsets")))
-        return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream), "D2H ctrl")))
-        return rc;
-    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seed batch"))) return rc;
-    if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
+    // a read whose passes 1-2 overflow its seed slots: the batch again with twice the slots
+    for (int mult = 1;; mult *= 2) {
+        const size_t out_b = seed_padded_entries(total, n_reads, mult) * sizeof(bsb_intv_t);
+        if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, out_b + 256, "seed output staging"))) return rc;
+        if ((rc = bsb_seed_batch_device_m(ctx, opt, n_reads, d_seqs, d_offs, total, max_len, (bsb_intv_t *)ctx->d_out,
+                                          d_out_off, mult)))
+            return rc;
+        int ctrl[2] = {0, 0};
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(out_off, d_out_off, off_b, cudaMemcpyDeviceToHost, ctx->stream),
+                           "D2H offsets")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream),
+                           "D2H ctrl")) ||
+            (rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seed batch")))
+            return rc;
+        if (!ctrl[1]) break;
+        if (mult >= kSeedSlotMultMax)
+            return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than %d times its buffer holds",
+                            ctrl[1] - 1, mult);
+        ++ctx->seed_regrown;
+    }
     if (out_off[n_reads] > max_out)
         return bsb_fail(ctx, BSB_EINVAL, "%lld seeds do not fit max_out %lld", (long long)out_off[n_reads], (long long)max_out);
     if (out_off[n_reads] > 0 &&

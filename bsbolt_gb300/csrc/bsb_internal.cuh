@@ -63,6 +63,7 @@ struct bsb_ctx {
     void *seed_scratch = nullptr;
     size_t seed_scratch_bytes = 0;
     int *seed_ctrl = nullptr;
+    int64_t seed_regrown = 0;     // seeding batches run again with more seed slots per read
     // tile map of the batched extension (host copy; device copy only when it is not the default)
     uint8_t tile_map[BSB_TILE_MAP_LEN] = {};
     uint8_t *d_tile_map = nullptr;
@@ -158,3 +159,11 @@ uint64_t ksw_map_tiles(const uint8_t *map);
 // beyond the rounding of the two double operations, so truncation agrees.  (Double division
 // runs on the GPU's slow fp64 pipe.)
 __host__ __device__ __forceinline__ int band_cap(int num, int e) { return (num + e) / e; }
+
+// bsb_seed_batch_device with mult times the per-read seed slots (d_out: seed_padded_entries(
+// total, n, mult) entries); the caller reads the overflow word (seed_ctrl[1], read + 1) and
+// runs the batch again with more slots, up to kSeedSlotMultMax.
+constexpr int kSeedSlotMultMax = 64;
+int bsb_seed_batch_device_m(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads, const uint8_t *d_seqs,
+                            const int64_t *d_offs, int64_t total_bases, int32_t max_len, bsb_intv_t *d_out,
+                            int64_t *d_out_off, int mult);

@@ -25,6 +25,8 @@
 #include "ksw_core.cuh"
 #include "scan.cuh"
 
+size_t seed_padded_entries(int64_t total_bases, int n_reads, int mult);   // seed.cu
+
 namespace {
 
 constexpr int kBT = 5;                  // kbtree order for 40-byte keys in 512-byte nodes
@@ -1569,14 +1571,11 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
     if ((rc = bsb_cuda(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
     const size_t off_b = sizeof(int64_t) * ((size_t)n_reads + 1);
     const size_t seq_b = al((size_t)total);
-    const size_t seeds_b = al(((size_t)2 * total + 32 * (size_t)n_reads) * sizeof(bsb_intv_t));
     if ((rc = bsb_ensure(ctx, &ctx->d_in, &ctx->d_in_bytes, seq_b + 2 * al(off_b) + 256, "align input staging")))
         return rc;
-    if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, seeds_b + 256, "align seed buffer"))) return rc;
     uint8_t *d_reads = (uint8_t *)ctx->d_in;
     int64_t *d_offs = (int64_t *)((char *)ctx->d_in + seq_b);
     int64_t *d_seed_off = (int64_t *)((char *)d_offs + al(off_b));
-    bsb_intv_t *d_seeds = (bsb_intv_t *)ctx->d_out;
     std::vector<int64_t> rel(n_reads + 1);
     for (int r = 0; r <= n_reads; ++r) rel[r] = offs[r] - offs[0];
     ctx->stage_valid = false;
@@ -1589,17 +1588,30 @@ static int align_batch(bsb_ctx *ctx, const bsb_align_opt_t *o, int32_t n_reads, 
     bsb_seed_opt_t so;
     so.min_seed_len = o->min_seed_len; so.split_factor = o->split_factor;
     so.split_width = o->split_width; so.max_mem_intv = o->max_mem_intv;
-    if ((rc = bsb_seed_batch_device(ctx, &so, n_reads, d_reads, d_offs, total, max_len, d_seeds, d_seed_off)) ||
-        (rc = bsb_cuda(ctx, cudaEventRecord(sev[1], ctx->stream), "stage mark")))
-        return rc;
+    // a read whose passes 1-2 overflow its seed slots: seeding again with twice the slots
+    bsb_intv_t *d_seeds = nullptr;
     int64_t n_seeds = 0;
-    int ctrl[2] = {0, 0};
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&n_seeds, d_seed_off + n_reads, 8, cudaMemcpyDeviceToHost, ctx->stream), "seed total")))
-        return rc;
-    if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream), "seed ctrl")))
-        return rc;
-    if ((rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seeding"))) return rc;
-    if (ctrl[1]) return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than its buffer holds", ctrl[1] - 1);
+    for (int mult = 1;; mult *= 2) {
+        const size_t seeds_b = al(seed_padded_entries(total, n_reads, mult) * sizeof(bsb_intv_t));
+        if ((rc = bsb_ensure(ctx, &ctx->d_out, &ctx->d_out_bytes, seeds_b + 256, "align seed buffer"))) return rc;
+        d_seeds = (bsb_intv_t *)ctx->d_out;
+        if ((rc = bsb_seed_batch_device_m(ctx, &so, n_reads, d_reads, d_offs, total, max_len, d_seeds, d_seed_off,
+                                          mult)) ||
+            (rc = bsb_cuda(ctx, cudaEventRecord(sev[1], ctx->stream), "stage mark")))
+            return rc;
+        int ctrl[2] = {0, 0};
+        if ((rc = bsb_cuda(ctx, cudaMemcpyAsync(&n_seeds, d_seed_off + n_reads, 8, cudaMemcpyDeviceToHost, ctx->stream),
+                           "seed total")) ||
+            (rc = bsb_cuda(ctx, cudaMemcpyAsync(ctrl, ctx->seed_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream),
+                           "seed ctrl")) ||
+            (rc = bsb_cuda(ctx, cudaStreamSynchronize(ctx->stream), "seeding")))
+            return rc;
+        if (!ctrl[1]) break;
+        if (mult >= kSeedSlotMultMax)
+            return bsb_fail(ctx, BSB_ETOOLONG, "read %d produced more seeds than %d times its buffer holds",
+                            ctrl[1] - 1, mult);
+        ++ctx->seed_regrown;
+    }
     bsb_reg_t *d_regs = nullptr;
     int64_t *d_reg_off = nullptr, n_regs = 0;
     if ((rc = bsb_align_regs_run(ctx, o, n_reads, d_reads, d_offs, d_seeds, d_seed_off, n_seeds, max_len, dedup, &d_regs,

@@ -132,12 +132,18 @@ enum { kCtrlNext1 = 0, kCtrlOverflow = 1, kCtrlQueued = 2, kCtrlNext2 = 3, kCtrl
 //   mode 0: item r < n_reads runs pass 1 of read r and queues its pass-2 re-seeds;
 //           item n_reads + r runs pass 3 of read r (independent of passes 1-2);
 //   mode 1: item w runs the pass-2 re-seed queue[w] = (read, index of the SMEM).
-// out holds, per read r, 2*len(r) + 32 slots starting at 2*(offs[r]-offs[0]) + 32*r:
-// the first part_cap0(len) for passes 1-2 (pass 2 appends with an atomic counter),
-// the rest (at least len/2 + 8: pass 3 finds at most one seed per min_seed_len + 1 >= 2
-// bases) for pass 3; count[2r + part] counts each part.
+// out holds, per read r, mult * (2*len(r) + 32) slots starting at mult * (2*(offs[r]-offs[0]) +
+// 32*r): the first part_cap0(len, mult) for passes 1-2 (pass 2 appends with an atomic
+// counter), the last part_cap1(len) (len/2 + 8: pass 3 finds at most one seed per
+// min_seed_len + 1 >= 2 bases) for pass 3; count[2r + part] counts each part.  Passes 1-2
+// have no such bound (every re-seed of a repeat can add SMEMs): a batch in which a read
+// overflows runs again with mult doubled.
 __device__ __host__ __forceinline__ int part_cap1(int len) { return len / 2 + 8; }
-__device__ __host__ __forceinline__ int part_cap0(int len) { return 2 * len + 32 - part_cap1(len); }
+__device__ __host__ __forceinline__ int part_cap0(int len, int mult) { return mult * (2 * len + 32) - part_cap1(len); }
+__device__ __host__ __forceinline__ int64_t part_base(int64_t rel_off, int r, int mult)
+{
+    return (int64_t)mult * (2 * rel_off + 32 * (int64_t)r);
+}
 
 // 4 blocks of 128 threads per SM on 64-bit intervals (128 registers), 5 on 32-bit ones.
 template <class IV>
@@ -145,7 +151,7 @@ __global__ void __launch_bounds__(kSeedBlock, sizeof(IV) == sizeof(DevIntv) ? 4 
 seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restrict__ seqs,
             const int64_t *__restrict__ offs, DevIntv *__restrict__ out, int *__restrict__ count,
             IV *__restrict__ scratch, int list_cap, int *__restrict__ ctrl, int2 *__restrict__ queue,
-            int queue_cap)
+            int queue_cap, int mult)
 {
     using T = IvT<IV>;
     using pos_t = typename T::pos_t;
@@ -212,8 +218,8 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
                 }
                 len = (int)len64;
                 q = seqs + o;
-                dst = out + 2 * (o - base_off) + 32 * (int64_t)r + (part ? part_cap0(len) : 0);
-                cap = part ? part_cap1(len) : part_cap0(len);
+                dst = out + part_base(o - base_off, r, mult) + (part ? part_cap0(len, mult) : 0);
+                cap = part ? part_cap1(len) : part_cap0(len, mult);
                 n = 0;
                 if (mode) {                                  // re-seed in the middle of a long, rare SMEM
                     const DevIntv sm = dst[k];
@@ -427,20 +433,20 @@ seed_kernel(DevFM F, SeedOpt opt, int mode, int n_reads, const uint8_t *__restri
 // Seeds of read r in the two parts of its padded region (a part that overflowed holds
 // its capacity; the launch reports the overflow).
 __device__ __forceinline__ void part_counts(const int *__restrict__ count, const int64_t *__restrict__ offs, int r,
-                                            int &na, int &nb)
+                                            int mult, int &na, int &nb)
 {
     const int len = (int)(offs[r + 1] - offs[r]);
-    na = min(count[2 * r], part_cap0(len));
+    na = min(count[2 * r], part_cap0(len, mult));
     nb = min(count[2 * r + 1], part_cap1(len));
 }
 
 // Seeds each read keeps (both parts, clamped to their caps), for the offset scan.
-__global__ void read_totals(const int *__restrict__ count, const int64_t *__restrict__ offs, int n,
+__global__ void read_totals(const int *__restrict__ count, const int64_t *__restrict__ offs, int n, int mult,
                             int *__restrict__ tot)
 {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int na, nb;
-        part_counts(count, offs, r, na, nb);
+        part_counts(count, offs, r, mult, na, nb);
         tot[r] = na + nb;
     }
 }
@@ -453,7 +459,7 @@ constexpr int kSortStage = 256, kCompactWarps = 4;
 // One warp per read: the read's two parts merged into info order by rank (keys staged in
 // the warp's slice of shared memory when they fit).
 __global__ void __launch_bounds__(kCompactWarps * 32)
-compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads,
+compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ offs, int n_reads, int mult,
               const int *__restrict__ count, const int64_t *__restrict__ out_off, DevIntv *__restrict__ out)
 {
     __shared__ uint64_t keys[kCompactWarps][kSortStage];
@@ -462,10 +468,10 @@ compact_seeds(const DevIntv *__restrict__ padded, const int64_t *__restrict__ of
     const int64_t base_off = offs[0];
     for (int r = blockIdx.x * kCompactWarps + wb; r < n_reads; r += gridDim.x * kCompactWarps) {
         const int len = (int)(offs[r + 1] - offs[r]);
-        const DevIntv *a = padded + 2 * (offs[r] - base_off) + 32 * (int64_t)r;
-        const DevIntv *b = a + part_cap0(len);
+        const DevIntv *a = padded + part_base(offs[r] - base_off, r, mult);
+        const DevIntv *b = a + part_cap0(len, mult);
         int na, nb;
-        part_counts(count, offs, r, na, nb);
+        part_counts(count, offs, r, mult, na, nb);
         const int m = na + nb;
         DevIntv *dst = out + out_off[r];
         const bool staged = m <= kSortStage;
@@ -579,18 +585,21 @@ int seed_threads(int n_sm, int max_len, int n_reads, uint64_t seq_len)
 
 // Pass-2 work items a batch can queue: at most one per SMEM of pass 1, i.e. per read
 // position.
-size_t seed_queue_entries(int64_t total_bases, int n_reads) { return (size_t)total_bases + (size_t)n_reads + 64; }
-
-size_t seed_padded_entries(int64_t total_bases, int n_reads)
+size_t seed_queue_entries(int64_t total_bases, int n_reads, int mult)
 {
-    return 2 * (size_t)total_bases + 32 * (size_t)n_reads;
+    return (size_t)mult * ((size_t)total_bases + (size_t)n_reads) + 64;
+}
+
+size_t seed_padded_entries(int64_t total_bases, int n_reads, int mult)
+{
+    return (size_t)mult * (2 * (size_t)total_bases + 32 * (size_t)n_reads);
 }
 
 cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, int split_width, int max_mem_intv,
                         int n_reads, const uint8_t *d_seqs, const int64_t *d_offs, int max_len,
                         void *d_padded, int *d_count, int64_t *d_out_off, void *d_out,
                         void *d_lists, int *d_ctrl, void *d_queue, int64_t queue_cap, int *d_tot,
-                        int64_t *d_scan_tmp, int n_sm, cudaStream_t st)
+                        int64_t *d_scan_tmp, int mult, int n_sm, cudaStream_t st)
 {
     SeedOpt o;
     o.min_seed_len = min_seed_len;
@@ -606,18 +615,18 @@ cudaError_t seed_launch(const DevFM &F, int min_seed_len, float split_factor, in
         if (narrow)
             seed_kernel<SeedIntv32><<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs,
                                                                    (DevIntv *)d_padded, d_count, (SeedIntv32 *)d_lists,
-                                                                   max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+                                                                   max_len + 2, d_ctrl, (int2 *)d_queue, qcap, mult);
         else
             seed_kernel<DevIntv><<<blocks, kSeedBlock, 0, st>>>(F, o, mode, n_reads, d_seqs, d_offs,
                                                                 (DevIntv *)d_padded, d_count, (DevIntv *)d_lists,
-                                                                max_len + 2, d_ctrl, (int2 *)d_queue, qcap);
+                                                                max_len + 2, d_ctrl, (int2 *)d_queue, qcap, mult);
     }
-    read_totals<<<n_sm * 4, 256, 0, st>>>(d_count, d_offs, n_reads, d_tot);
+    read_totals<<<n_sm * 4, 256, 0, st>>>(d_count, d_offs, n_reads, mult, d_tot);
     e = scan_i32_i64(d_tot, n_reads, d_out_off, d_scan_tmp, st);
     if (e != cudaSuccess) return e;
     const int cb = (int)((n_reads + kCompactWarps - 1) / kCompactWarps);
     compact_seeds<<<cb < n_sm * 16 ? cb : n_sm * 16, kCompactWarps * 32, 0, st>>>(
-        (const DevIntv *)d_padded, d_offs, n_reads, d_count, d_out_off, (DevIntv *)d_out);
+        (const DevIntv *)d_padded, d_offs, n_reads, mult, d_count, d_out_off, (DevIntv *)d_out);
     return cudaGetLastError();
 }
 

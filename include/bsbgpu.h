@@ -218,7 +218,10 @@ typedef struct {
  * read r = seqs[offs[r] .. offs[r+1]).  out receives every read's seed list
  * in the reference's order (sorted by info), out_off[r] .. out_off[r+1]
  * (n_reads + 1 entries).  Reads shorter than min_seed_len get no seeds
- * (mem_chain, bwamem.c:266).  Reads longer than 1024 give BSB_ETOOLONG. */
+ * (mem_chain, bwamem.c:266).  Reads longer than 1024 give BSB_ETOOLONG.  Each read
+ * first gets 2*len + 32 seed slots; a batch in which a read's SMEMs and re-seeds need more
+ * runs again with twice the slots, up to 64 times (bsb_mem_align1_batch and
+ * bsb_align_regs_batch do the same). */
 int bsb_seed_batch(bsb_ctx *ctx, const bsb_seed_opt_t *opt, int32_t n_reads,
                    const uint8_t *seqs, const int64_t *offs,
                    bsb_intv_t *out, int64_t max_out, int64_t *out_off);

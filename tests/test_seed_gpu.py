@@ -126,3 +126,42 @@ def test_occurrence_layouts_give_the_same_seeds_and_sa(gpu_ctx, idx, monkeypatch
             assert np.array_equal(seed.sa_batch(ctx, rows).astype(np.int64), want)
     finally:
         ctx.close()
+
+
+def test_seed_slots_grow_for_reads_with_many_seeds(ctx_idx, idx):
+    """min_seed_len 8 and split_width 3 give some reads more SMEMs and re-seeds than their
+    2*len + 32 seed slots: the batch runs again with more slots per read (seeding and the
+    alignment batch alike), and the seeds and regions equal the oracle's."""
+    bi = index.BwaIndex(idx)
+    pac = bi.pac_codes()
+    rng = np.random.Generator(np.random.PCG64(71))
+    reads = []
+    for k in range(1500):
+        L = int(rng.integers(1, 160))
+        st = int(rng.integers(0, len(pac) - L - 1))
+        r = pac[st:st + L].copy()
+        if k % 2:
+            r = (3 - r[::-1]).astype(np.uint8)
+        e = rng.random(L) < 0.02
+        r[e] = rng.integers(0, 4, int(e.sum()))
+        if k % 5 == 0 and L > 20:
+            p = int(rng.integers(0, L - 5))
+            r[p:p + int(rng.integers(1, 5))] = 4
+        reads.append(r.astype(np.uint8))
+    offs = np.zeros(len(reads) + 1, np.int64)
+    offs[1:] = np.cumsum([len(r) for r in reads])
+    seqs = np.concatenate(reads)
+    ob = oracle.OracleBwt(bi.primary, bi.L2[1:], bi.bwt, bi.sa, bi.sa_intv)
+    got, off = seed.seed_batch(ctx_idx, seqs, offs, min_seed_len=8, split_width=3, max_mem_intv=50)
+    ref, roff = ob.collect_intv(seqs, offs, min_seed_len=8, split_width=3, max_mem_intv=50, n_threads=8)
+    lens = offs[1:] - offs[:-1]
+    assert ((roff[1:] - roff[:-1]) > 1.5 * lens + 24).any(), "no read needs more than its first slots"
+    assert np.array_equal(off, roff) and np.array_equal(got, ref)
+    o = [1, 4, 6, 1, 6, 1, 100, 100, 5, 5, 8, 500, 3, 50, 10000]
+    opt = _lib.AlignOpt.bwa_defaults(min_seed_len=8, split_width=3, max_mem_intv=50)
+    regs, roff2 = seed.align_regs(ctx_idx, seqs, offs, opt)
+    anns = np.array([(a.offset, a.len, 0) for a in bi.anns], dtype=oracle.ANN_DTYPE)
+    want = oracle.align_regs(ob, anns, bi.pac, bi.l_pac, oracle.Opt.from_list(o), seqs, offs, n_threads=8)
+    assert np.array_equal(roff2, want["regs_off"])
+    for f in want["regs"].dtype.names:
+        assert np.array_equal(regs[f], want["regs"][f]), f"reg.{f}"
