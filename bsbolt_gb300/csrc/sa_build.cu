@@ -1,18 +1,18 @@
-// sa_build.cu -- the suffix array of BWA's index text, built on the GPU.
+// sa_build.cu -- the suffixes of BWA's index text, sorted on the GPU.
 //
 // bwa index sorts the suffixes of the forward 2-bit pac followed by its reverse complement
 // (2*l_pac symbols, bntseq.c / bwtindex.c) with a sentinel '$' that sorts before every base;
 // the BWT, the occurrence array and the sampled SA (.bwt, .sa) are read off that order.
 // On the host (host_index.c) an SA-IS with 32-bit indexes does this up to 2^31 symbols and
-// takes minutes per billion; here prefix doubling runs on device radix sorts (CUB, part of
+// takes minutes per billion.  Here prefix doubling runs on device radix sorts (CUB, part of
 // the CUDA toolkit): every suffix is first keyed by its next 21 symbols (3 bits each, 0 past
-// the end), sorted, and given the rank of its group's first row; then each round keys suffix
-// i by (rank[i], rank[i + h]) and sorts again, h = 21, 42, 84, ... until every rank is
-// distinct.  Suffixes whose first h symbols reach the sentinel are already alone in their
-// group, so rank[i + h] past the end can be anything.  Ranks are 32-bit: up to 2^32 - 1
-// suffixes (texts below 2^32 - 1 symbols, references up to ~1.07 Gb converted both ways).
-// Device memory: ~33 bytes per symbol at the peak (two 8-byte key and two 4-byte index
-// buffers of the sort, the rank array, the text), all freed before returning.
+// the end) and sorted; then each round keys suffix i by (rank[i], rank[i + h]) and sorts again,
+// h = 21, 42, 84, ... until every rank is distinct.  Suffixes whose first h symbols reach the
+// sentinel are already alone in their group, so rank[i + h] past the end can be anything.
+//   bsb_build_suffix_array: 32-bit ranks (texts below 2^32 - 1 symbols), all suffixes sorted
+//   together each round, the whole array copied back (~33 bytes of device memory per symbol).
+//   bsb_build_bwt: 64-bit ranks, suffixes sorted in chunks that fit device memory, only the
+//   BWT and the sampled rows copied back (described above the function).
 
 #include <algorithm>
 #include <vector>

@@ -171,9 +171,9 @@ int bsb_index_load(bsb_ctx *ctx, const char *prefix);
 /* Suffix array of the text bwa index sorts -- the 2-bit pac of l_pac bases, then its
  * reverse complement, then the '$' that sorts first (bwtindex.c; is.c / bwt_gen.c) -- sorted on
  * the GPU by prefix doubling over device radix sorts: sa[r] for r = 0 .. 2*l_pac (host buffer
- * of 2*l_pac + 1 int64).  The host's .bwt / .sa writer turns it into BWA's files
- * (bsbolt_gb300.index.build_index with a context).  Up to 2*l_pac + 1 <= 2^32 - 1 suffixes
- * (BSB_ETOOLONG beyond); takes ~33 bytes of device memory per text symbol, freed on return.
+ * of 2*l_pac + 1 int64), for the host's .bwt / .sa writer (bsbh_write_bwt_sa64).  Up to
+ * 2*l_pac + 1 <= 2^32 - 1 suffixes (BSB_ETOOLONG beyond); takes ~33 bytes of device memory
+ * per text symbol, freed on return.
  * No reference counterpart: bwa index sorts on the CPU. */
 int bsb_build_suffix_array(bsb_ctx *ctx, const uint8_t *pac, int64_t l_pac, int64_t *sa);
 
