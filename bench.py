@@ -17,12 +17,17 @@ roofline = integer pipe: 14 int ops per reference cell against the measured
          add+max throughput of this GPU for the cell width the dominant kernel
          computes in (bsb_probe_int16x2_peak for the 16-bit two-cells-per-register
          kernels of even-C shapes, bsb_probe_int_peak for the 32-bit ones).
-cpu_baseline = the CPU port of ksw_extend2 (oracle/) on a bounded sample,
-         all host cores.
+cpu_baseline = the reference's own ksw_extend2, compiled from BSBolt's sources
+         (oracle/_ref/libref_ksw.so), on a bounded sample, all host cores.
 
---impl reference: the CPU implementation of the path timed on the host cores
-(the reference's own sources cannot be built on the GPU machine, so this is the
-oracle port of ksw.c:380-479, which is bit-exact to it by tests/golden/).
+--impl reference: the same reference ksw_extend2 timed on the host cores over
+the workload, all cores (the oracle port of ksw.c:380-479 when the reference
+sources were not staged).
+Further blocks of the same JSON line (each skippable): the seeds -> regions
+pass on a 2 Mb, a 100 Mb (PE and RRBS-like) and the 3.1 Gb human-scale
+reference (index sorted on the GPU), the learned job and read orders, the tile
+autotuner, bwa_gen_cigar2, mate rescue, and stock bwa mem against bwa_gpu mem
+from SAM.
 Multi-GPU: replicas only -- every rank extends its own 4M-job batch.
 """
 from __future__ import annotations
@@ -1334,7 +1339,7 @@ def run_ours(args, ws, rank, local):
             big1g = pipeline_ref1gb(ctx, n_pairs=args.ref1gb_pairs)
         except Exception as e:   # reported, never hidden
             big1g = {"error": f"{type(e).__name__}: {e}"}
-    if rank == 0 and args.ref3gb:
+    if rank == 0 and not args.no_ref3gb:
         try:
             big3g = pipeline_ref1gb(ctx, n_pairs=args.ref3gb_pairs, tag="3gb", learned=not args.no_learned)
         except Exception as e:   # reported, never hidden
@@ -1457,9 +1462,9 @@ def main():
     ap.add_argument("--ref1gb", action="store_true",
                     help="add the 1 Gb-reference block (index sorted on the GPU; a few minutes to build)")
     ap.add_argument("--ref1gb-pairs", type=int, default=200_000)
-    ap.add_argument("--ref3gb", action="store_true",
-                    help="add the 3.1 Gb human-scale block (24 contigs, 45%% repeats; the index is sorted on the "
-                         "GPU with 64-bit ranks: ~10 min and ~200 GB of device memory the first time)")
+    ap.add_argument("--no-ref3gb", action="store_true",
+                    help="skip the 3.1 Gb human-scale block (24 contigs, 45%% repeats; the index is sorted on "
+                         "the GPU with 64-bit ranks: ~3 min and ~200 GB of device memory the first time)")
     ap.add_argument("--ref3gb-pairs", type=int, default=200_000)
     ap.add_argument("--sam-pairs", type=int, default=500_000,
                     help="2x150 pairs of the SAM block on the 100 Mb reference (the full workload is 4M)")
