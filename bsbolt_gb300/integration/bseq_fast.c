@@ -235,6 +235,36 @@ static void fq_alloc1(fq_build_t *B, int64_t i)
     s->oseq = B->conversion ? (char *)malloc((size_t)r->seq_l + 1) : 0;
 }
 
+/* With the native output step (sam_out.c), the batch's names, bases, qualities and original
+ * bases are carved from one block, the first read's name at its start, which the output step
+ * frees at once (sam_out_take_block); comments stay separate, since mem's input step frees
+ * them itself unless -C (fastmap.c:26-30).  0 when the block cannot be had. */
+static int fq_alloc_block(fq_build_t *B)
+{
+    size_t total = 0;
+    int64_t i;
+    char *p;
+    for (i = 0; i < B->n; ++i) {
+        const fq_entry_t *e = &B->ent[i];
+        const int l = B->rec[e->stream][e->rec].seq_l;
+        total += (size_t)e->name_l + 1 + (size_t)l + 1 + (l ? (size_t)l + 1 : 0) + (B->conversion ? (size_t)l + 1 : 0);
+    }
+    if (B->n == 0 || !(p = (char *)malloc(total))) return 0;
+    for (i = 0; i < B->n; ++i) {
+        const fq_entry_t *e = &B->ent[i];
+        const fq_rec_t *r = &B->rec[e->stream][e->rec];
+        bseq1_t *s = &B->seqs[i];
+        memset(s, 0, sizeof *s);
+        s->name = p, p += e->name_l + 1;
+        s->seq = p, p += r->seq_l + 1;
+        if (r->seq_l) s->qual = p, p += r->seq_l + 1;
+        if (B->conversion) s->oseq = p, p += r->seq_l + 1;
+        s->comment = r->cmt_l ? (char *)malloc((size_t)r->cmt_l + 1) : 0;
+    }
+    sam_out_give_block(B->seqs[0].name);
+    return 1;
+}
+
 static void fq_copy(char *d, const char *src, int l)
 {
     memcpy(d, src, (size_t)l);
@@ -413,7 +443,7 @@ bseq1_t *bseq_read_fast(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int
     if (!seqs) goto undo;
     B.st[0] = st1, B.st[1] = st2, B.rec[0] = v1.a, B.rec[1] = v2.a, B.ent = ent, B.seqs = seqs;
     B.conversion = conversion, B.next = 0, B.n = n;
-    {
+    if (!sam_out_enabled() || !fq_alloc_block(&B)) {
         int64_t i;
         for (i = 0; i < n; ++i) fq_alloc1(&B, i);
     }

@@ -81,6 +81,11 @@ int sam_out_enabled(void);
 void sam_out_begin(bseq1_t *first);
 void sam_out_read(bseq1_t *read);
 void sam_out_end(void);
+/* the output step's time by part, one line (BSB_GPU_STATS) */
+void sam_out_report(FILE *fp);
+/* bseq_read_fast hands over a batch whose read strings (but comments) are one block starting at
+ * the first read's name; sam_out_end frees it at once */
+void sam_out_give_block(void *block);
 
 #ifdef __cplusplus
 }

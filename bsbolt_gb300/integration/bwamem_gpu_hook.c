@@ -98,6 +98,7 @@ static void hook_report(void)
             g_t_start > 0 ? hook_now() - g_t_start : 0.);
     fprintf(stderr, "[bsb_gpu] host steps: reading and converting the reads %.3f s, SAM output %.3f s "
             "(each beside the other steps of the pipeline)\n", g_t_read, g_t_write);
+    if (sam_out_enabled()) sam_out_report(stderr);
     if (g_t_first_read > 0.)
         fprintf(stderr, "[bsb_gpu] timeline: load to first read %.3f s, first read to last SAM output %.3f s "
                 "(alignment steps %.3f s of it), last output to exit %.3f s (pipeline end %.3f s after it, "

@@ -10,7 +10,8 @@
  * counted as bisulfite-ambiguous (setUnmapped, bs_sorter.cpp:51-82).  Each written read is
  * counted by its mapping class; the other queue is dropped.  Here the same decisions are made
  * in one pass over the reads (it is sequential, and cheap), then the records are measured and
- * copied into one buffer on threads and written with one fwrite, and the reads' strings are
+ * copied into one buffer on threads, each record freed by the thread that copied it (worker2's
+ * threads allocated them), the buffer written with one fwrite, and the reads' other strings
  * freed on the calling thread (the pipeline thread that read the batch allocated them).
  *
  * The hook links this in place of the samSorter calls (-Wl,--wrap=new_samSorter,
@@ -22,6 +23,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include <unistd.h>
 
 #include "bwa.h"
@@ -34,6 +36,36 @@ typedef struct {
 } so_batch_t;
 
 static so_batch_t g_so;      /* kt_pipeline runs one output step at a time */
+
+/* Blocks holding a whole batch's read strings (bseq_fast.c), by their first read's name: at most
+ * the pipeline's batches in flight. */
+#define SO_BLOCKS 16
+static void *g_blocks[SO_BLOCKS];
+static pthread_mutex_t g_blocks_mu = PTHREAD_MUTEX_INITIALIZER;
+
+void sam_out_give_block(void *block)
+{
+    int k;
+    pthread_mutex_lock(&g_blocks_mu);
+    for (k = 0; k < SO_BLOCKS && g_blocks[k]; ++k) {}
+    if (k < SO_BLOCKS) g_blocks[k] = block;
+    pthread_mutex_unlock(&g_blocks_mu);
+    if (k == SO_BLOCKS) {                  /* more batches in flight than the pipeline starts */
+        fprintf(stderr, "[sam_out] too many read batches in flight\n");
+        abort();
+    }
+}
+
+/* 1 (and the entry dropped) when the batch whose first read's name is at p was one block */
+static int so_take_block(void *p)
+{
+    int k, found = 0;
+    pthread_mutex_lock(&g_blocks_mu);
+    for (k = 0; k < SO_BLOCKS; ++k)
+        if (p && g_blocks[k] == p) g_blocks[k] = 0, found = 1;
+    pthread_mutex_unlock(&g_blocks_mu);
+    return found;
+}
 
 int sam_out_enabled(void)
 {
@@ -99,8 +131,24 @@ typedef struct {
     size_t *off;             /* byte offset of each record (off[n] = total) */
     char *buf;
     int64_t n, next;
-    int phase;               /* 0: rewrite and measure, 1: copy */
+    int phase;               /* 0: rewrite and measure, 1: copy (and free the record) */
 } so_write_t;
+
+/* seconds in each part of the output step, for BSB_GPU_STATS (sam_out_report) */
+static double g_so_t[5];     /* decisions, measuring, copying, writing, freeing */
+
+static double so_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + ts.tv_nsec * 1e-9;
+}
+
+void sam_out_report(FILE *fp)
+{
+    fprintf(fp, "[bsb_gpu] SAM output step: decisions %.3f s, measuring %.3f s, copying %.3f s, writing %.3f s, "
+            "freeing the reads %.3f s\n", g_so_t[0], g_so_t[1], g_so_t[2], g_so_t[3], g_so_t[4]);
+}
 
 static void *so_worker(void *arg)
 {
@@ -117,8 +165,10 @@ static void *so_worker(void *arg)
                     r->sam = so_unmapped(r);
                 }
                 W->off[i] = r->sam ? strlen(r->sam) : 0;
-            } else if (W->off[i + 1] > W->off[i]) {
-                memcpy(W->buf + W->off[i], r->sam, W->off[i + 1] - W->off[i]);
+            } else {
+                if (W->off[i + 1] > W->off[i]) memcpy(W->buf + W->off[i], r->sam, W->off[i + 1] - W->off[i]);
+                free(r->sam);        /* allocated by worker2's threads: freed here, in parallel */
+                r->sam = 0;
             }
         }
     }
@@ -167,6 +217,7 @@ void sam_out_end(void)
         fprintf(stderr, "[sam_out] out of memory\n");
         abort();
     }
+    double t0 = so_now(), t1;
     /* one pass: groups of consecutive reads with one name (processRead, bs_sorter.cpp:37-51) */
     for (i = 0; i < g_so.n;) {
         const char *name = g_so.r[i]->name;
@@ -202,7 +253,9 @@ void sam_out_end(void)
         i = k;
     }
     W.n = n_out;
+    t1 = so_now(), g_so_t[0] += t1 - t0, t0 = t1;
     so_parallel(&W, 0);
+    t1 = so_now(), g_so_t[1] += t1 - t0, t0 = t1;
     {
         size_t acc = 0, len;
         for (i = 0; i < n_out; ++i) len = W.off[i], W.off[i] = acc, acc += len;
@@ -213,10 +266,12 @@ void sam_out_end(void)
             abort();
         }
         so_parallel(&W, 1);
+        t1 = so_now(), g_so_t[2] += t1 - t0, t0 = t1;
         if (acc && fwrite(W.buf, 1, acc, stdout) != acc) {
             fprintf(stderr, "[sam_out] write error\n");
             exit(1);
         }
+        t1 = so_now(), g_so_t[3] += t1 - t0, t0 = t1;
     }
     /* the reference prints the batch's counts from processEnd (bs_sorter_wrapper.cpp) */
     fprintf(stderr, "BSStat TotalReads: %d\n", reads_observed);
@@ -227,8 +282,19 @@ void sam_out_end(void)
     fprintf(stderr, "BSStat C_G2A: %d\n", cg2a);
     fprintf(stderr, "BSStat Unaligned: %d\n", unaligned);
     fprintf(stderr, "BSStat BSAmbiguous: %d\n", bs_ambiguous);
-    for (i = 0; i < g_so.n; ++i) so_free_read(g_so.r[i]);
+    if (g_so.n && so_take_block(g_so.r[0]->name)) {    /* the batch's strings are one block */
+        void *block = g_so.r[0]->name;
+        for (i = 0; i < g_so.n; ++i) {
+            bseq1_t *r = g_so.r[i];
+            free(r->comment); free(r->sam);
+            r->name = r->comment = r->seq = r->qual = r->sam = r->oseq = 0;
+        }
+        free(block);
+    } else {
+        for (i = 0; i < g_so.n; ++i) so_free_read(g_so.r[i]);
+    }
     free(W.buf); free(W.out); free(W.unmapped); free(W.off); free(g1); free(g2);
+    g_so_t[4] += so_now() - t0;
     g_so.n = 0;
     g_so.active = 0;
 }
