@@ -266,3 +266,14 @@ def test_glue_output_step_bsstat_matches_samsorter(pe, mode):
     assert ref and glue == ref
     if mode == "se_undirectional":
         assert ref["BSAmbiguous:"] > 0
+
+
+def test_glue_reads_string_by_string(pe):
+    """With BSB_SAM_WRITER=0 the FASTQ reader allocates every read's strings one by one (the
+    reference's samSorter frees them so); the glue's output step then frees them one by one as
+    well, in many small batches, and the SAM is the stock one."""
+    fa, r1, r2 = pe[:3]
+    extra = ["-L", "5,5", "-K", "50000"]
+    ref = sam_sets.run_mem(BWA, fa, [r1, r2], extra)
+    glue = sam_sets.run_mem(GLUE, fa, [r1, r2], extra, env=dict(os.environ, BSB_SAM_WRITER="0"))
+    assert len(ref) >= 3000 and glue == ref
