@@ -11,7 +11,8 @@
  * over several lines, CR or NUL bytes, an empty sequence line, bytes before a header, a last
  * record without its newline -- hands the unread bytes back to the kstream and calls the
  * reference's own bseq_read, for that batch and every later one.  BSB_FASTQ_READER=0 keeps
- * the reference's reader throughout.
+ * the reference's reader throughout.  With the native output step (sam_out.c) a batch's names,
+ * bases, qualities and original bases are one allocation, which that step frees at once.
  *
  * Link with -Wl,--wrap=bseq_read and call bseq_read_fast from __wrap_bseq_read.
  */

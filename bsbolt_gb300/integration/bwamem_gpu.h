@@ -76,7 +76,8 @@ bseq1_t *bseq_read_fast(int64_t chunk_size, int *n_, void *ks1_, void *ks2_, int
 /* The output step of fastmap.c:process (samSorter, bs_sorter.cpp) with the same stdout bytes and
  * BSStat lines, records copied on threads and written once per batch (sam_out.c):
  * sam_out_begin(first read), sam_out_read per further read with a record, sam_out_end writes,
- * prints and frees.  sam_out_enabled: 0 when BSB_SAM_WRITER=0. */
+ * prints and frees (the records on the copying threads, a batch of read strings from
+ * bseq_read_fast at once).  sam_out_enabled: 0 when BSB_SAM_WRITER=0. */
 int sam_out_enabled(void);
 void sam_out_begin(bseq1_t *first);
 void sam_out_read(bseq1_t *read);
